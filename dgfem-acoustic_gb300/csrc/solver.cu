@@ -1,0 +1,565 @@
+// C ABI of the GPU RK4 right-hand side (include/dgcuda.h): context creation
+// (device layout of the reference Mesh arrays), state transfer, sources, the
+// step loop (CUDA graphs of step chunks), per-kernel timing and monitors.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/dgcuda.h"
+#include "host/capi_common.h"
+#include "host/layout.h"
+#include "host/refel.h"
+#include "kernels.h"
+#include "stage_kernel.cuh"
+
+using dg::fail;
+
+namespace dgk {
+bool get_kernels(int prec, int dim, int order, KernelSet *out) {
+    if (prec == DG_PREC_FP64) return dim == 2 ? kernels_f64_2d(order, out) : kernels_f64_3d(order, out);
+    return dim == 2 ? kernels_f32_2d(order, out) : kernels_f32_3d(order, out);
+}
+}  // namespace dgk
+
+namespace {
+
+const int kGraphChunk = 32;
+
+template <typename Real>
+__global__ void cast_kernel(const double *src, Real *dst, long long n) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; i < n; i += (long long)gridDim.x * blockDim.x) dst[i] = Real(src[i]);
+}
+template <typename Real>
+__global__ void uncast_kernel(const Real *src, double *dst, long long n) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; i < n; i += (long long)gridDim.x * blockDim.x) dst[i] = double(src[i]);
+}
+
+// FP64 monitors: thread per element, u^T M u per field, non-finite count.
+template <typename Real>
+__global__ void monitor_kernel(const Real *u, long long fstride, int K, int np, int nq, const double *mass,
+                               const double *detj, double rho, double c0, double *out /*[2+nq]*/,
+                               unsigned long long *bad) {
+    __shared__ double red[256][5];
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double loc[5] = {0, 0, 0, 0, 0};
+    unsigned long long nbad = 0;
+    if (e < K) {
+        for (int f = 0; f < nq; ++f) {
+            const Real *q = u + f * fstride + (long long)e * np;
+            double s = 0;
+            for (int i = 0; i < np; ++i) {
+                double qi = double(q[i]);
+                if (!isfinite(qi)) ++nbad;
+                double t = 0;
+                for (int j = 0; j < np; ++j) t += mass[i * np + j] * double(q[j]);
+                s += qi * t;
+            }
+            loc[1 + f] = s * detj[e];
+        }
+        double en = loc[1] / (rho * c0 * c0);
+        for (int f = 1; f < nq; ++f) en += rho * loc[1 + f];
+        loc[0] = 0.5 * en;
+    }
+    for (int k = 0; k < 5; ++k) red[threadIdx.x][k] = loc[k];
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int k = 0; k < 5; ++k) red[threadIdx.x][k] += red[threadIdx.x + s][k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 1 + nq; ++k) atomicAdd(&out[k], red[0][k]);
+    if (nbad) atomicAdd(bad, nbad);
+}
+
+}  // namespace
+
+struct dg_ctx {
+    int dim = 0, order = 0, np = 0, nf = 0, nfp = 0, nq = 0, K = 0;
+    long long ndof = 0;  // K * np
+    int prec = 0, flux_sign = 0, device = 0, use_graph = 1;
+    size_t rsize = 8;
+    double c0 = 1, rho0 = 1, v0[3] = {0, 0, 0};
+    cudaStream_t stream = nullptr;
+    char *d_state = nullptr;  // u, acc, wa, wb
+    void *d_u = nullptr, *d_acc = nullptr, *d_wa = nullptr, *d_wb = nullptr;
+    double *d_geo = nullptr;
+    void *d_fgeo = nullptr;
+    int2 *d_conn = nullptr;
+    void *d_ops = nullptr;
+    uint8_t *d_tabs = nullptr;
+    double *d_t0 = nullptr;
+    double *d_stage64 = nullptr;  // FP64 staging (FP32 contexts)
+    double *d_mass = nullptr, *d_detj = nullptr, *d_mon = nullptr;
+    unsigned long long *d_bad = nullptr;
+    // sources
+    int src_nodes = 0;
+    int *d_src_dof = nullptr, *d_src_off = nullptr, *d_src_list = nullptr;
+    double *d_src_params = nullptr;
+    std::vector<double> src_duration;
+    dgk::KernelSet ks;
+    int grid = 0;
+    // graph cache
+    cudaGraphExec_t gexec = nullptr;
+    double graph_dt = 0;
+    int graph_src = -1;
+    // events for profiling
+    std::vector<cudaEvent_t> events;
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char *what) {
+    return fail(DG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(call)                                             \
+    do {                                                     \
+        cudaError_t _e = (call);                             \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call);  \
+    } while (0)
+
+void free_ctx(dg_ctx *c) {
+    if (!c) return;
+    if (c->device >= 0) cudaSetDevice(c->device);
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    for (auto ev : c->events) cudaEventDestroy(ev);
+    void *ptrs[] = {c->d_state, c->d_geo, c->d_fgeo, c->d_conn, c->d_ops, c->d_tabs, c->d_t0, c->d_stage64,
+                    c->d_mass, c->d_detj, c->d_mon, c->d_bad, c->d_src_dof, c->d_src_off, c->d_src_list,
+                    c->d_src_params};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+template <typename Real>
+void fill_args(dg_ctx *c, dgk::StageArgs<Real> &a, int stage, double dt) {
+    a.fstride = c->ndof;
+    a.bstride = 0;
+    a.geo = c->d_geo;
+    a.fgeo = reinterpret_cast<const Real *>(c->d_fgeo);
+    a.conn = c->d_conn;
+    a.ops = reinterpret_cast<const Real *>(c->d_ops);
+    a.tabs = c->d_tabs;
+    a.K = c->K;
+    a.dt = Real(dt);
+    a.rc2 = Real(c->rho0 * c->c0 * c->c0);
+    a.inv_rho = Real(1.0 / c->rho0);
+    a.half_c0 = Real(0.5 * c->c0);
+    a.c0 = Real(c->c0);
+    a.rho = Real(c->rho0);
+    for (int k = 0; k < 3; ++k) a.v0[k] = Real(c->v0[k]);
+    Real *u = (Real *)c->d_u, *acc = (Real *)c->d_acc, *wa = (Real *)c->d_wa, *wb = (Real *)c->d_wb;
+    a.u = u;
+    a.acc = acc;
+    switch (stage) {
+        case 0: a.win = u; a.wout = wa; break;
+        case 1: a.win = wa; a.wout = wb; break;
+        case 2: a.win = wb; a.wout = wa; break;
+        default: a.win = wa; a.wout = u; break;
+    }
+}
+
+cudaError_t launch_stage(dg_ctx *c, int stage, double dt) {
+    dim3 grid(c->grid, 1, 1), block(c->ks.threads, 1, 1);
+    if (c->prec == DG_PREC_FP64) {
+        dgk::StageArgs<double> a;
+        fill_args<double>(c, a, stage, dt);
+        void *args[] = {&a};
+        return cudaLaunchKernel(c->ks.stage[stage], grid, block, args, c->ks.smem, c->stream);
+    } else {
+        dgk::StageArgs<float> a;
+        fill_args<float>(c, a, stage, dt);
+        void *args[] = {&a};
+        return cudaLaunchKernel(c->ks.stage[stage], grid, block, args, c->ks.smem, c->stream);
+    }
+}
+
+cudaError_t launch_inject(dg_ctx *c, int kstep, double dt) {
+    if (!c->src_nodes) return cudaSuccess;
+    dim3 grid((c->src_nodes + 127) / 128, 1, 1), block(128, 1, 1);
+    long long bstride = 0;
+    void *p = c->d_u;  // field 0 of u
+    int nn = c->src_nodes;
+    void *args[] = {&p, &bstride, &c->d_src_dof, &c->d_src_off, &c->d_src_list, &c->d_src_params, &c->d_t0,
+                    &kstep, &dt, &nn};
+    return cudaLaunchKernel(c->ks.inject, grid, block, args, 0, c->stream);
+}
+
+cudaError_t launch_step(dg_ctx *c, int kstep, double dt) {
+    cudaError_t e = launch_inject(c, kstep, dt);
+    for (int s = 0; s < 4 && e == cudaSuccess; ++s) e = launch_stage(c, s, dt);
+    return e;
+}
+
+bool any_source_active(dg_ctx *c, double t) {
+    for (double d : c->src_duration)
+        if (t < d) return true;
+    return false;
+}
+
+}  // namespace
+
+extern "C" {
+
+void dg_default_opts(dg_opts *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->precision = DG_PREC_FP64;
+    o->flux_sign = DG_FLUX_REFERENCE;
+    o->device = 0;
+    o->use_graph = 1;
+}
+
+int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts_in, dg_ctx **out) {
+    if (!m || !ph || !out) return fail(DG_ERR_ARG, "null argument");
+    *out = nullptr;
+    dg_opts opts;
+    if (opts_in) opts = *opts_in;
+    else dg_default_opts(&opts);
+    if (m->dim != 2 && m->dim != 3) return fail(DG_ERR_UNSUPPORTED, "dimension must be 2 or 3");
+    if (m->order < 1 || m->order > 5) return fail(DG_ERR_UNSUPPORTED, "order must be in 1..5");
+    if (opts.precision != DG_PREC_FP64 && opts.precision != DG_PREC_FP32)
+        return fail(DG_ERR_ARG, "unknown precision");
+    if (opts.flux_sign != DG_FLUX_REFERENCE && opts.flux_sign != DG_FLUX_UPWIND)
+        return fail(DG_ERR_ARG, "unknown flux sign mode");
+    if (!(ph->c0 > 0) || !(ph->rho0 > 0)) return fail(DG_ERR_ARG, "c0 and rho0 must be positive");
+    dg::Layout lay;
+    {
+        std::string err;
+        try {
+            err = dg::build_layout(*m, opts.flux_sign, lay);
+        } catch (std::exception &e) {
+            err = e.what();
+        }
+        if (!err.empty()) return fail(DG_ERR_MESH, err);
+    }
+    const int dim = lay.dim, np = lay.np, nf = lay.nf, nfp = lay.nfp, K = lay.K;
+    (void)nf; (void)nfp;
+    dg_ctx *c = new dg_ctx();
+    c->dim = dim; c->order = m->order; c->np = np; c->nf = nf; c->nfp = nfp; c->nq = dim + 1; c->K = K;
+    c->ndof = (long long)K * np;
+    c->prec = opts.precision; c->flux_sign = opts.flux_sign; c->device = opts.device; c->use_graph = opts.use_graph;
+    c->rsize = c->prec == DG_PREC_FP64 ? 8 : 4;
+    c->c0 = ph->c0; c->rho0 = ph->rho0;
+    for (int k = 0; k < 3; ++k) c->v0[k] = ph->v0[k];
+    if (!dgk::get_kernels(c->prec, dim, m->order, &c->ks)) {
+        free_ctx(c);
+        return fail(DG_ERR_UNSUPPORTED, "no kernel compiled for this order");
+    }
+    int rc = DG_OK;
+    auto fin = [&](cudaError_t e, const char *what) {
+        if (e != cudaSuccess && rc == DG_OK) rc = cuda_fail(e, what);
+        return e == cudaSuccess;
+    };
+    do {
+        if (!fin(cudaSetDevice(c->device), "cudaSetDevice")) break;
+        if (!fin(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate")) break;
+        size_t field_bytes = (size_t)c->ndof * c->rsize;
+        size_t state_bytes = field_bytes * c->nq;
+        if (!fin(cudaMalloc(&c->d_state, 4 * state_bytes), "cudaMalloc(state)")) break;
+        c->d_u = c->d_state;
+        c->d_acc = c->d_state + state_bytes;
+        c->d_wa = c->d_state + 2 * state_bytes;
+        c->d_wb = c->d_state + 3 * state_bytes;
+        if (!fin(cudaMemsetAsync(c->d_state, 0, 4 * state_bytes, c->stream), "cudaMemset")) break;
+        if (!fin(cudaMalloc(&c->d_geo, lay.geo.size() * 8), "cudaMalloc(geo)")) break;
+        if (!fin(cudaMemcpy(c->d_geo, lay.geo.data(), lay.geo.size() * 8, cudaMemcpyHostToDevice), "copy geo"))
+            break;
+        auto upload_real = [&](const std::vector<double> &v, void **dst) -> bool {
+            if (!fin(cudaMalloc(dst, v.size() * c->rsize), "cudaMalloc")) return false;
+            if (c->prec == DG_PREC_FP64)
+                return fin(cudaMemcpy(*dst, v.data(), v.size() * 8, cudaMemcpyHostToDevice), "copy");
+            std::vector<float> f(v.begin(), v.end());
+            return fin(cudaMemcpy(*dst, f.data(), f.size() * 4, cudaMemcpyHostToDevice), "copy");
+        };
+        if (!upload_real(lay.fgeo, &c->d_fgeo)) break;
+        if (!upload_real(lay.ops, &c->d_ops)) break;
+        if (!fin(cudaMalloc(&c->d_conn, lay.conn.size() * sizeof(int)), "cudaMalloc(conn)")) break;
+        if (!fin(cudaMemcpy(c->d_conn, lay.conn.data(), lay.conn.size() * sizeof(int), cudaMemcpyHostToDevice),
+                 "copy conn"))
+            break;
+        if (!fin(cudaMalloc(&c->d_tabs, lay.tabs.size()), "cudaMalloc(tabs)")) break;
+        if (!fin(cudaMemcpy(c->d_tabs, lay.tabs.data(), lay.tabs.size(), cudaMemcpyHostToDevice), "copy tabs"))
+            break;
+        if (!fin(cudaMalloc(&c->d_t0, 8), "cudaMalloc(t0)")) break;
+        if (!fin(cudaMalloc(&c->d_mass, (size_t)np * np * 8), "cudaMalloc(mass)")) break;
+        if (!fin(cudaMemcpy(c->d_mass, lay.mass.data(), (size_t)np * np * 8, cudaMemcpyHostToDevice), "copy mass"))
+            break;
+        if (!fin(cudaMalloc(&c->d_detj, (size_t)K * 8), "cudaMalloc(detj)")) break;
+        if (!fin(cudaMemcpy(c->d_detj, lay.detj.data(), (size_t)K * 8, cudaMemcpyHostToDevice), "copy detj"))
+            break;
+        if (!fin(cudaMalloc(&c->d_mon, 8 * 8), "cudaMalloc(mon)")) break;
+        if (!fin(cudaMalloc(&c->d_bad, 8), "cudaMalloc(bad)")) break;
+        if (c->prec != DG_PREC_FP64)
+            if (!fin(cudaMalloc(&c->d_stage64, (size_t)c->ndof * 8), "cudaMalloc(staging)")) break;
+        for (int s = 0; s < 4; ++s)
+            if (!fin(cudaFuncSetAttribute(c->ks.stage[s], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)c->ks.smem),
+                     "cudaFuncSetAttribute"))
+                break;
+        if (rc != DG_OK) break;
+        int per_sm = 0, nsm = 0;
+        if (!fin(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c->ks.stage[0], c->ks.threads, c->ks.smem),
+                 "occupancy"))
+            break;
+        if (!fin(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device), "attribute")) break;
+        int ntiles = (K + c->ks.epb - 1) / c->ks.epb;
+        c->grid = std::max(1, std::min(ntiles, std::max(per_sm, 1) * nsm));
+        if (!fin(cudaStreamSynchronize(c->stream), "sync")) break;
+    } while (0);
+    if (rc != DG_OK) {
+        free_ctx(c);
+        return rc;
+    }
+    *out = c;
+    return DG_OK;
+}
+
+void dg_destroy(dg_ctx *c) { free_ctx(c); }
+
+int dg_set_state(dg_ctx *c, const double *const u[4]) {
+    if (!c || !u) return fail(DG_ERR_ARG, "null argument");
+    for (int f = 0; f < c->nq; ++f)
+        if (!u[f]) return fail(DG_ERR_ARG, "null field");
+    if (c->dim == 2 && u[3]) {
+        for (long long i = 0; i < c->ndof; ++i)
+            if (u[3][i] != 0.0) return fail(DG_ERR_UNSUPPORTED, "2D meshes carry vz == 0; got a nonzero vz");
+    }
+    CK(cudaSetDevice(c->device));
+    size_t fb = (size_t)c->ndof * c->rsize;
+    for (int f = 0; f < c->nq; ++f) {
+        char *dst = (char *)c->d_u + f * fb;
+        if (c->prec == DG_PREC_FP64) {
+            CK(cudaMemcpyAsync(dst, u[f], fb, cudaMemcpyHostToDevice, c->stream));
+        } else {
+            CK(cudaMemcpyAsync(c->d_stage64, u[f], (size_t)c->ndof * 8, cudaMemcpyHostToDevice, c->stream));
+            cast_kernel<float><<<1024, 256, 0, c->stream>>>(c->d_stage64, (float *)dst, c->ndof);
+            CK(cudaGetLastError());
+        }
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_get_state(dg_ctx *c, double *const u[4]) {
+    if (!c || !u) return fail(DG_ERR_ARG, "null argument");
+    CK(cudaSetDevice(c->device));
+    size_t fb = (size_t)c->ndof * c->rsize;
+    for (int f = 0; f < c->nq; ++f) {
+        if (!u[f]) continue;
+        const char *src = (const char *)c->d_u + f * fb;
+        if (c->prec == DG_PREC_FP64) {
+            CK(cudaMemcpyAsync(u[f], src, fb, cudaMemcpyDeviceToHost, c->stream));
+        } else {
+            uncast_kernel<float><<<1024, 256, 0, c->stream>>>((const float *)src, c->d_stage64, c->ndof);
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(u[f], c->d_stage64, (size_t)c->ndof * 8, cudaMemcpyDeviceToHost, c->stream));
+        }
+    }
+    if (c->dim == 2 && u[3]) std::memset(u[3], 0, (size_t)c->ndof * 8);
+    CK(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_set_sources(dg_ctx *c, int nsrc, const int *offsets, const int *dof_idx, const double *params) {
+    if (!c || nsrc < 0 || (nsrc > 0 && (!offsets || !params))) return fail(DG_ERR_ARG, "bad source arguments");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int *p : {c->d_src_dof, c->d_src_off, c->d_src_list})
+        if (p) cudaFree(p);
+    if (c->d_src_params) cudaFree(c->d_src_params);
+    c->d_src_dof = c->d_src_off = c->d_src_list = nullptr;
+    c->d_src_params = nullptr;
+    c->src_nodes = 0;
+    c->src_duration.clear();
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+    if (nsrc == 0) return DG_OK;
+    std::map<int, std::vector<int>> per_dof;  // dof -> sources in order
+    for (int s = 0; s < nsrc; ++s) {
+        if (offsets[s + 1] < offsets[s]) return fail(DG_ERR_ARG, "source offsets must be non-decreasing");
+        for (int k = offsets[s]; k < offsets[s + 1]; ++k) {
+            int d = dof_idx[k];
+            if (d < 0 || d >= c->ndof) return fail(DG_ERR_ARG, "source node index out of range");
+            per_dof[d].push_back(s);
+        }
+        c->src_duration.push_back(params[s * 4 + 3]);
+    }
+    std::vector<int> dofs, off(1, 0), lst;
+    for (auto &kv : per_dof) {
+        dofs.push_back(kv.first);
+        lst.insert(lst.end(), kv.second.begin(), kv.second.end());
+        off.push_back((int)lst.size());
+    }
+    c->src_nodes = (int)dofs.size();
+    if (!c->src_nodes) return DG_OK;
+    CK(cudaMalloc(&c->d_src_dof, dofs.size() * 4));
+    CK(cudaMalloc(&c->d_src_off, off.size() * 4));
+    CK(cudaMalloc(&c->d_src_list, lst.size() * 4));
+    CK(cudaMalloc(&c->d_src_params, (size_t)nsrc * 4 * 8));
+    CK(cudaMemcpy(c->d_src_dof, dofs.data(), dofs.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->d_src_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->d_src_list, lst.data(), lst.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->d_src_params, params, (size_t)nsrc * 4 * 8, cudaMemcpyHostToDevice));
+    return DG_OK;
+}
+
+int dg_rk4_steps(dg_ctx *c, double *t, double dt, int nsteps) {
+    if (!c || !t || nsteps < 0) return fail(DG_ERR_ARG, "bad step arguments");
+    if (!(dt > 0) || !std::isfinite(dt)) return fail(DG_ERR_ARG, "dt must be positive and finite");
+    CK(cudaSetDevice(c->device));
+    int done = 0;
+    while (done < nsteps) {
+        int m = std::min(kGraphChunk, nsteps - done);
+        double t0 = *t;
+        // the chunk's source activity decides whether injection is launched
+        double tend = t0;
+        for (int k = 0; k < m; ++k) tend += dt;
+        int with_src = (c->src_nodes && any_source_active(c, t0)) ? 1 : 0;
+        CK(cudaMemcpyAsync(c->d_t0, &t0, 8, cudaMemcpyHostToDevice, c->stream));
+        if (c->use_graph && m == kGraphChunk) {
+            if (!c->gexec || c->graph_dt != dt || c->graph_src != with_src) {
+                if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+                cudaError_t e = cudaSuccess;
+                int saved = c->src_nodes;
+                if (!with_src) c->src_nodes = 0;
+                for (int k = 0; k < m && e == cudaSuccess; ++k) e = launch_step(c, k, dt);
+                c->src_nodes = saved;
+                cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+                if (e != cudaSuccess) return cuda_fail(e, "launch during capture");
+                if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+                e = cudaGraphInstantiate(&c->gexec, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+                c->graph_dt = dt;
+                c->graph_src = with_src;
+            }
+            CK(cudaGraphLaunch(c->gexec, c->stream));
+        } else {
+            int saved = c->src_nodes;
+            if (!with_src) c->src_nodes = 0;
+            cudaError_t e = cudaSuccess;
+            for (int k = 0; k < m && e == cudaSuccess; ++k) e = launch_step(c, k, dt);
+            c->src_nodes = saved;
+            if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+        }
+        // t0 lives on the host stack: a pageable copy is staged before return
+        *t = tend;
+        done += m;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_profile_steps(dg_ctx *c, double *t, double dt, int nsteps, dg_kernel_times *out) {
+    if (!c || !t || !out || nsteps < 0) return fail(DG_ERR_ARG, "bad arguments");
+    if (!(dt > 0) || !std::isfinite(dt)) return fail(DG_ERR_ARG, "dt must be positive and finite");
+    CK(cudaSetDevice(c->device));
+    std::memset(out, 0, sizeof(*out));
+    if (nsteps == 0) return DG_OK;
+    // a pair of events around every launch
+    size_t need = (size_t)nsteps * 5 * 2;
+    while (c->events.size() < need) {
+        cudaEvent_t ev;
+        CK(cudaEventCreate(&ev));
+        c->events.push_back(ev);
+    }
+    std::vector<int> kind;  // 0..3 stage, 4 inject
+    size_t ei = 0;
+    double tt = *t;
+    for (int k = 0; k < nsteps; ++k) {
+        CK(cudaMemcpyAsync(c->d_t0, &tt, 8, cudaMemcpyHostToDevice, c->stream));
+        if (c->src_nodes && any_source_active(c, tt)) {
+            CK(cudaEventRecord(c->events[ei++], c->stream));
+            CK(launch_inject(c, 0, dt));
+            CK(cudaEventRecord(c->events[ei++], c->stream));
+            kind.push_back(4);
+        }
+        for (int s = 0; s < 4; ++s) {
+            CK(cudaEventRecord(c->events[ei++], c->stream));
+            CK(launch_stage(c, s, dt));
+            CK(cudaEventRecord(c->events[ei++], c->stream));
+            kind.push_back(s);
+        }
+        tt += dt;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    for (size_t j = 0; j < kind.size(); ++j) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, c->events[2 * j], c->events[2 * j + 1]));
+        if (kind[j] == 4) { out->inject_ms += ms; out->inject_launches++; }
+        else { out->stage_ms[kind[j]] += ms; out->stage_launches[kind[j]]++; }
+    }
+    float tot = 0;
+    CK(cudaEventElapsedTime(&tot, c->events[0], c->events[2 * kind.size() - 1]));
+    out->total_ms = tot;
+    *t = tt;
+    return DG_OK;
+}
+
+int dg_monitors(dg_ctx *c, double *energy, double *l2, long long *status) {
+    if (!c) return fail(DG_ERR_ARG, "null context");
+    CK(cudaSetDevice(c->device));
+    CK(cudaMemsetAsync(c->d_mon, 0, 8 * 8, c->stream));
+    CK(cudaMemsetAsync(c->d_bad, 0, 8, c->stream));
+    int blocks = (c->K + 255) / 256;
+    if (c->prec == DG_PREC_FP64)
+        monitor_kernel<double><<<blocks, 256, 0, c->stream>>>((const double *)c->d_u, c->ndof, c->K, c->np, c->nq,
+                                                              c->d_mass, c->d_detj, c->rho0, c->c0, c->d_mon,
+                                                              c->d_bad);
+    else
+        monitor_kernel<float><<<blocks, 256, 0, c->stream>>>((const float *)c->d_u, c->ndof, c->K, c->np, c->nq,
+                                                             c->d_mass, c->d_detj, c->rho0, c->c0, c->d_mon,
+                                                             c->d_bad);
+    CK(cudaGetLastError());
+    double h[8];
+    unsigned long long bad = 0;
+    CK(cudaMemcpyAsync(h, c->d_mon, 8 * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&bad, c->d_bad, 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (energy) *energy = h[0];
+    if (l2)
+        for (int f = 0; f < 4; ++f) l2[f] = f < c->nq ? std::sqrt(std::max(h[1 + f], 0.0)) : 0.0;
+    if (status) *status = (long long)bad;
+    return bad ? DG_ERR_NONFINITE : DG_OK;
+}
+
+int dg_synchronize(dg_ctx *c) {
+    if (!c) return fail(DG_ERR_ARG, "null context");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_info(dg_ctx *c, long long *dofs, int *fields, long long *state_bytes) {
+    if (!c) return fail(DG_ERR_ARG, "null context");
+    if (dofs) *dofs = c->ndof;
+    if (fields) *fields = c->nq;
+    if (state_bytes) *state_bytes = (long long)c->ndof * c->nq * c->rsize * 4;
+    return DG_OK;
+}
+
+void *dg_host_alloc(unsigned long long bytes) {
+    void *p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+        dg::set_error("cudaMallocHost failed");
+        return nullptr;
+    }
+    return p;
+}
+
+void dg_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

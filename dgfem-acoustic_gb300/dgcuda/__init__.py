@@ -1,0 +1,459 @@
+"""Python host side of the GB300 DG acoustic RK4 library.
+
+A thin ctypes layer over the C ABI declared in include/dgcuda.h (the GPU
+solver) and include/dgmesh.h (mesh reading/generation, the reference-
+semantics Mesh precompute, the .conf parser).  The flow mirrors the
+reference's main (src/dgalerkin.cpp:11-63):
+
+    mesh = Mesh.read_msh("square.msh")            # gmsh::open
+    cfg = Config.parse("config.conf", mesh)       # config::parseConfig
+    pre = Precomp(mesh, cfg.bcs)                  # Mesh mesh(msh, config)
+    u = pre.initial_state(cfg.ics)                # Gaussian initial conditions
+    sol = Solver(pre, cfg.c0, cfg.rho0, cfg.v0)   # precomputeMassMatrix + set-up
+    sol.set_state(u); sol.rk4_steps(t, dt, n)     # solver::rungeKutta steps
+
+Everything runs through lib/libdgcuda.so; there is no CPU fallback: a missing
+library or a missing GPU raises DGError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent.parent
+LIB_PATH = PKG / "lib" / "libdgcuda.so"
+
+PREC_FP64, PREC_FP32 = 0, 1
+FLUX_REFERENCE, FLUX_UPWIND = 0, 1
+ERRORS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "unsupported", -4: "non-finite values",
+          -5: "I/O error", -6: "mesh error", -7: "out of memory", -8: "configuration error"}
+
+
+class DGError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads lib/libdgcuda.so (built by build.py); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise DGError(-5, f"{LIB_PATH} is missing: build it with dgfem-acoustic_gb300/build.py")
+        _lib = C.CDLL(str(LIB_PATH))
+        _declare(_lib)
+    return _lib
+
+
+def _check(code: int) -> None:
+    if code != 0:
+        raise DGError(code, lib().dg_last_error().decode())
+
+
+P_d, P_i, P_u8 = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_ubyte)
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("dim", C.c_int), ("order", C.c_int), ("num_el", C.c_int), ("el_num_nodes", C.c_int),
+                ("f_num", C.c_int), ("f_num_per_el", C.c_int), ("f_num_nodes", C.c_int), ("fc", C.c_int),
+                ("el_jacobians", P_d), ("el_jacobian_dets", P_d), ("f_normals", P_d), ("f_jacobian_dets", P_d),
+                ("el_f_ids", P_i), ("el_f_orientation", P_i), ("f_nbr_el_ids", P_i), ("f_n_to_el_n_ids", P_i),
+                ("f_bc", P_i), ("f_is_boundary", P_u8)]
+
+
+class PhysDesc(C.Structure):
+    _fields_ = [("c0", C.c_double), ("rho0", C.c_double), ("v0", C.c_double * 3)]
+
+
+class Opts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("flux_sign", C.c_int), ("device", C.c_int), ("use_graph", C.c_int),
+                ("elems_per_block", C.c_int), ("reserved", C.c_int * 3)]
+
+
+class KernelTimes(C.Structure):
+    _fields_ = [("stage_ms", C.c_double * 4), ("stage_launches", C.c_int * 4), ("inject_ms", C.c_double),
+                ("inject_launches", C.c_int), ("total_ms", C.c_double)]
+
+
+class LayoutView(C.Structure):
+    _fields_ = [("dim", C.c_int), ("order", C.c_int), ("np", C.c_int), ("nf", C.c_int), ("nfp", C.c_int),
+                ("nq", C.c_int), ("nperm", C.c_int), ("num_el", C.c_int), ("geo", P_d), ("fgeo", P_d),
+                ("conn", P_i), ("ops", P_d), ("n_ops", C.c_int), ("tabs", P_u8), ("n_tabs", C.c_int),
+                ("mass", P_d)]
+
+
+class RawView(C.Structure):
+    _fields_ = [("dim", C.c_int), ("order", C.c_int), ("el_type", C.c_int), ("np", C.c_int),
+                ("num_nodes", C.c_int), ("node_tags", P_i), ("xyz", P_d), ("num_el", C.c_int),
+                ("el_tags", P_i), ("el_nodes", P_i), ("num_phys", C.c_int), ("phys_dim", P_i),
+                ("phys_tag", P_i), ("phys_name", C.POINTER(C.c_char_p)), ("phys_node_offsets", P_i),
+                ("phys_nodes", P_i)]
+
+
+class ConfigView(C.Structure):
+    _fields_ = [("time_start", C.c_double), ("time_end", C.c_double), ("time_step", C.c_double),
+                ("time_rate", C.c_double), ("num_threads", C.c_int), ("v0", C.c_double * 3),
+                ("rho0", C.c_double), ("c0", C.c_double), ("num_sources", C.c_int), ("sources", P_d),
+                ("num_ics", C.c_int), ("ics", P_d), ("num_bcs", C.c_int), ("bc_phys_tags", P_i),
+                ("bc_reflecting", P_i), ("element_type", C.c_char_p), ("time_int_method", C.c_char_p),
+                ("save_file", C.c_char_p), ("precision", C.c_char_p), ("flux_sign", C.c_char_p)]
+
+
+def _declare(L: C.CDLL) -> None:
+    vp = C.c_void_p
+    sig = {
+        "dg_last_error": (C.c_char_p, []),
+        "dg_default_opts": (None, [C.POINTER(Opts)]),
+        "dg_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(PhysDesc), C.POINTER(Opts), C.POINTER(vp)]),
+        "dg_destroy": (None, [vp]),
+        "dg_set_state": (C.c_int, [vp, C.POINTER(P_d)]),
+        "dg_get_state": (C.c_int, [vp, C.POINTER(P_d)]),
+        "dg_set_sources": (C.c_int, [vp, C.c_int, P_i, P_i, P_d]),
+        "dg_rk4_steps": (C.c_int, [vp, P_d, C.c_double, C.c_int]),
+        "dg_profile_steps": (C.c_int, [vp, P_d, C.c_double, C.c_int, C.POINTER(KernelTimes)]),
+        "dg_monitors": (C.c_int, [vp, P_d, P_d, C.POINTER(C.c_longlong)]),
+        "dg_synchronize": (C.c_int, [vp]),
+        "dg_info": (C.c_int, [vp, C.POINTER(C.c_longlong), P_i, C.POINTER(C.c_longlong)]),
+        "dg_host_alloc": (vp, [C.c_ulonglong]),
+        "dg_host_free": (None, [vp]),
+        "dg_layout_build": (C.c_int, [C.POINTER(MeshDesc), C.c_int, C.POINTER(vp)]),
+        "dg_layout_get": (C.c_int, [vp, C.POINTER(LayoutView)]),
+        "dg_layout_free": (None, [vp]),
+        "dgm_read_msh": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
+        "dgm_write_msh": (C.c_int, [vp, C.c_char_p]),
+        "dgm_box_tri": (C.c_int, [C.c_int, C.c_int, P_d, P_d, C.c_int, C.POINTER(C.c_char_p), C.POINTER(vp)]),
+        "dgm_box_tet": (C.c_int, [C.c_int, C.c_int, C.c_int, P_d, P_d, C.c_int, C.POINTER(C.c_char_p), P_i,
+                                  C.c_int, C.c_char_p, C.POINTER(vp)]),
+        "dgm_get_raw": (C.c_int, [vp, C.POINTER(RawView)]),
+        "dgm_free_mesh": (None, [vp]),
+        "dgm_precompute": (C.c_int, [vp, C.c_int, P_i, P_i, C.POINTER(vp)]),
+        "dgm_get_desc": (C.c_int, [vp, C.POINTER(MeshDesc)]),
+        "dgm_get_dof_coords": (C.c_int, [vp, C.POINTER(P_d)]),
+        "dgm_get_face_node_tags": (C.c_int, [vp, C.POINTER(P_i)]),
+        "dgm_min_edge": (C.c_double, [vp]),
+        "dgm_free_precomp": (None, [vp]),
+        "dgm_gaussian_ic": (C.c_int, [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, P_d]),
+        "dgm_source_dofs": (C.c_int, [vp, C.c_double, C.c_double, C.c_double, C.c_double, P_i, C.c_int, P_i]),
+        "dgm_parse_config": (C.c_int, [C.c_char_p, vp, C.POINTER(vp)]),
+        "dgm_get_config": (C.c_int, [vp, C.POINTER(ConfigView)]),
+        "dgm_free_config": (None, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(P_d)
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(P_i)
+
+
+def _arr(ptr, n, dtype) -> np.ndarray:
+    if n == 0:
+        return np.zeros(0, dtype=dtype)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+class Mesh:
+    """Raw mesh: nodes, volume elements (gmsh order) and physical groups."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle) if not isinstance(handle, C.c_void_p) else handle
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.dgm_free_mesh(self._h)
+            self._h = None
+
+    @classmethod
+    def read_msh(cls, path: str | os.PathLike) -> "Mesh":
+        h = C.c_void_p()
+        _check(lib().dgm_read_msh(str(path).encode(), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def box_tri(cls, nx: int, ny: int, lo=(-1.0, -1.0), hi=(1.0, 1.0), order: int = 3,
+                side_names=("Reflecting",) * 4) -> "Mesh":
+        h = C.c_void_p()
+        names = (C.c_char_p * 4)(*[(s.encode() if s else None) for s in side_names])
+        lo_a, hi_a = np.array(lo, float), np.array(hi, float)
+        _check(lib().dgm_box_tri(nx, ny, _dptr(lo_a), _dptr(hi_a), order, names, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def box_tet(cls, nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), order: int = 3,
+                side_names=("Absorbing",) * 6, removed=(), obstacle_name: str = "Reflecting") -> "Mesh":
+        h = C.c_void_p()
+        names = (C.c_char_p * 6)(*[(s.encode() if s else None) for s in side_names])
+        lo_a, hi_a = np.array(lo, float), np.array(hi, float)
+        rem = np.array(list(removed), dtype=np.int32)
+        _check(lib().dgm_box_tet(nx, ny, nz, _dptr(lo_a), _dptr(hi_a), order, names,
+                                 _iptr(rem) if rem.size else None, int(rem.size), obstacle_name.encode(), C.byref(h)))
+        return cls(h)
+
+    def write_msh(self, path: str | os.PathLike) -> None:
+        _check(lib().dgm_write_msh(self._h, str(path).encode()))
+
+    def raw(self) -> dict:
+        v = RawView()
+        _check(lib().dgm_get_raw(self._h, C.byref(v)))
+        off = _arr(v.phys_node_offsets, v.num_phys + 1, np.int32)
+        return {
+            "dim": v.dim, "order": v.order, "el_type": v.el_type, "np": v.np,
+            "node_tags": _arr(v.node_tags, v.num_nodes, np.int32),
+            "xyz": _arr(v.xyz, 3 * v.num_nodes, np.float64).reshape(-1, 3),
+            "el_tags": _arr(v.el_tags, v.num_el, np.int32),
+            "el_nodes": _arr(v.el_nodes, v.num_el * v.np, np.int32).reshape(-1, v.np),
+            "phys_dim": _arr(v.phys_dim, v.num_phys, np.int32),
+            "phys_tag": _arr(v.phys_tag, v.num_phys, np.int32),
+            "phys_name": [v.phys_name[i].decode() for i in range(v.num_phys)],
+            "phys_offsets": off,
+            "phys_nodes": _arr(v.phys_nodes, int(off[-1]) if off.size else 0, np.int32),
+        }
+
+    def bcs(self, mapping: dict[str, bool] | None = None) -> list[tuple[int, bool]]:
+        """(physical tag, reflecting) for boundary groups whose name starts with
+        Reflecting/Absorbing, or as given by mapping name -> reflecting."""
+        r = self.raw()
+        out = []
+        for d, t, n in zip(r["phys_dim"], r["phys_tag"], r["phys_name"]):
+            if d != r["dim"] - 1:
+                continue
+            if mapping is not None:
+                if n in mapping:
+                    out.append((int(t), bool(mapping[n])))
+            elif n.startswith("Reflecting"):
+                out.append((int(t), True))
+            elif n.startswith("Absorbing"):
+                out.append((int(t), False))
+        return sorted(out)
+
+
+class Config:
+    """Parsed .conf (config::parseConfig)."""
+
+    def __init__(self, handle):
+        self._h = handle
+        v = ConfigView()
+        _check(lib().dgm_get_config(self._h, C.byref(v)))
+        self.time_start, self.time_end, self.time_step, self.time_rate = (v.time_start, v.time_end,
+                                                                          v.time_step, v.time_rate)
+        self.num_threads = v.num_threads
+        self.v0 = tuple(v.v0)
+        self.rho0, self.c0 = v.rho0, v.c0
+        self.sources = _arr(v.sources, 9 * v.num_sources, np.float64).reshape(-1, 9)
+        self.ics = _arr(v.ics, 6 * v.num_ics, np.float64).reshape(-1, 6)
+        tags = _arr(v.bc_phys_tags, v.num_bcs, np.int32)
+        refl = _arr(v.bc_reflecting, v.num_bcs, np.int32)
+        self.bcs = [(int(a), bool(b)) for a, b in zip(tags, refl)]
+        self.element_type = v.element_type.decode()
+        self.time_int_method = v.time_int_method.decode()
+        self.save_file = v.save_file.decode()
+        self.precision = v.precision.decode()
+        self.flux_sign = v.flux_sign.decode()
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.dgm_free_config(self._h)
+            self._h = None
+
+    @classmethod
+    def parse(cls, path: str | os.PathLike, mesh: Mesh) -> "Config":
+        h = C.c_void_p()
+        _check(lib().dgm_parse_config(str(path).encode(), mesh._h, C.byref(h)))
+        return cls(h)
+
+
+class Precomp:
+    """Reference-semantics Mesh precompute (the arrays of include/Mesh.h)."""
+
+    def __init__(self, mesh: Mesh, bcs: list[tuple[int, bool]] | None = None):
+        if bcs is None:
+            bcs = mesh.bcs()
+        tags = np.array([b[0] for b in bcs], dtype=np.int32)
+        refl = np.array([1 if b[1] else 0 for b in bcs], dtype=np.int32)
+        h = C.c_void_p()
+        _check(lib().dgm_precompute(mesh._h, len(bcs), _iptr(tags) if len(bcs) else None,
+                                    _iptr(refl) if len(bcs) else None, C.byref(h)))
+        self._h = h
+        self.mesh = mesh
+        d = self.desc()
+        self.dim, self.order, self.num_el, self.np = d.dim, d.order, d.num_el, d.el_num_nodes
+        self.f_num, self.nf, self.nfp, self.fc = d.f_num, d.f_num_per_el, d.f_num_nodes, d.fc
+        self.ndof = self.num_el * self.np
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.dgm_free_precomp(self._h)
+            self._h = None
+
+    def desc(self) -> MeshDesc:
+        d = MeshDesc()
+        _check(lib().dgm_get_desc(self._h, C.byref(d)))
+        return d
+
+    def arrays(self) -> dict:
+        d = self.desc()
+        K, F, nf, nfp = d.num_el, d.f_num, d.f_num_per_el, d.f_num_nodes
+        tags = P_i()
+        _check(lib().dgm_get_face_node_tags(self._h, C.byref(tags)))
+        return {
+            "fc": d.fc,
+            "el_jacobians": _arr(d.el_jacobians, 9 * K, np.float64).reshape(K, 9),
+            "el_jacobian_dets": _arr(d.el_jacobian_dets, K, np.float64),
+            "f_normals": _arr(d.f_normals, 3 * F, np.float64).reshape(F, 3),
+            "f_jacobian_dets": _arr(d.f_jacobian_dets, F, np.float64),
+            "el_f_ids": _arr(d.el_f_ids, K * nf, np.int32).reshape(K, nf),
+            "el_f_orientation": _arr(d.el_f_orientation, K * nf, np.int32).reshape(K, nf),
+            "f_nbr_el_ids": _arr(d.f_nbr_el_ids, 2 * F, np.int32).reshape(F, 2),
+            "f_n_to_el_n_ids": _arr(d.f_n_to_el_n_ids, 2 * F * nfp, np.int32).reshape(F, nfp, 2),
+            "f_bc": _arr(d.f_bc, F, np.int32),
+            "f_is_boundary": _arr(d.f_is_boundary, F, np.uint8),
+            "f_node_tags": _arr(tags, F * nfp, np.int32).reshape(F, nfp),
+        }
+
+    def layout(self, flux: str = "reference") -> dict:
+        """The element-centric arrays dg_create uploads (host side, no GPU)."""
+        d = self.desc()
+        h = C.c_void_p()
+        _check(lib().dg_layout_build(C.byref(d), {"reference": FLUX_REFERENCE, "upwind": FLUX_UPWIND}[flux],
+                                     C.byref(h)))
+        try:
+            v = LayoutView()
+            _check(lib().dg_layout_get(h, C.byref(v)))
+            K, nf, np_, dim = v.num_el, v.nf, v.np, v.dim
+            return {
+                "dim": dim, "order": v.order, "np": np_, "nf": nf, "nfp": v.nfp, "nq": v.nq, "nperm": v.nperm,
+                "geo": _arr(v.geo, K * dim * dim, np.float64).reshape(K, dim, dim),
+                "fgeo": _arr(v.fgeo, K * nf * 4, np.float64).reshape(K, nf, 4),
+                "conn": _arr(v.conn, K * nf * 2, np.int32).reshape(K, nf, 2),
+                "ops": _arr(v.ops, v.n_ops, np.float64),
+                "tabs": _arr(v.tabs, v.n_tabs, np.int32),
+                "mass": _arr(v.mass, np_ * np_, np.float64).reshape(np_, np_),
+            }
+        finally:
+            lib().dg_layout_free(h)
+
+    def dof_coords(self) -> np.ndarray:
+        p = P_d()
+        _check(lib().dgm_get_dof_coords(self._h, C.byref(p)))
+        return _arr(p, 3 * self.ndof, np.float64).reshape(-1, 3)
+
+    def min_edge(self) -> float:
+        return float(lib().dgm_min_edge(self._h))
+
+    def initial_state(self, ics) -> np.ndarray:
+        """u[4][ndof] with the reference's Gaussian initial conditions
+        (rows: 0, x, y, z, size, amp)."""
+        u = np.zeros((4, self.ndof))
+        for ic in ics:
+            _check(lib().dgm_gaussian_ic(self._h, ic[1], ic[2], ic[3], ic[4], ic[5], _dptr(u[0])))
+        return u
+
+    def source_dofs(self, x: float, y: float, z: float, size: float) -> np.ndarray:
+        cnt = C.c_int()
+        _check(lib().dgm_source_dofs(self._h, x, y, z, size, None, 0, C.byref(cnt)))
+        idx = np.zeros(max(cnt.value, 1), dtype=np.int32)
+        _check(lib().dgm_source_dofs(self._h, x, y, z, size, _iptr(idx), cnt.value, C.byref(cnt)))
+        return idx[:cnt.value]
+
+
+class Solver:
+    """GPU RK4 right-hand side context (dg_create ... dg_destroy)."""
+
+    def __init__(self, pre: Precomp, c0: float, rho0: float, v0=(0.0, 0.0, 0.0), precision: str = "fp64",
+                 flux: str = "reference", use_graph: bool = True, device: int = 0):
+        d = pre.desc()
+        ph = PhysDesc(c0, rho0, (C.c_double * 3)(*v0))
+        o = Opts()
+        lib().dg_default_opts(C.byref(o))
+        o.precision = {"fp64": PREC_FP64, "fp32": PREC_FP32}[precision]
+        o.flux_sign = {"reference": FLUX_REFERENCE, "upwind": FLUX_UPWIND}[flux]
+        o.use_graph = 1 if use_graph else 0
+        o.device = device
+        h = C.c_void_p()
+        _check(lib().dg_create(C.byref(d), C.byref(ph), C.byref(o), C.byref(h)))
+        self._h = h
+        self.pre = pre
+        self.dim = pre.dim
+        self.ndof = pre.ndof
+        self.precision = precision
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.dg_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def set_state(self, u: np.ndarray) -> None:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        assert u.shape == (4, self.ndof)
+        ptrs = (P_d * 4)(*[_dptr(u[q]) for q in range(4)])
+        _check(lib().dg_set_state(self._h, ptrs))
+
+    def get_state(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((4, self.ndof))
+        ptrs = (P_d * 4)(*[_dptr(out[q]) for q in range(4)])
+        _check(lib().dg_get_state(self._h, ptrs))
+        return out
+
+    def set_sources(self, sources: list[tuple[np.ndarray, float, float, float, float]]) -> None:
+        """sources: (dof indices, amp, freq, phase, duration) in config order."""
+        off = np.zeros(len(sources) + 1, dtype=np.int32)
+        idx, par = [], []
+        for s, (dofs, amp, freq, phase, dur) in enumerate(sources):
+            idx.append(np.asarray(dofs, dtype=np.int32))
+            off[s + 1] = off[s] + len(dofs)
+            par += [amp, freq, phase, dur]
+        idx_a = np.concatenate(idx) if idx else np.zeros(1, dtype=np.int32)
+        par_a = np.array(par if par else [0.0], dtype=np.float64)
+        _check(lib().dg_set_sources(self._h, len(sources), _iptr(off), _iptr(idx_a), _dptr(par_a)))
+
+    def rk4_steps(self, t: float, dt: float, nsteps: int) -> float:
+        tt = C.c_double(t)
+        _check(lib().dg_rk4_steps(self._h, C.byref(tt), dt, nsteps))
+        return tt.value
+
+    def profile_steps(self, t: float, dt: float, nsteps: int) -> tuple[float, dict]:
+        tt = C.c_double(t)
+        kt = KernelTimes()
+        _check(lib().dg_profile_steps(self._h, C.byref(tt), dt, nsteps, C.byref(kt)))
+        return tt.value, {"stage_ms": list(kt.stage_ms), "stage_launches": list(kt.stage_launches),
+                          "inject_ms": kt.inject_ms, "inject_launches": kt.inject_launches,
+                          "total_ms": kt.total_ms}
+
+    def monitors(self) -> tuple[float, list[float], int]:
+        e = C.c_double()
+        l2 = (C.c_double * 4)()
+        bad = C.c_longlong()
+        code = lib().dg_monitors(self._h, C.byref(e), l2, C.byref(bad))
+        if code not in (0, -4):
+            _check(code)
+        return e.value, list(l2), bad.value
+
+    def synchronize(self) -> None:
+        _check(lib().dg_synchronize(self._h))
+
+    def info(self) -> dict:
+        d, f, b = C.c_longlong(), C.c_int(), C.c_longlong()
+        _check(lib().dg_info(self._h, C.byref(d), C.byref(f), C.byref(b)))
+        return {"dofs_per_field": d.value, "fields": f.value, "state_bytes": b.value}
+
+
+def cfl_dt(pre: Precomp, c0: float, v0=(0.0, 0.0, 0.0), cfl: float = 0.5) -> float:
+    """dt = CFL * h_min / ((2p+1) (c0 + |v0|)), h_min = shortest element edge."""
+    vmag = float(np.linalg.norm(v0))
+    return cfl * pre.min_edge() / ((2 * pre.order + 1) * (c0 + vmag))

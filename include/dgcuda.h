@@ -1,0 +1,168 @@
+/*
+ * dgcuda.h - C ABI of the GB300 RK4 right-hand side for the linearised-Euler /
+ * acoustic DG solver (drop-in for the step loop of DGFEM-Acoustic).
+ *
+ * What it replaces (reference file:line):
+ *   dg_create      Mesh::precomputeMassMatrix (src/Mesh.cpp:440-466) and the
+ *                  per-stage scratch set-up of solver::rungeKutta
+ *                  (src/solver.cpp:173-194); it reads the arrays the Mesh
+ *                  constructor builds (include/Mesh.h:31-108, 140-223).
+ *   dg_set_state   the caller-owned state u[4][numNodes]
+ *                  (src/dgalerkin.cpp:36, layout include/Mesh.h:34-36).
+ *   dg_set_sources source node selection (src/solver.cpp:197-210).
+ *   dg_rk4_steps   one iteration of the time loop per step: hard sources
+ *                  (src/solver.cpp:248-256), the four RK stages of
+ *                  Mesh::updateFlux (src/Mesh.cpp:569-674), numStep
+ *                  (src/solver.cpp:35-52) with Mesh::precomputeFlux
+ *                  (src/Mesh.cpp:500-539), Mesh::getElFlux (src/Mesh.cpp:548-557),
+ *                  Mesh::getElStiffVector (src/Mesh.cpp:476-489), and the RK
+ *                  combination (src/solver.cpp:261-285); t += dt.
+ *   dg_get_state   the copy-out at save steps (src/solver.cpp:226-235).
+ *   dg_monitors    no counterpart: FP64 discrete energy, L2 norms, NaN check.
+ *
+ * Conventions: 0 = success, negative = error (DG_ERR_*); no exceptions cross
+ * the ABI.  A context is not thread-safe; use one per host thread.  The host
+ * keeps ownership of every array passed in; dg_create copies what it needs.
+ * All element data are for straight-sided (affine) simplices: per-quadrature-
+ * point arrays of the reference are passed at their first point only.
+ */
+#ifndef DGCUDA_H
+#define DGCUDA_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DG_OK 0
+#define DG_ERR_ARG (-1)
+#define DG_ERR_CUDA (-2)
+#define DG_ERR_UNSUPPORTED (-3)
+#define DG_ERR_NONFINITE (-4)
+#define DG_ERR_IO (-5)
+#define DG_ERR_MESH (-6)
+#define DG_ERR_NOMEM (-7)
+#define DG_ERR_CONFIG (-8)
+
+#define DG_PREC_FP64 0 /* FP64 throughout */
+#define DG_PREC_FP32 1 /* FP32 state and flux, FP64 geometry factors */
+
+#define DG_FLUX_REFERENCE 0 /* interior jump sign fc*orientation, as the reference (Mesh.cpp:524) */
+#define DG_FLUX_UPWIND 1    /* interior jump sign +1 on every face */
+
+typedef struct dg_ctx dg_ctx;
+
+/* The reference Mesh arrays (include/Mesh.h), at the first quadrature point. */
+typedef struct dg_mesh_desc {
+    int dim;          /* m_elDim: 2 or 3 */
+    int order;        /* m_elOrder: 1..5 */
+    int num_el;       /* m_elNum */
+    int el_num_nodes; /* m_elNumNodes */
+    int f_num;        /* m_fNum */
+    int f_num_per_el; /* m_fNumPerEl */
+    int f_num_nodes;  /* m_fNumNodes */
+    int fc;           /* numerical flux coefficient fc (Mesh.h:143, Mesh.cpp:210-211) */
+    const double *el_jacobians;      /* [num_el][9]: dx_x/du_u at [u*3+x] (Mesh.h:37-39) */
+    const double *el_jacobian_dets;  /* [num_el] (Mesh.h:40-42) */
+    const double *f_normals;         /* [f_num][3] after the boundary flip (Mesh.h:88-90, Mesh.cpp:336-353) */
+    const double *f_jacobian_dets;   /* [f_num] (Mesh.h:70-72) */
+    const int *el_f_ids;             /* [num_el][f_num_per_el] (Mesh.h:91-93) */
+    const int *el_f_orientation;     /* [num_el][f_num_per_el], +-1 (Mesh.h:100-102) */
+    const int *f_nbr_el_ids;         /* [f_num][2], -1 for a missing side (Mesh.h:94-96) */
+    const int *f_n_to_el_n_ids;      /* [f_num][f_num_nodes][2], -1 for a missing side (Mesh.h:97-99) */
+    const int *f_bc;                 /* [f_num]: 1 reflecting, otherwise absorbing (Mesh.h:218) */
+    const unsigned char *f_is_boundary; /* [f_num] (Mesh.h:217) */
+} dg_mesh_desc;
+
+/* Mean flow and medium (include/configParser.h:26-28). */
+typedef struct dg_phys_desc {
+    double c0, rho0;
+    double v0[3];
+} dg_phys_desc;
+
+typedef struct dg_opts {
+    int precision;   /* DG_PREC_FP64 | DG_PREC_FP32 */
+    int flux_sign;   /* DG_FLUX_REFERENCE | DG_FLUX_UPWIND */
+    int device;      /* CUDA device ordinal */
+    int use_graph;   /* capture step chunks in CUDA graphs (1) or launch directly (0) */
+    int elems_per_block; /* 0 = built-in choice */
+    int reserved[3];
+} dg_opts;
+
+/* Per-kernel timing of dg_profile_steps (CUDA events on the solver stream). */
+typedef struct dg_kernel_times {
+    double stage_ms[4];   /* summed device time of the stage kernels */
+    int stage_launches[4];
+    double inject_ms;
+    int inject_launches;
+    double total_ms;      /* first event to last event */
+} dg_kernel_times;
+
+void dg_default_opts(dg_opts *opts);
+
+int dg_create(const dg_mesh_desc *mesh, const dg_phys_desc *phys, const dg_opts *opts, dg_ctx **out);
+void dg_destroy(dg_ctx *ctx);
+
+/* u[q] points to num_el*el_num_nodes doubles, field q = p, vx, vy, vz,
+ * element-major (u[q][el*el_num_nodes + n]).  In 2D vz must be zero. */
+int dg_set_state(dg_ctx *ctx, const double *const u[4]);
+int dg_get_state(dg_ctx *ctx, double *const u[4]);
+
+/* Hard sources: for source s, nodes dof_idx[offsets[s] .. offsets[s+1]) get
+ * p = amp*sin(2*pi*freq*t + phase) while t < duration, at the start of each
+ * step.  params[s*4 + 0..3] = amp, freq, phase, duration.  Later sources
+ * overwrite earlier ones on shared nodes. */
+int dg_set_sources(dg_ctx *ctx, int nsrc, const int *offsets, const int *dof_idx, const double *params);
+
+/* nsteps classical RK4 steps starting at *t; *t is advanced by repeated
+ * t += dt in double, as the reference loop does. */
+int dg_rk4_steps(dg_ctx *ctx, double *t, double dt, int nsteps);
+
+/* Same steps with CUDA events around every kernel (no graph). */
+int dg_profile_steps(dg_ctx *ctx, double *t, double dt, int nsteps, dg_kernel_times *times);
+
+/* FP64 monitors: energy = 1/2 sum_e u_e^T M_e (p^2/(rho0 c0^2) + rho0 |v|^2);
+ * l2[q] = sqrt(u_q^T M u_q); status = number of non-finite values. */
+int dg_monitors(dg_ctx *ctx, double *energy, double *l2, long long *status);
+
+/* Waits for all work of the context. */
+int dg_synchronize(dg_ctx *ctx);
+
+/* Sizes and the device data the context holds (for callers that time or
+ * inspect it): number of DOFs per field, fields evolved, bytes of state. */
+int dg_info(dg_ctx *ctx, long long *dofs_per_field, int *fields, long long *state_bytes);
+
+/* Pinned host buffers for fast dg_set_state / dg_get_state. */
+void *dg_host_alloc(unsigned long long bytes);
+void dg_host_free(void *p);
+
+/* Host-side view of the element-centric layout dg_create uploads (no GPU
+ * work; for inspection and tests).  geo [num_el][dim*dim] inverse Jacobians
+ * B[x][u]; fgeo [num_el][nf][4] outward normal and detJf/detJe; conn
+ * [num_el][nf][2] neighbour and connectivity word (bits 0-1 neighbour's local
+ * face, 2-4 face permutation, 5-6 kind 0 interior / 1 reflecting /
+ * 2 absorbing, 7 negative jump sign); ops = D as [u][j][i] then LIFT as
+ * [face*nfp+k][i]; tabs = face masks [nf][nfp] then permutations
+ * [nperm][nfp]; mass [np][np] reference mass matrix. */
+typedef struct dg_layout dg_layout;
+typedef struct dg_layout_view {
+    int dim, order, np, nf, nfp, nq, nperm, num_el;
+    const double *geo;
+    const double *fgeo;
+    const int *conn;
+    const double *ops;
+    int n_ops;
+    const unsigned char *tabs;
+    int n_tabs;
+    const double *mass;
+} dg_layout_view;
+int dg_layout_build(const dg_mesh_desc *mesh, int flux_sign, dg_layout **out);
+int dg_layout_get(const dg_layout *layout, dg_layout_view *view);
+void dg_layout_free(dg_layout *layout);
+
+/* Message of the last error on this thread. */
+const char *dg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DGCUDA_H */
