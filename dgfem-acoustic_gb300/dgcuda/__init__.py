@@ -453,7 +453,25 @@ class Solver:
         return {"dofs_per_field": d.value, "fields": f.value, "state_bytes": b.value}
 
 
+def min_inradius(pre: Precomp) -> float:
+    """Smallest inscribed radius over the elements (from the vertex nodes)."""
+    x = pre.dof_coords().reshape(pre.num_el, pre.np, 3)[:, :pre.dim + 1, :]
+    if pre.dim == 2:
+        a = x[:, 1] - x[:, 0]
+        b = x[:, 2] - x[:, 0]
+        area = 0.5 * np.linalg.norm(np.cross(a, b), axis=1)
+        per = (np.linalg.norm(a, axis=1) + np.linalg.norm(b, axis=1) + np.linalg.norm(x[:, 2] - x[:, 1], axis=1))
+        return float(np.min(2 * area / per))
+    a, b, c = x[:, 1] - x[:, 0], x[:, 2] - x[:, 0], x[:, 3] - x[:, 0]
+    vol = np.abs(np.einsum("ij,ij->i", a, np.cross(b, c))) / 6
+    faces = [(0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3)]
+    surf = sum(0.5 * np.linalg.norm(np.cross(x[:, j] - x[:, i], x[:, k] - x[:, i]), axis=1) for i, j, k in faces)
+    return float(np.min(3 * vol / surf))
+
+
 def cfl_dt(pre: Precomp, c0: float, v0=(0.0, 0.0, 0.0), cfl: float = 0.5) -> float:
-    """dt = CFL * h_min / ((2p+1) (c0 + |v0|)), h_min = shortest element edge."""
+    """dt = CFL * h_min / ((2p+1) (c0 + |v0|)) with h_min twice the smallest
+    inscribed radius (the reference takes dt from the .conf file; this is the
+    rule used for the generated benchmark configurations)."""
     vmag = float(np.linalg.norm(v0))
-    return cfl * pre.min_edge() / ((2 * pre.order + 1) * (c0 + vmag))
+    return cfl * 2 * min_inradius(pre) / ((2 * pre.order + 1) * (c0 + vmag))

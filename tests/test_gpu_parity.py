@@ -1,0 +1,105 @@
+"""GPU parity: the product's CUDA path (through the C ABI) against the CPU
+oracle on the same seeded inputs.  FP64 tolerance: 1e-10 relative L2 per
+field (the factored operators differ from the oracle's quadrature only by
+rounding); FP32: 1e-5 relative L2."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import dgcuda as D
+import oracle_py as O
+
+pytestmark = pytest.mark.gpu
+
+C0, RHO0 = 340.0, 1.225
+FP64_TOL = 1e-10
+FP32_TOL = 1e-5
+
+
+def rel_l2(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / nb if nb > 0 else np.linalg.norm(a - b)
+
+
+def make_mesh(dim, order, bc):
+    if dim == 2:
+        names = {"refl": ("Reflecting",) * 4, "abs": ("Absorbing",) * 4,
+                 "mixed": ("Reflecting", "Absorbing", "Reflecting", "Absorbing")}[bc]
+        return D.Mesh.box_tri(5, 4, (-1.0, -1.0), (1.0, 0.8), order=order, side_names=names)
+    names = {"refl": ("Reflecting",) * 6, "abs": ("Absorbing",) * 6,
+             "mixed": ("Absorbing", "Reflecting") * 3}[bc]
+    return D.Mesh.box_tet(3, 2, 2, (0.0, 0.0, 0.0), (1.0, 0.7, 0.6), order=order, side_names=names)
+
+
+def run_pair(dim, order, bc, v0=(0.0, 0.0, 0.0), flux="reference", nsteps=12, precision="fp64",
+             sources=None, seed=0, use_graph=True):
+    mesh = make_mesh(dim, order, bc)
+    pre = D.Precomp(mesh)
+    dt = D.cfl_dt(pre, C0, v0)
+    rng = np.random.default_rng(seed)
+    centre = pre.dof_coords().mean(axis=0)
+    u0 = pre.initial_state([(0, *centre, 0.02, 1.0)])
+    u0[1:dim + 1] += 1e-3 * rng.standard_normal((dim, pre.ndof))
+    sol = D.Solver(pre, C0, RHO0, v0, precision=precision, flux=flux, use_graph=use_graph)
+    sol.set_state(u0)
+    src_cfg = None
+    if sources:
+        lst = []
+        for (x, y, z, size, amp, f, ph, dur) in sources:
+            lst.append((pre.source_dofs(x, y, z, size), amp, f, ph, dur))
+        sol.set_sources(lst)
+        src_cfg = np.array([[0, x, y, z, size, amp, f, ph, dur] for (x, y, z, size, amp, f, ph, dur) in sources])
+    t = sol.rk4_steps(0.0, dt, nsteps)
+    got = sol.get_state()
+    orc = O.Oracle(mesh.raw(), dt, C0, RHO0, v0=v0, bcs=mesh.bcs(), upwind=(flux == "upwind"), sources=src_cfg)
+    orc.set_state(u0)
+    t_ref, _ = orc.run(0.0, nsteps)
+    ref = orc.get_state()
+    assert t == t_ref
+    return got, ref, dim
+
+
+@pytest.mark.parametrize("dim,order", [(2, 1), (2, 2), (2, 3), (2, 4), (2, 5), (3, 1), (3, 2), (3, 3), (3, 4)])
+@pytest.mark.parametrize("bc", ["refl", "mixed"])
+def test_fp64_matches_oracle(dim, order, bc):
+    got, ref, dim = run_pair(dim, order, bc)
+    tol = FP64_TOL if order <= 3 else 1e-9
+    for q in range(dim + 1):
+        assert rel_l2(got[q], ref[q]) <= tol, (q, rel_l2(got[q], ref[q]))
+    assert np.all(got[3] == 0) if dim == 2 else True
+
+
+@pytest.mark.parametrize("dim,order,v0", [(2, 3, (60.0, -30.0, 0.0)), (3, 3, (102.0, 0.0, 0.0)),
+                                          (3, 2, (20.0, 10.0, -15.0))])
+def test_fp64_mean_flow(dim, order, v0):
+    got, ref, dim = run_pair(dim, order, "abs", v0=v0)
+    for q in range(dim + 1):
+        assert rel_l2(got[q], ref[q]) <= FP64_TOL
+
+
+@pytest.mark.parametrize("dim,order", [(2, 3), (3, 3), (3, 2)])
+def test_fp64_upwind_mode(dim, order):
+    got, ref, dim = run_pair(dim, order, "mixed", flux="upwind")
+    for q in range(dim + 1):
+        assert rel_l2(got[q], ref[q]) <= FP64_TOL
+
+
+def test_fp64_sources():
+    srcs = [(0.2, 0.1, 0.0, 0.3, 2.0, 1500.0, 0.0, 1e-3), (-0.3, 0.2, 0.0, 0.25, 1.0, 900.0, 0.5, 2e-5)]
+    got, ref, dim = run_pair(2, 3, "refl", sources=srcs, nsteps=40)
+    for q in range(3):
+        assert rel_l2(got[q], ref[q]) <= FP64_TOL
+
+
+def test_graph_and_direct_launches_agree():
+    a, _, _ = run_pair(2, 3, "mixed", nsteps=70, use_graph=True)
+    b, _, _ = run_pair(2, 3, "mixed", nsteps=70, use_graph=False)
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("dim,order", [(2, 3), (3, 3)])
+def test_fp32_close_to_oracle(dim, order):
+    got, ref, dim = run_pair(dim, order, "mixed", precision="fp32", flux="upwind")
+    for q in range(dim + 1):
+        assert rel_l2(got[q], ref[q]) <= FP32_TOL
