@@ -412,10 +412,11 @@ int dg_set_sources(dg_ctx *c, int nsrc, const int *offsets, const int *dof_idx, 
     return DG_OK;
 }
 
-int dg_rk4_steps(dg_ctx *c, double *t, double dt, int nsteps) {
-    if (!c || !t || nsteps < 0) return fail(DG_ERR_ARG, "bad step arguments");
-    if (!(dt > 0) || !std::isfinite(dt)) return fail(DG_ERR_ARG, "dt must be positive and finite");
-    CK(cudaSetDevice(c->device));
+}  // extern "C"
+
+namespace {
+// Enqueues nsteps steps on the context stream (graph chunks of kGraphChunk).
+int enqueue_steps(dg_ctx *c, double *t, double dt, int nsteps) {
     int done = 0;
     while (done < nsteps) {
         int m = std::min(kGraphChunk, nsteps - done);
@@ -457,8 +458,42 @@ int dg_rk4_steps(dg_ctx *c, double *t, double dt, int nsteps) {
         *t = tend;
         done += m;
     }
+    return DG_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int dg_rk4_steps(dg_ctx *c, double *t, double dt, int nsteps) {
+    if (!c || !t || nsteps < 0) return fail(DG_ERR_ARG, "bad step arguments");
+    if (!(dt > 0) || !std::isfinite(dt)) return fail(DG_ERR_ARG, "dt must be positive and finite");
+    CK(cudaSetDevice(c->device));
+    int rc = enqueue_steps(c, t, dt, nsteps);
+    if (rc != DG_OK) return rc;
     CK(cudaStreamSynchronize(c->stream));
     return DG_OK;
+}
+
+int dg_rk4_steps_timed(dg_ctx *c, double *t, double dt, int nsteps, double *ms) {
+    if (!c || !t || !ms || nsteps < 0) return fail(DG_ERR_ARG, "bad step arguments");
+    if (!(dt > 0) || !std::isfinite(dt)) return fail(DG_ERR_ARG, "dt must be positive and finite");
+    CK(cudaSetDevice(c->device));
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaEventRecord(a, c->stream));
+    int rc = enqueue_steps(c, t, dt, nsteps);
+    if (rc == DG_OK) {
+        CK(cudaEventRecord(b, c->stream));
+        CK(cudaEventSynchronize(b));
+        float f = 0;
+        CK(cudaEventElapsedTime(&f, a, b));
+        *ms = f;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return rc;
 }
 
 int dg_profile_steps(dg_ctx *c, double *t, double dt, int nsteps, dg_kernel_times *out) {

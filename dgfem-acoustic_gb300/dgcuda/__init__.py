@@ -117,6 +117,7 @@ def _declare(L: C.CDLL) -> None:
         "dg_get_state": (C.c_int, [vp, C.POINTER(P_d)]),
         "dg_set_sources": (C.c_int, [vp, C.c_int, P_i, P_i, P_d]),
         "dg_rk4_steps": (C.c_int, [vp, P_d, C.c_double, C.c_int]),
+        "dg_rk4_steps_timed": (C.c_int, [vp, P_d, C.c_double, C.c_int, P_d]),
         "dg_profile_steps": (C.c_int, [vp, P_d, C.c_double, C.c_int, C.POINTER(KernelTimes)]),
         "dg_monitors": (C.c_int, [vp, P_d, P_d, C.POINTER(C.c_longlong)]),
         "dg_synchronize": (C.c_int, [vp]),
@@ -426,6 +427,12 @@ class Solver:
         tt = C.c_double(t)
         _check(lib().dg_rk4_steps(self._h, C.byref(tt), dt, nsteps))
         return tt.value
+
+    def rk4_steps_timed(self, t: float, dt: float, nsteps: int) -> tuple[float, float]:
+        """Steps bracketed by CUDA events on the solver stream: (t, device ms)."""
+        tt, ms = C.c_double(t), C.c_double()
+        _check(lib().dg_rk4_steps_timed(self._h, C.byref(tt), dt, nsteps, C.byref(ms)))
+        return tt.value, ms.value
 
     def profile_steps(self, t: float, dt: float, nsteps: int) -> tuple[float, dict]:
         tt = C.c_double(t)

@@ -117,6 +117,10 @@ int dg_set_sources(dg_ctx *ctx, int nsrc, const int *offsets, const int *dof_idx
  * t += dt in double, as the reference loop does. */
 int dg_rk4_steps(dg_ctx *ctx, double *t, double dt, int nsteps);
 
+/* dg_rk4_steps bracketed by CUDA events on the solver stream; *ms = device
+ * time of the whole run. */
+int dg_rk4_steps_timed(dg_ctx *ctx, double *t, double dt, int nsteps, double *ms);
+
 /* Same steps with CUDA events around every kernel (no graph). */
 int dg_profile_steps(dg_ctx *ctx, double *t, double dt, int nsteps, dg_kernel_times *times);
 
