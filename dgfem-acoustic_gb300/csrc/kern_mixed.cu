@@ -1,0 +1,97 @@
+// Mixed-precision stage kernels (tensor-core contraction with exact
+// accumulation) and the host-side slicing of the operator B.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "kernels.h"
+#include "mixed_kernel.cuh"
+
+namespace dgk {
+
+namespace {
+
+template <int DIM, int P>
+void b_image(const double *ops, std::vector<uint8_t> &img, std::vector<int> &eb) {
+    using MS = MixedShape<DIM, P>;
+    constexpr int NP = MS::NP, KTOT = MS::KTOT, KSTEPS = MS::KSTEPS, NPAD = MS::NPAD;
+    const double *D = ops;                      // [u][j][i]
+    const double *L = ops + DIM * NP * NP;      // [slot][i]
+    img.assign(MS::BBYTES, 0);
+    eb.assign(NPAD, 0);
+    std::vector<double> row(KTOT);
+    for (int i = 0; i < NP; ++i) {
+        double amax = 0;
+        for (int k = 0; k < KTOT; ++k) {
+            double v;
+            if (k < DIM * NP) {
+                int u = k / NP, j = k % NP;
+                v = D[((size_t)u * NP + j) * NP + i];
+            } else {
+                v = L[(size_t)(k - DIM * NP) * NP + i];
+            }
+            row[k] = v;
+            amax = std::fmax(amax, std::fabs(v));
+        }
+        int e = 0;
+        if (amax > 0) std::frexp(amax, &e);
+        eb[i] = e;
+        for (int k = 0; k < KTOT; ++k) {
+            double x = std::ldexp(row[k], -e) * 256.0;
+            for (int sl = 0; sl < 4; ++sl) {
+                double m = std::nearbyint(x);
+                x = (x - m) * 256.0;
+                float val = (float)std::ldexp(m, -8 * sl);
+                uint32_t bits;
+                std::memcpy(&bits, &val, 4);
+                uint16_t h = (uint16_t)(bits >> 16);
+                size_t off = (size_t)(sl * KSTEPS + k / 16) * MS::BTILE + (i / 8) * 256 + ((k % 16) / 8) * 128 +
+                             (i % 8) * 16 + (k % 8) * 2;
+                std::memcpy(&img[off], &h, 2);
+            }
+        }
+    }
+}
+
+template <int DIM, int P>
+bool fill(MixedKernelSet *ks) {
+    using MS = MixedShape<DIM, P>;
+    if constexpr (!MS::FITS) {
+        return false;
+    } else {
+        ks->stage[0] = (const void *)&mixed_stage_kernel<DIM, P, 1>;
+        ks->stage[1] = (const void *)&mixed_stage_kernel<DIM, P, 2>;
+        ks->stage[2] = (const void *)&mixed_stage_kernel<DIM, P, 3>;
+        ks->stage[3] = (const void *)&mixed_stage_kernel<DIM, P, 4>;
+        ks->elems_per_tile = MS::ELEMS;
+        ks->threads = 256;
+        ks->smem = MS::SMEM_LAUNCH;
+        ks->b_image = &b_image<DIM, P>;
+        ks->npad = MS::NPAD;
+        return true;
+    }
+}
+
+}  // namespace
+
+bool get_mixed_kernels(int dim, int order, MixedKernelSet *ks) {
+    if (dim == 2) {
+        switch (order) {
+            case 1: return fill<2, 1>(ks);
+            case 2: return fill<2, 2>(ks);
+            case 3: return fill<2, 3>(ks);
+            case 4: return fill<2, 4>(ks);
+            case 5: return fill<2, 5>(ks);
+        }
+    } else if (dim == 3) {
+        switch (order) {
+            case 1: return fill<3, 1>(ks);
+            case 2: return fill<3, 2>(ks);
+            case 3: return fill<3, 3>(ks);
+            case 4: return fill<3, 4>(ks);
+        }
+    }
+    return false;
+}
+
+}  // namespace dgk

@@ -3,6 +3,9 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stddef.h>
+#include <stdint.h>
+
+#include <vector>
 
 namespace dgk {
 
@@ -21,5 +24,45 @@ bool kernels_f64_2d(int order, KernelSet *out);
 bool kernels_f64_3d(int order, KernelSet *out);
 bool kernels_f32_2d(int order, KernelSet *out);
 bool kernels_f32_3d(int order, KernelSet *out);
+
+}  // namespace dgk
+
+namespace dgk {
+
+// Mixed-precision (tensor-core) stage kernels of one (dimension, order).
+struct MixedKernelSet {
+    const void *stage[4] = {nullptr, nullptr, nullptr, nullptr};
+    int elems_per_tile = 0;
+    int threads = 0;
+    size_t smem = 0;
+    int npad = 0;
+    // builds the shared-memory image of the sliced operator and its row
+    // exponents from the layout operators (D as [u][j][i], LIFT as [slot][i])
+    void (*b_image)(const double *ops, std::vector<uint8_t> &img, std::vector<int> &eb) = nullptr;
+};
+
+bool get_mixed_kernels(int dim, int order, MixedKernelSet *out);
+
+// Arguments of the mixed-precision stage kernels.
+struct MixedArgs {
+    const float *win;      // stage input
+    const float *u;        // state, FP32 high part
+    float *ulo;            // state, FP32 low part
+    float *acc;
+    float *wout;           // next stage input (stage 4: u)
+    long long fstride;
+    const double *geo;     // [K][DIM*DIM]
+    const float *fgeo;     // [K][NF][4]
+    const int2 *conn;      // [K][NF]
+    const uint8_t *bimg;   // B slices, shared-memory image
+    const int *beb;        // B row exponents [NPAD]
+    const uint8_t *tabs;
+    int K;
+    float dt;
+    float rc2, inv_rho, half_c0, c0, rho;
+    float v0[3];
+    int *err;              // set to 1 on a wait timeout
+};
+
 
 }  // namespace dgk

@@ -1,0 +1,363 @@
+// Mixed-precision stage kernel: FP32 state tiles, FP64 geometry factors, and
+// the volume + lift contraction on the tensor cores with exact accumulation.
+//
+// For a tile of ELEMS elements the right-hand side of every (field, element)
+// row r is one contraction over K = DIM*NP + NF*NFP columns,
+//   C[r][i] = sum_k A[r][k] B[i][k],
+//   A[r] = ( Fhat_u(j) for u, j | -(detJf/detJe) Fn(slot) ),
+//   B[i] = ( D_u[i][j]          | LIFT[i][slot] ),
+// so that dt*C is the stage increment (weak volume term minus lift, already
+// multiplied by M^-1).  To keep the contraction at FP64-grade accuracy with
+// FP32 accumulators, both operands are cut into four fixed-point slices with
+// one exponent per row: a = 2^(ea-8) sum_s m_s 2^(-8s), |m_s| <= 256 integer,
+// stored in BF16 exactly; B is sliced on the host the same way per output
+// node.  Slice products are integers (times 2^-8(i+j)); the pairs with
+// i+j = 0 and i+j = 1 sum exactly in two FP32 tensor-memory accumulators
+// (|sum| < 2^24 units), pairs with 2 <= i+j <= 4 go to a third one.  The
+// epilogue adds the three in double-FP32, scales by 2^(ea+eb-16) dt and
+// applies the RK4 stage update with the state u kept as an FP32 pair.
+//
+// Roles: all threads stage the tile's state and compute the face values into
+// shared memory; warps 0-3 (one thread per row, warp w <-> tensor-memory lanes
+// 32w..32w+31) build their A row, store the slices with tcgen05.st, and after
+// the MMAs read the accumulators with tcgen05.ld for the epilogue; one thread
+// issues the 13 x KSTEPS tcgen05.mma and commits them to an mbarrier.
+// Every wait is bounded; on timeout the kernel records an error and stops.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "stage_kernel.cuh"
+#include "kernels.h"
+#include "tc_ptx.cuh"
+
+namespace dgk {
+
+template <int DIM, int P>
+struct MixedShape {
+    using S = Shape<DIM, P>;
+    static constexpr int NP = S::NP, NF = S::NF, NFP = S::NFP, NQ = S::NQ, NSLOT = S::NSLOT;
+    static constexpr int NPERM = S::NPERM;
+    static constexpr int KTOT = DIM * NP + NSLOT;
+    static constexpr int KPAD = (KTOT + 15) / 16 * 16;
+    static constexpr int KSTEPS = KPAD / 16;
+    static constexpr int NPAD = (NP + 15) / 16 * 16;
+    static constexpr int ELEMS = 128 / NQ;          // elements per tile
+    static constexpr int ACOLS = KPAD / 2;          // tensor-memory columns per A slice
+    static constexpr int ACC = 4 * ACOLS;           // first accumulator column
+    static constexpr int TMEM_COLS = 512;
+    static constexpr bool FITS = ACC + 3 * NPAD <= TMEM_COLS;
+    static constexpr int BTILE = NPAD * 32;         // bytes of one (slice, K-step) B tile
+    static constexpr int BBYTES = 4 * KSTEPS * BTILE;
+    static constexpr int QS = NP + 1;               // padded element stride in the state tile
+    // shared memory layout (bytes)
+    static constexpr int OFF_B = 0;
+    static constexpr int OFF_Q = OFF_B + BBYTES;
+    static constexpr int OFF_FN = OFF_Q + NQ * ELEMS * QS * 4;
+    static constexpr int OFF_TAB = OFF_FN + ELEMS * NSLOT * 4 * 4;
+    static constexpr int OFF_EB = (OFF_TAB + S::NTAB + 15) / 16 * 16;
+    static constexpr int OFF_BAR = OFF_EB + NPAD * 4;
+    static constexpr int SMEM = OFF_BAR + 16;
+    // at least half of the SM's shared memory, so one CTA (the tensor-memory
+    // owner) runs per SM
+    static constexpr int SMEM_LAUNCH = SMEM < 118 * 1024 ? 118 * 1024 : SMEM;
+};
+
+// Pair list of the slice products: (A slice, B slice), i + j <= 4.
+__device__ __constant__ const int8_t kPairA[13] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 1, 2, 3};
+__device__ __constant__ const int8_t kPairB[13] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0, 3, 2, 1};
+
+
+// (hi, lo) = a + b exactly (Knuth two-sum).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+template <int DIM, int P, int STAGE>
+__global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) {
+    using MS = MixedShape<DIM, P>;
+    constexpr int NP = MS::NP, NF = MS::NF, NFP = MS::NFP, NQ = MS::NQ, NSLOT = MS::NSLOT;
+    constexpr int ELEMS = MS::ELEMS, QS = MS::QS, KTOT = MS::KTOT, KPAD = MS::KPAD, KSTEPS = MS::KSTEPS;
+    constexpr int NPAD = MS::NPAD, ACOLS = MS::ACOLS;
+    static_assert(MS::FITS, "tile does not fit in tensor memory");
+    extern __shared__ __align__(1024) unsigned char smem[];
+    float *sQ = reinterpret_cast<float *>(smem + MS::OFF_Q);
+    float *sFn = reinterpret_cast<float *>(smem + MS::OFF_FN);
+    uint8_t *sTab = smem + MS::OFF_TAB;
+    int *sEb = reinterpret_cast<int *>(smem + MS::OFF_EB);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + MS::OFF_BAR);
+    uint32_t *sTmem = reinterpret_cast<uint32_t *>(smem + MS::OFF_BAR + 8);
+    int *sFail = reinterpret_cast<int *>(smem + MS::OFF_BAR + 12);
+    const uint8_t *sFmask = sTab;
+    const uint8_t *sPerm = sTab + NF * NFP;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) {
+        dgtc::tmem_alloc(sTmem, MS::TMEM_COLS);
+        dgtc::tmem_relinquish();
+    }
+    if (tid == 0) {
+        dgtc::mbar_init(bar, 1);
+        dgtc::fence_mbar_init();
+        *sFail = 0;
+    }
+    {
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.bimg);
+        uint4 *dst = reinterpret_cast<uint4 *>(smem + MS::OFF_B);
+        for (int k = tid; k < MS::BBYTES / 16; k += 256) dst[k] = src[k];
+        for (int k = tid; k < Shape<DIM, P>::NTAB; k += 256) sTab[k] = a.tabs[k];
+        for (int k = tid; k < NPAD; k += 256) sEb[k] = a.beb[k];
+    }
+    dgtc::fence_proxy_async_smem();
+    dgtc::fence_before_sync();
+    __syncthreads();
+    dgtc::fence_after_sync();
+    const uint32_t tbase = *sTmem;
+    const uint32_t idesc = dgtc::idesc_bf16_f32(128, NPAD);
+    const uint32_t sB = dgtc::smem_u32(smem + MS::OFF_B);
+    bool alive = true;
+    uint32_t phase = 0;
+
+    const int ntiles = (a.K + ELEMS - 1) / ELEMS;
+    for (int tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x) {
+        const long long ebase = (long long)tile * ELEMS;
+        // 1. stage the tile's input state
+        for (int idx = tid; idx < NQ * ELEMS * NP; idx += 256) {
+            const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
+            const int le = rem / NP, j = rem - le * NP;
+            const bool ok = ebase + le < a.K;
+            sQ[(f * ELEMS + le) * QS + j] = ok ? a.win[f * a.fstride + ebase * NP + rem] : 0.0f;
+        }
+        __syncthreads();
+        // 2. face values, negated and scaled: -(detJf/detJe) Fn
+        for (int task = tid; task < ELEMS * NSLOT; task += 256) {
+            const int le = task / NSLOT, s = task - le * NSLOT;
+            const int lf = s / NFP, k = s - lf * NFP;
+            const long long e = ebase + le;
+            float Fn[NQ];
+#pragma unroll
+            for (int f = 0; f < NQ; ++f) Fn[f] = 0.0f;
+            float scale = 0.0f;
+            if (e < a.K) {
+                const int vi = sFmask[lf * NFP + k];
+                float own[NQ];
+#pragma unroll
+                for (int f = 0; f < NQ; ++f) own[f] = sQ[(f * ELEMS + le) * QS + vi];
+                const int2 cn = a.conn[e * NF + lf];
+                const float4 g4 = *reinterpret_cast<const float4 *>(&a.fgeo[(e * NF + lf) * 4]);
+                const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
+                float n[DIM];
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) n[x] = gg[x];
+                scale = gg[DIM];
+                float vn0 = 0.0f;
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) vn0 = fmaf(a.v0[x], n[x], vn0);
+                const int kind = (cn.y >> 5) & 3;
+                if (kind == kKindInterior) {
+                    const int nlf = cn.y & 3, pm = (cn.y >> 2) & 7;
+                    const float tau = (cn.y & 128) ? -1.0f : 1.0f;
+                    const int nvi = sFmask[nlf * NFP + sPerm[pm * NFP + k]];
+                    const long long nb = (long long)cn.x * NP + nvi;
+                    float o[NQ];
+#pragma unroll
+                    for (int f = 0; f < NQ; ++f) o[f] = __ldg(&a.win[f * a.fstride + nb]);
+                    const float sp = own[0] + o[0];
+                    float svn = 0.0f;
+#pragma unroll
+                    for (int x = 0; x < DIM; ++x) svn = fmaf(own[1 + x] + o[1 + x], n[x], svn);
+                    const float hj = a.half_c0 * tau;
+                    Fn[0] = fmaf(hj, own[0] - o[0], 0.5f * fmaf(vn0, sp, a.rc2 * svn));
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d)
+                        Fn[1 + d] = fmaf(hj, own[1 + d] - o[1 + d],
+                                         0.5f * fmaf(vn0, own[1 + d] + o[1 + d], a.inv_rho * sp * n[d]));
+                } else if (kind == kKindReflecting) {
+                    float vn = 0.0f;
+#pragma unroll
+                    for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
+                    float vw[DIM], vwn = 0.0f;
+#pragma unroll
+                    for (int x = 0; x < DIM; ++x) {
+                        vw[x] = own[1 + x] - vn * n[x];
+                        vwn = fmaf(vw[x], n[x], vwn);
+                    }
+                    Fn[0] = fmaf(vn0, own[0], a.rc2 * vwn);
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) Fn[1 + d] = fmaf(vn0, vw[d], a.inv_rho * own[0] * n[d]);
+                } else {
+                    float vn = 0.0f;
+#pragma unroll
+                    for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
+                    const float q0 = 0.25f * a.c0;
+                    Fn[0] = fmaf(q0, own[0], 0.25f * a.c0 * a.c0 * a.rho * vn);
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) Fn[1 + d] = fmaf(0.25f * n[d] * a.inv_rho, own[0], q0 * n[d] * vn);
+                }
+            }
+#pragma unroll
+            for (int f = 0; f < NQ; ++f) sFn[(le * NSLOT + s) * 4 + f] = -scale * Fn[f];
+        }
+        __syncthreads();
+
+        // 3. A rows: contravariant fluxes and face values, sliced into tensor memory
+        const int r = tid;                      // row (warps 0-3)
+        const int f = r / ELEMS, le = r - f * ELEMS;
+        const bool row_ok = (warp < 4) && (f < NQ) && (ebase + le < a.K);
+        int ea = 0;
+        float Bg[DIM][DIM], au[DIM];
+        if (warp < 4) {
+            const long long e = ebase + le;
+#pragma unroll
+            for (int x = 0; x < DIM; ++x)
+#pragma unroll
+                for (int u = 0; u < DIM; ++u) Bg[x][u] = row_ok ? (float)a.geo[e * DIM * DIM + x * DIM + u] : 0.0f;
+#pragma unroll
+            for (int u = 0; u < DIM; ++u) {
+                float s = 0.0f;
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) s = fmaf(Bg[x][u], a.v0[x], s);
+                au[u] = s;
+            }
+        }
+        // value of A[r][k]
+        auto aval = [&](int k) -> float {
+            if (!row_ok || k >= KTOT) return 0.0f;
+            if (k < DIM * NP) {
+                const int u = k / NP, j = k - u * NP;
+                const float *q = &sQ[le * QS + j];
+                const float p = q[0];
+                if (f == 0) {
+                    float w = 0.0f;
+#pragma unroll
+                    for (int x = 0; x < DIM; ++x) w = fmaf(Bg[x][u], q[(1 + x) * ELEMS * QS], w);
+                    return fmaf(au[u], p, a.rc2 * w);
+                }
+                const float vd = q[f * ELEMS * QS];
+                return fmaf(au[u], vd, a.inv_rho * p * Bg[f - 1][u]);
+            }
+            return sFn[(le * NSLOT + (k - DIM * NP)) * 4 + f];
+        };
+        if (warp < 4) {
+            float amax = 0.0f;
+            for (int k = 0; k < KTOT; ++k) amax = fmaxf(amax, fabsf(aval(k)));
+            if (amax > 0.0f) frexpf(amax, &ea);
+            for (int c = 0; c < KSTEPS; ++c) {
+                uint32_t w[4][8];
+#pragma unroll
+                for (int h = 0; h < 8; ++h) {
+                    float m[2][4];
+#pragma unroll
+                    for (int t = 0; t < 2; ++t) {
+                        float x = ldexpf(aval(c * 16 + 2 * h + t), -ea) * 256.0f;
+#pragma unroll
+                        for (int sl = 0; sl < 4; ++sl) {
+                            const float mi = rintf(x);
+                            m[t][sl] = mi;
+                            x = (x - mi) * 256.0f;
+                        }
+                    }
+#pragma unroll
+                    for (int sl = 0; sl < 4; ++sl) {
+                        const float sc = sl == 0 ? 1.0f : sl == 1 ? 0.00390625f : sl == 2 ? 1.52587890625e-05f
+                                                                                        : 5.9604644775390625e-08f;
+                        w[sl][h] = dgtc::pack_bf16(m[0][sl] * sc, m[1][sl] * sc);
+                    }
+                }
+                __syncwarp();
+#pragma unroll
+                for (int sl = 0; sl < 4; ++sl)
+                    dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, sl * ACOLS + c * 8), w[sl]);
+            }
+            dgtc::tmem_st_wait();
+        }
+        dgtc::fence_before_sync();
+        __syncthreads();
+
+        // 4. tensor-core contraction: 13 slice pairs x KSTEPS
+        if (tid == 128) {
+            dgtc::fence_after_sync();
+            bool first[3] = {true, true, true};
+#pragma unroll 1
+            for (int pi = 0; pi < 13; ++pi) {
+                const int ia = kPairA[pi], jb = kPairB[pi];
+                const int slot = (ia + jb) < 2 ? (ia + jb) : 2;
+                const uint32_t d = tbase + MS::ACC + slot * NPAD;
+#pragma unroll 1
+                for (int t = 0; t < KSTEPS; ++t) {
+                    const uint64_t bd = dgtc::desc_kmajor(sB + (jb * KSTEPS + t) * MS::BTILE, 128, 256);
+                    dgtc::mma_bf16_ts(d, tbase + ia * ACOLS + t * 8, bd, idesc, first[slot] ? 0u : 1u);
+                    first[slot] = false;
+                }
+            }
+            dgtc::mma_commit(bar);
+        }
+        __syncwarp();
+
+        // 5. epilogue: combine the accumulators, RK4 stage update
+        if (warp < 4 && !dgtc::mbar_wait_bounded(bar, phase, 1u << 24)) *sFail = 1;
+        phase ^= 1u;
+        __syncthreads();
+        if (*sFail) {
+            alive = false;
+        } else if (warp < 4) {
+            dgtc::fence_after_sync();
+            const long long base = f * a.fstride + (ebase + le) * NP;
+#pragma unroll 1
+            for (int c = 0; c < NPAD; c += 16) {
+                uint32_t v0[16], v1[16], v2[16];
+                __syncwarp();
+                dgtc::tmem_ld16(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 0 * NPAD + c), v0);
+                dgtc::tmem_ld16(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 1 * NPAD + c), v1);
+                dgtc::tmem_ld16(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 2 * NPAD + c), v2);
+                dgtc::tmem_ld_wait();
+#pragma unroll 4
+                for (int t = 0; t < 16; ++t) {
+                    const int i = c + t;
+                    if (!row_ok || i >= NP) break;
+                    float hi, lo;
+                    two_sum(__uint_as_float(v0[t]), __uint_as_float(v1[t]), hi, lo);
+                    lo += __uint_as_float(v2[t]);
+                    const float sc = ldexpf(a.dt, ea + sEb[i] - 16);
+                    const float rr = fmaf(sc, hi, sc * lo);
+                    const long long idx = base + i;
+                    if (STAGE == 1) {
+                        a.acc[idx] = rr;
+                        a.wout[idx] = a.u[idx] + (a.ulo[idx] + 0.5f * rr);
+                    } else if (STAGE == 2) {
+                        a.acc[idx] = fmaf(2.0f, rr, a.acc[idx]);
+                        a.wout[idx] = a.u[idx] + (a.ulo[idx] + 0.5f * rr);
+                    } else if (STAGE == 3) {
+                        a.acc[idx] = fmaf(2.0f, rr, a.acc[idx]);
+                        a.wout[idx] = a.u[idx] + (a.ulo[idx] + rr);
+                    } else {
+                        const float dlt = (a.acc[idx] + rr) * (1.0f / 6.0f);
+                        float s, e;
+                        two_sum(a.u[idx], dlt, s, e);
+                        e += a.ulo[idx];
+                        const float nh = s + e;
+                        a.wout[idx] = nh;
+                        a.ulo[idx] = e - (nh - s);
+                    }
+                }
+            }
+        }
+        dgtc::fence_before_sync();
+        __syncthreads();
+    }
+    if (!alive) {
+        // the MMAs of the failed tile may still be in flight: wait once more
+        // (bounded) before releasing tensor memory
+        if (tid == 0) {
+            atomicExch(a.err, 1);
+            dgtc::mbar_wait_bounded(bar, phase ^ 1u, 1u << 24);
+        }
+    }
+    dgtc::fence_after_sync();
+    __syncthreads();
+    if (warp == 0) dgtc::tmem_dealloc(tbase, MS::TMEM_COLS);
+}
+
+}  // namespace dgk

@@ -41,6 +41,19 @@ __global__ void uncast_kernel(const Real *src, double *dst, long long n) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     for (; i < n; i += (long long)gridDim.x * blockDim.x) dst[i] = double(src[i]);
 }
+// State kept as an FP32 pair (mixed form): x = hi + lo.
+__global__ void split_kernel(const double *src, float *hi, float *lo, long long n) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float h = float(src[i]);
+        hi[i] = h;
+        lo[i] = float(src[i] - double(h));
+    }
+}
+__global__ void join_kernel(const float *hi, const float *lo, double *dst, long long n) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; i < n; i += (long long)gridDim.x * blockDim.x) dst[i] = double(hi[i]) + double(lo[i]);
+}
 
 // FP64 monitors: thread per element, u^T M u per field, non-finite count.
 template <typename Real>
@@ -107,6 +120,13 @@ struct dg_ctx {
     std::vector<double> src_duration;
     dgk::KernelSet ks;
     int grid = 0;
+    // mixed form
+    bool mixed = false;
+    dgk::MixedKernelSet mks;
+    float *d_ulo = nullptr;      // low part of the state pair
+    uint8_t *d_bimg = nullptr;   // sliced operator image
+    int *d_beb = nullptr;        // operator row exponents
+    int *d_err = nullptr;        // device-side error flag (wait timeouts)
     // graph cache
     cudaGraphExec_t gexec = nullptr;
     double graph_dt = 0;
@@ -133,7 +153,7 @@ void free_ctx(dg_ctx *c) {
     for (auto ev : c->events) cudaEventDestroy(ev);
     void *ptrs[] = {c->d_state, c->d_geo, c->d_fgeo, c->d_conn, c->d_ops, c->d_tabs, c->d_t0, c->d_stage64,
                     c->d_mass, c->d_detj, c->d_mon, c->d_bad, c->d_src_dof, c->d_src_off, c->d_src_list,
-                    c->d_src_params};
+                    c->d_src_params, c->d_ulo, c->d_bimg, c->d_beb, c->d_err};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -169,6 +189,35 @@ void fill_args(dg_ctx *c, dgk::StageArgs<Real> &a, int stage, double dt) {
 }
 
 cudaError_t launch_stage(dg_ctx *c, int stage, double dt) {
+    if (c->mixed) {
+        dgk::MixedArgs a;
+        dgk::StageArgs<float> s;
+        fill_args<float>(c, s, stage, dt);
+        a.win = s.win;
+        a.u = s.u;
+        a.ulo = c->d_ulo;
+        a.acc = s.acc;
+        a.wout = s.wout;
+        a.fstride = s.fstride;
+        a.geo = s.geo;
+        a.fgeo = s.fgeo;
+        a.conn = s.conn;
+        a.bimg = c->d_bimg;
+        a.beb = c->d_beb;
+        a.tabs = s.tabs;
+        a.K = s.K;
+        a.dt = s.dt;
+        a.rc2 = s.rc2;
+        a.inv_rho = s.inv_rho;
+        a.half_c0 = s.half_c0;
+        a.c0 = s.c0;
+        a.rho = s.rho;
+        for (int k = 0; k < 3; ++k) a.v0[k] = s.v0[k];
+        a.err = c->d_err;
+        void *args[] = {&a};
+        return cudaLaunchKernel(c->mks.stage[stage], dim3(c->grid), dim3(c->mks.threads), args, c->mks.smem,
+                                c->stream);
+    }
     dim3 grid(c->grid, 1, 1), block(c->ks.threads, 1, 1);
     if (c->prec == DG_PREC_FP64) {
         dgk::StageArgs<double> a;
@@ -189,8 +238,9 @@ cudaError_t launch_inject(dg_ctx *c, int kstep, double dt) {
     long long bstride = 0;
     void *p = c->d_u;  // field 0 of u
     int nn = c->src_nodes;
+    void *plo = c->d_ulo;  // null unless the state is kept as a pair
     void *args[] = {&p, &bstride, &c->d_src_dof, &c->d_src_off, &c->d_src_list, &c->d_src_params, &c->d_t0,
-                    &kstep, &dt, &nn};
+                    &kstep, &dt, &nn, &plo};
     return cudaLaunchKernel(c->ks.inject, grid, block, args, 0, c->stream);
 }
 
@@ -227,7 +277,7 @@ int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts
     else dg_default_opts(&opts);
     if (m->dim != 2 && m->dim != 3) return fail(DG_ERR_UNSUPPORTED, "dimension must be 2 or 3");
     if (m->order < 1 || m->order > 5) return fail(DG_ERR_UNSUPPORTED, "order must be in 1..5");
-    if (opts.precision != DG_PREC_FP64 && opts.precision != DG_PREC_FP32)
+    if (opts.precision != DG_PREC_FP64 && opts.precision != DG_PREC_FP32 && opts.precision != DG_PREC_MIXED)
         return fail(DG_ERR_ARG, "unknown precision");
     if (opts.flux_sign != DG_FLUX_REFERENCE && opts.flux_sign != DG_FLUX_UPWIND)
         return fail(DG_ERR_ARG, "unknown flux sign mode");
@@ -251,9 +301,15 @@ int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts
     c->rsize = c->prec == DG_PREC_FP64 ? 8 : 4;
     c->c0 = ph->c0; c->rho0 = ph->rho0;
     for (int k = 0; k < 3; ++k) c->v0[k] = ph->v0[k];
-    if (!dgk::get_kernels(c->prec, dim, m->order, &c->ks)) {
+    c->mixed = c->prec == DG_PREC_MIXED;
+    // the mixed form keeps FP32 stage data and uses the FP32 helper kernels
+    if (!dgk::get_kernels(c->mixed ? DG_PREC_FP32 : c->prec, dim, m->order, &c->ks)) {
         free_ctx(c);
         return fail(DG_ERR_UNSUPPORTED, "no kernel compiled for this order");
+    }
+    if (c->mixed && !dgk::get_mixed_kernels(dim, m->order, &c->mks)) {
+        free_ctx(c);
+        return fail(DG_ERR_UNSUPPORTED, "the mixed form supports orders 1-4 in 3D and 1-5 in 2D");
     }
     int rc = DG_OK;
     auto fin = [&](cudaError_t e, const char *what) {
@@ -314,6 +370,29 @@ int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts
         if (!fin(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device), "attribute")) break;
         int ntiles = (K + c->ks.epb - 1) / c->ks.epb;
         c->grid = std::max(1, std::min(ntiles, std::max(per_sm, 1) * nsm));
+        if (c->mixed) {
+            if (!fin(cudaMalloc(&c->d_ulo, field_bytes * c->nq), "cudaMalloc(ulo)")) break;
+            if (!fin(cudaMemsetAsync(c->d_ulo, 0, field_bytes * c->nq, c->stream), "cudaMemset")) break;
+            std::vector<uint8_t> img;
+            std::vector<int> eb;
+            c->mks.b_image(lay.ops.data(), img, eb);
+            if (!fin(cudaMalloc(&c->d_bimg, img.size()), "cudaMalloc(bimg)")) break;
+            if (!fin(cudaMemcpy(c->d_bimg, img.data(), img.size(), cudaMemcpyHostToDevice), "copy bimg")) break;
+            if (!fin(cudaMalloc(&c->d_beb, eb.size() * sizeof(int)), "cudaMalloc(beb)")) break;
+            if (!fin(cudaMemcpy(c->d_beb, eb.data(), eb.size() * sizeof(int), cudaMemcpyHostToDevice), "copy beb"))
+                break;
+            if (!fin(cudaMalloc(&c->d_err, sizeof(int)), "cudaMalloc(err)")) break;
+            if (!fin(cudaMemset(c->d_err, 0, sizeof(int)), "cudaMemset(err)")) break;
+            for (int s = 0; s < 4; ++s)
+                if (!fin(cudaFuncSetAttribute(c->mks.stage[s], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)c->mks.smem),
+                         "cudaFuncSetAttribute(mixed)"))
+                    break;
+            if (rc != DG_OK) break;
+            // one CTA per SM: each owns the SM's tensor memory
+            int mtiles = (K + c->mks.elems_per_tile - 1) / c->mks.elems_per_tile;
+            c->grid = std::max(1, std::min(mtiles, nsm));
+        }
         if (!fin(cudaStreamSynchronize(c->stream), "sync")) break;
     } while (0);
     if (rc != DG_OK) {
@@ -342,7 +421,11 @@ int dg_set_state(dg_ctx *c, const double *const u[4]) {
             CK(cudaMemcpyAsync(dst, u[f], fb, cudaMemcpyHostToDevice, c->stream));
         } else {
             CK(cudaMemcpyAsync(c->d_stage64, u[f], (size_t)c->ndof * 8, cudaMemcpyHostToDevice, c->stream));
-            cast_kernel<float><<<1024, 256, 0, c->stream>>>(c->d_stage64, (float *)dst, c->ndof);
+            if (c->mixed)
+                split_kernel<<<1024, 256, 0, c->stream>>>(c->d_stage64, (float *)dst, c->d_ulo + f * c->ndof,
+                                                          c->ndof);
+            else
+                cast_kernel<float><<<1024, 256, 0, c->stream>>>(c->d_stage64, (float *)dst, c->ndof);
             CK(cudaGetLastError());
         }
     }
@@ -360,7 +443,11 @@ int dg_get_state(dg_ctx *c, double *const u[4]) {
         if (c->prec == DG_PREC_FP64) {
             CK(cudaMemcpyAsync(u[f], src, fb, cudaMemcpyDeviceToHost, c->stream));
         } else {
-            uncast_kernel<float><<<1024, 256, 0, c->stream>>>((const float *)src, c->d_stage64, c->ndof);
+            if (c->mixed)
+                join_kernel<<<1024, 256, 0, c->stream>>>((const float *)src, c->d_ulo + f * c->ndof, c->d_stage64,
+                                                         c->ndof);
+            else
+                uncast_kernel<float><<<1024, 256, 0, c->stream>>>((const float *)src, c->d_stage64, c->ndof);
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(u[f], c->d_stage64, (size_t)c->ndof * 8, cudaMemcpyDeviceToHost, c->stream));
         }
@@ -464,6 +551,21 @@ int enqueue_steps(dg_ctx *c, double *t, double dt, int nsteps) {
 
 extern "C" {
 
+}  // extern "C"
+
+namespace {
+// Device-side error flag of the mixed kernels (a bounded wait that ran out).
+int check_device_error(dg_ctx *c) {
+    if (!c->d_err) return DG_OK;
+    int h = 0;
+    CK(cudaMemcpy(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) return fail(DG_ERR_CUDA, "tensor-core stage kernel: an MMA completion wait timed out");
+    return DG_OK;
+}
+}  // namespace
+
+extern "C" {
+
 int dg_rk4_steps(dg_ctx *c, double *t, double dt, int nsteps) {
     if (!c || !t || nsteps < 0) return fail(DG_ERR_ARG, "bad step arguments");
     if (!(dt > 0) || !std::isfinite(dt)) return fail(DG_ERR_ARG, "dt must be positive and finite");
@@ -471,7 +573,7 @@ int dg_rk4_steps(dg_ctx *c, double *t, double dt, int nsteps) {
     int rc = enqueue_steps(c, t, dt, nsteps);
     if (rc != DG_OK) return rc;
     CK(cudaStreamSynchronize(c->stream));
-    return DG_OK;
+    return check_device_error(c);
 }
 
 int dg_rk4_steps_timed(dg_ctx *c, double *t, double dt, int nsteps, double *ms) {
@@ -493,7 +595,8 @@ int dg_rk4_steps_timed(dg_ctx *c, double *t, double dt, int nsteps, double *ms) 
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    return rc;
+    if (rc != DG_OK) return rc;
+    return check_device_error(c);
 }
 
 int dg_profile_steps(dg_ctx *c, double *t, double dt, int nsteps, dg_kernel_times *out) {
@@ -539,7 +642,7 @@ int dg_profile_steps(dg_ctx *c, double *t, double dt, int nsteps, dg_kernel_time
     CK(cudaEventElapsedTime(&tot, c->events[0], c->events[2 * kind.size() - 1]));
     out->total_ms = tot;
     *t = tt;
-    return DG_OK;
+    return check_device_error(c);
 }
 
 int dg_monitors(dg_ctx *c, double *energy, double *l2, long long *status) {

@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(EPB *Shape<DIM, P>::NP)
 template <typename Real>
 __global__ void inject_kernel(Real *p, long long bstride, const int *node_dof, const int *node_src_off,
                               const int *node_src, const double *params, const double *t0, int kstep, double dt,
-                              int nnodes) {
+                              int nnodes, Real *plo) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nnodes) return;
     double t = *t0;
@@ -317,7 +317,12 @@ __global__ void inject_kernel(Real *p, long long bstride, const int *node_dof, c
             set = true;
         }
     }
-    if (set) p[(long long)blockIdx.y * bstride + node_dof[j]] = Real(val);
+    if (set) {
+        const long long at = (long long)blockIdx.y * bstride + node_dof[j];
+        p[at] = Real(val);
+        // state kept as a pair: low part of the injected value
+        if (plo) plo[at] = Real(val - double(Real(val)));
+    }
 }
 
 }  // namespace dgk

@@ -26,7 +26,7 @@ import numpy as np
 PKG = Path(__file__).resolve().parent.parent
 LIB_PATH = PKG / "lib" / "libdgcuda.so"
 
-PREC_FP64, PREC_FP32 = 0, 1
+PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
 FLUX_REFERENCE, FLUX_UPWIND = 0, 1
 ERRORS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "unsupported", -4: "non-finite values",
           -5: "I/O error", -6: "mesh error", -7: "out of memory", -8: "configuration error"}
@@ -127,6 +127,7 @@ def _declare(L: C.CDLL) -> None:
         "dg_layout_build": (C.c_int, [C.POINTER(MeshDesc), C.c_int, C.POINTER(vp)]),
         "dg_layout_get": (C.c_int, [vp, C.POINTER(LayoutView)]),
         "dg_layout_free": (None, [vp]),
+        "dg_tc_selftest": (C.c_int, [C.c_int, P_d]),
         "dgm_read_msh": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
         "dgm_write_msh": (C.c_int, [vp, C.c_char_p]),
         "dgm_box_tri": (C.c_int, [C.c_int, C.c_int, P_d, P_d, C.c_int, C.POINTER(C.c_char_p), C.POINTER(vp)]),
@@ -379,7 +380,7 @@ class Solver:
         ph = PhysDesc(c0, rho0, (C.c_double * 3)(*v0))
         o = Opts()
         lib().dg_default_opts(C.byref(o))
-        o.precision = {"fp64": PREC_FP64, "fp32": PREC_FP32}[precision]
+        o.precision = {"fp64": PREC_FP64, "fp32": PREC_FP32, "mixed": PREC_MIXED}[precision]
         o.flux_sign = {"reference": FLUX_REFERENCE, "upwind": FLUX_UPWIND}[flux]
         o.use_graph = 1 if use_graph else 0
         o.device = device

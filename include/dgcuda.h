@@ -45,6 +45,9 @@ extern "C" {
 
 #define DG_PREC_FP64 0 /* FP64 throughout */
 #define DG_PREC_FP32 1 /* FP32 state and flux, FP64 geometry factors */
+#define DG_PREC_MIXED 2 /* FP32 stage data, state kept as an FP32 pair, volume + lift
+                         * contraction on the tensor cores (BF16 fixed-point slices,
+                         * exact FP32 accumulation); orders 1-4 in 3D, 1-5 in 2D */
 
 #define DG_FLUX_REFERENCE 0 /* interior jump sign fc*orientation, as the reference (Mesh.cpp:524) */
 #define DG_FLUX_UPWIND 1    /* interior jump sign +1 on every face */
@@ -162,6 +165,12 @@ typedef struct dg_layout_view {
 int dg_layout_build(const dg_mesh_desc *mesh, int flux_sign, dg_layout **out);
 int dg_layout_get(const dg_layout *layout, dg_layout_view *view);
 void dg_layout_free(dg_layout *layout);
+
+/* Self-test of the tensor-core primitives of the mixed form (no counterpart
+ * in the reference): a 128x32x112 BF16 GEMM with A in tensor memory and B in
+ * shared memory on the given device; *max_abs_err = 0 when the FP32 result
+ * is exact. */
+int dg_tc_selftest(int device, double *max_abs_err);
 
 /* Message of the last error on this thread. */
 const char *dg_last_error(void);

@@ -103,3 +103,42 @@ def test_fp32_close_to_oracle(dim, order):
     got, ref, dim = run_pair(dim, order, "mixed", precision="fp32", flux="upwind")
     for q in range(dim + 1):
         assert rel_l2(got[q], ref[q]) <= FP32_TOL
+
+
+MIXED_TOL = 1e-7
+
+
+@pytest.mark.parametrize("dim,order", [(2, 1), (2, 2), (2, 3), (2, 4), (2, 5), (3, 1), (3, 2), (3, 3), (3, 4)])
+@pytest.mark.parametrize("bc", ["refl", "mixed"])
+def test_mixed_form_matches_oracle(dim, order, bc):
+    """Tensor-core form: FP32 stage data, exact contraction, state as an FP32
+    pair -- close to FP64 over a short run (tolerance 1e-7 relative L2)."""
+    got, ref, dim = run_pair(dim, order, bc, precision="mixed", flux="upwind", v0=(30.0, -20.0, 10.0))
+    for q in range(dim + 1):
+        assert rel_l2(got[q], ref[q]) <= MIXED_TOL, (q, rel_l2(got[q], ref[q]))
+
+
+def test_mixed_form_with_sources_and_partial_tiles():
+    srcs = [(0.2, 0.1, 0.0, 0.3, 2.0, 1500.0, 0.0, 1e-3)]
+    got, ref, dim = run_pair(2, 3, "refl", sources=srcs, nsteps=40, precision="mixed")
+    for q in range(3):
+        assert rel_l2(got[q], ref[q]) <= MIXED_TOL
+
+
+def test_mixed_form_long_run_against_fp64():
+    """1000 steps of a 3D order-3 box with Mach 0.3 mean flow and absorbing
+    walls (a growing, boundary-driven solution): the mixed form stays within
+    1e-5 relative L2 of the FP64 form."""
+    mesh = D.Mesh.box_tet(6, 6, 6, order=3, side_names=("Absorbing",) * 6)
+    pre = D.Precomp(mesh)
+    v0 = (0.3 * C0, 0.0, 0.0)
+    dt = D.cfl_dt(pre, C0, v0)
+    u0 = pre.initial_state([(0, 0.45, 0.55, 0.5, 2 * 0.05 ** 2, 1.0)])
+    out = {}
+    for prec in ("fp64", "mixed"):
+        s = D.Solver(pre, C0, RHO0, v0, precision=prec, flux="upwind")
+        s.set_state(u0)
+        s.rk4_steps(0.0, dt, 1000)
+        out[prec] = s.get_state()
+    for q in range(4):
+        assert rel_l2(out["mixed"][q], out["fp64"][q]) <= 1e-5
