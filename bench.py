@@ -6,9 +6,11 @@ linearised Euler with uniform mean flow Mach 0.3 along x (c0 = 340,
 rho0 = 1.225), absorbing boundaries, Gaussian pressure pulse sigma = 0.05 at
 a seeded interior point, dt from CFL 0.5.  Four evolved fields (p, vx, vy,
 vz); density is p/c0^2 at output.  A step is one classical RK4 time step
-(four fused stage launches).  The chosen form is FP32 state and flux with
-FP64 geometry factors; the plain FP64 form is measured beside it, and the
-chosen form's error against FP64 is measured after the configuration's 2000
+(four fused stage launches).  The chosen form (--form, default "mixed") keeps
+FP32 stage data, the state as an FP32 pair, and runs the volume + lift
+contraction on the tcgen05 tensor cores with exact fixed-point accumulation;
+the plain FP64 form and the FP32 CUDA-core form are measured beside it, and
+every form's error against FP64 is measured after the configuration's 2000
 steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -199,15 +201,18 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ byte model
-def stage_bytes(pre, real_bytes: int) -> list[float]:
+def stage_bytes(pre, real_bytes: int, pair_state: bool = False) -> list[float]:
     """Algorithmic HBM bytes of each fused stage launch (unique bytes: state
     reads/writes, geometry once; neighbour traces are L2 re-reads).
     Stage 1 reads u, writes acc and w; stages 2-3 read w, u, acc and write
-    acc, w; stage 4 reads w, u, acc and writes u."""
+    acc, w; stage 4 reads w, u, acc and writes u.  With the state kept as an
+    FP32 pair (mixed form) every read of u also reads its low part and stage 4
+    writes both."""
     nq = pre.dim + 1
     n = pre.ndof * nq
     geo = pre.num_el * (pre.dim * pre.dim * 8 + pre.nf * 4 * real_bytes + pre.nf * 8)
-    return [n * real_bytes * k + geo for k in (3, 5, 5, 4)]
+    words = (4, 6, 6, 6) if pair_state else (3, 5, 5, 4)
+    return [n * real_bytes * k + geo for k in words]
 
 
 # ------------------------------------------------------------------ CPU (oracle)
@@ -279,6 +284,37 @@ def reference_arm(args, world, rank, pg):
 
 
 # ------------------------------------------------------------------ GPU arm
+FORMS = {
+    "mixed": ("FP32 stage data, state kept as an FP32 pair, volume + lift contraction on the tcgen05 tensor "
+              "cores with BF16 fixed-point slices and exact FP32 accumulation, FP64 geometry factors",
+              "f32+bf16x4 (exact accumulation)", "mixed_stage_kernel<3,3> (tcgen05 kind::f16, A in TMEM)"),
+    "fp32": ("FP32 state and flux, FP64 geometry factors, fused stage kernel on CUDA cores", "f32",
+             "stage_kernel<3,3,float>"),
+    "fp64": ("FP64 throughout, fused stage kernel on CUDA cores", "f64", "stage_kernel<3,3,double>"),
+}
+
+
+def roofline_for(sol, pre, form, t, dt, nprof):
+    _, prof = sol.profile_steps(t, dt, nprof)
+    real = 8 if form == "fp64" else 4
+    sb = stage_bytes(pre, real, pair_state=(form == "mixed"))
+    avg_ms = [prof["stage_ms"][s] / max(prof["stage_launches"][s], 1) for s in range(4)]
+    achieved = sum(sb) / (sum(avg_ms) * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = ncu_traffic(f"stage_kernel_cube40_p3_{form}.md")
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "peak_source": peak_kind, "algorithmic_bytes_per_launch": sum(sb) / 4,
+            "stage_ms": avg_ms, "kernel": FORMS[form][2]}
+
+
+def timed_form(D, pre, form, u0, dt, v0, local, steps, warmup):
+    sol = D.Solver(pre, C0, RHO0, v0, precision=form, flux=FLUX, device=local)
+    sol.set_state(u0)
+    t = sol.rk4_steps(0.0, dt, warmup)
+    t, ms = sol.rk4_steps_timed(t, dt, steps)
+    return sol, t, ms
+
+
 def ours_arm(args, world, rank, local, pg):
     import dgcuda as D
 
@@ -290,12 +326,11 @@ def ours_arm(args, world, rank, local, pg):
         f"{time.time() - t_setup:.1f}s")
     nq = pre.dim + 1
     dof_stage_per_step = pre.ndof * nq * 4
+    form = args.form
 
-    sol = D.Solver(pre, C0, RHO0, v0, precision="fp32", flux=FLUX, device=local)
+    sol = D.Solver(pre, C0, RHO0, v0, precision=form, flux=FLUX, device=local)
     sol.set_state(u0)
-    t = 0.0
-    if args.warmup:
-        t = sol.rk4_steps(t, dt, args.warmup)
+    t = sol.rk4_steps(0.0, dt, args.warmup)
 
     # timed region: K steps, CUDA events on the solver stream, graph chunks
     barrier(pg)
@@ -308,61 +343,57 @@ def ours_arm(args, world, rank, local, pg):
     units = allreduce_sum(pg, dof_stage_per_step * args.steps)
     value = units / (ms_max * 1e-3)
     e, _, bad = sol.monitors()
-
-    # per-kernel timing of the same workload (events around every launch)
-    _, prof = sol.profile_steps(t, dt, min(args.steps, 200))
-    real = 4
-    sb = stage_bytes(pre, real)
-    avg_ms = [prof["stage_ms"][s] / max(prof["stage_launches"][s], 1) for s in range(4)]
-    achieved = sum(sb) / (sum(avg_ms) * 1e-3) / 1e9
-    peak, peak_kind = measured_peaks()
-    traffic = ncu_traffic("stage_kernel_cube40_p3_fp32.md")
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": sum(sb) / 4, "stage_ms": avg_ms,
-                "kernel": "stage_kernel<3,3,float> (fused volume + face flux + lift + RK4 update)"}
+    roofline = roofline_for(sol, pre, form, t, dt, min(args.steps, 100))
 
     # end to end: every step set_state from pinned host memory, one step,
     # get_state into pinned host memory, through the C ABI
-    n_e2e = 0 if args.no_e2e else args.steps
+    n_e2e = 0 if args.no_e2e else min(args.steps, 200)
     L = D.lib()
     nbytes = 4 * pre.ndof * 8
-    hin = L.dg_host_alloc(nbytes)
-    hout = L.dg_host_alloc(nbytes)
-    if not hin or not hout:
-        raise RuntimeError("pinned host allocation failed")
-    import ctypes as C
+    e2e_value = None
+    if n_e2e:
+        import ctypes as C
 
-    uin = np.ctypeslib.as_array((C.c_double * (4 * pre.ndof)).from_address(hin)).reshape(4, pre.ndof)
-    uout = np.ctypeslib.as_array((C.c_double * (4 * pre.ndof)).from_address(hout)).reshape(4, pre.ndof)
-    uin[:] = u0
-    barrier(pg)
-    sol.synchronize()
-    w0 = time.perf_counter()
-    te = 0.0
-    for _ in range(n_e2e):
-        sol.set_state(uin)
-        te = sol.rk4_steps(te, dt, 1)
-        sol.get_state(uout)
-    sol.synchronize()
-    w1 = time.perf_counter()
-    barrier(pg)
-    e2e_s = allreduce_max(pg, w1 - w0)
-    e2e_value = allreduce_sum(pg, dof_stage_per_step * n_e2e) / e2e_s if n_e2e else None
-    L.dg_host_free(hin)
-    L.dg_host_free(hout)
+        hin, hout = L.dg_host_alloc(nbytes), L.dg_host_alloc(nbytes)
+        if not hin or not hout:
+            raise RuntimeError("pinned host allocation failed")
+        uin = np.ctypeslib.as_array((C.c_double * (4 * pre.ndof)).from_address(hin)).reshape(4, pre.ndof)
+        uout = np.ctypeslib.as_array((C.c_double * (4 * pre.ndof)).from_address(hout)).reshape(4, pre.ndof)
+        uin[:] = u0
+        barrier(pg)
+        sol.synchronize()
+        w0 = time.perf_counter()
+        te = 0.0
+        for _ in range(n_e2e):
+            sol.set_state(uin)
+            te = sol.rk4_steps(te, dt, 1)
+            sol.get_state(uout)
+        sol.synchronize()
+        w1 = time.perf_counter()
+        barrier(pg)
+        e2e_value = allreduce_sum(pg, dof_stage_per_step * n_e2e) / allreduce_max(pg, w1 - w0)
+        L.dg_host_free(hin)
+        L.dg_host_free(hout)
+    sol.close()
 
-    # plain FP64 form on the same workload
-    plain_info, acc = None, None
-    if args.no_plain:
-        args.accuracy_steps = 0
-    plain = None if args.no_plain else D.Solver(pre, C0, RHO0, v0, precision="fp64", flux=FLUX, device=local)
-    if plain is not None:
-        plain_info = plain_form(plain, u0, dt, args, dof_stage_per_step)
-    if plain is not None and args.accuracy_steps > 0:
-        acc = accuracy(D, pre, plain, u0, dt, v0, args, local, nq)
-    if plain is not None:
-        plain.close()
+    # the other forms on the same workload, and the accuracy of every form
+    # against the FP64 form after the configuration's steps
+    others = {}
+    if not args.no_plain:
+        for f2 in ("fp64", "fp32", "mixed"):
+            if f2 == form:
+                continue
+            nsteps = max(5, min(args.steps, 40 if f2 == "fp64" else 400))
+            s2, t2, ms2 = timed_form(D, pre, f2, u0, dt, v0, local, nsteps, 3)
+            others[f2] = {"value": dof_stage_per_step * nsteps / (ms2 * 1e-3), "unit": UNIT,
+                          "ms_per_step": ms2 / nsteps, "form": FORMS[f2][0],
+                          "roofline": roofline_for(s2, pre, f2, t2, dt, 5 if f2 == "fp64" else 40)}
+            s2.close()
+    acc = None
+    if args.accuracy_steps > 0 and not args.no_plain:
+        acc = accuracy_all(D, pre, u0, dt, v0, args, local, nq)
+    if "fp64" in others:
+        others["fp64"]["chosen_over_this"] = value / others["fp64"]["value"]
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -372,14 +403,15 @@ def ours_arm(args, world, rank, local, pg):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "vs_baseline": None, "dtype": FORMS[form][1], "data": "synthetic",
         "config": {"workload": WORKLOAD if args.cells == NCELL else WORKLOAD + f" (profiling case: {args.cells}^3 cells)",
-                   "form": "FP32 state and flux, FP64 geometry factors, fused stage kernel",
-                   "tets": pre.num_el, "dofs_per_field": pre.ndof, "fields": nq, "dt": dt, "flux_sign": FLUX,
+                   "form": FORMS[form][0], "tets": pre.num_el, "dofs_per_field": pre.ndof, "fields": nq, "dt": dt,
+                   "flux_sign": FLUX,
                    "l2": "inputs larger than L2 (FP32 state 4 x %.0f MB)" % (pre.ndof * nq * 4 / 1e6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "plain_fp64": plain_info,
         "accuracy": acc,
+        "plain_fp64": others.get("fp64"),
+        "other_forms": {k: v for k, v in others.items() if k != "fp64"},
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
@@ -388,35 +420,30 @@ def ours_arm(args, world, rank, local, pg):
         "gpu_launches": 4 * args.steps,
         "monitors": {"energy": e, "nonfinite": bad},
     }
-    if plain_info:
-        plain_info["chosen_over_plain"] = value / plain_info["value"]
     print(json.dumps(line), flush=True)
 
 
-def plain_form(plain, u0, dt, args, dof_stage_per_step):
-    plain.set_state(u0)
-    tp = plain.rk4_steps(0.0, dt, 3)
-    n_plain = max(5, min(args.steps, 40))
-    tp, pms = plain.rk4_steps_timed(tp, dt, n_plain)
-    _, pprof = plain.profile_steps(tp, dt, 5)
-    pavg = [pprof["stage_ms"][s] / max(pprof["stage_launches"][s], 1) for s in range(4)]
-    return {"value": dof_stage_per_step * n_plain / (pms * 1e-3), "unit": UNIT, "ms_per_step": pms / n_plain,
-            "stage_ms": pavg}
-
-
-def accuracy(D, pre, plain, u0, dt, v0, args, local, nq):
-    a32 = D.Solver(pre, C0, RHO0, v0, precision="fp32", flux=FLUX, device=local)
-    a32.set_state(u0)
-    plain.set_state(u0)
-    a32.rk4_steps(0.0, dt, args.accuracy_steps)
-    plain.rk4_steps(0.0, dt, args.accuracy_steps)
-    r32, r64 = a32.get_state(), plain.get_state()
-    per = [float(np.linalg.norm(r32[q] - r64[q]) / np.linalg.norm(r64[q])) for q in range(nq)]
-    e64, _, _ = plain.monitors()
-    a32.close()
-    return {"rel_l2_vs_fp64": max(per), "per_field": per, "steps": args.accuracy_steps, "fp64_energy_final": e64,
-            "fp64_vs_oracle": "FP64 GPU form matches the CPU oracle to <=1e-10 relative L2 "
-                              "(tests/test_gpu_parity.py)"}
+def accuracy_all(D, pre, u0, dt, v0, args, local, nq):
+    """Every form after the configuration's steps, relative L2 per field
+    against the FP64 form (which the parity tests tie to the CPU oracle)."""
+    res = {}
+    states = {}
+    for f2 in ("fp64", "mixed", "fp32"):
+        s = D.Solver(pre, C0, RHO0, v0, precision=f2, flux=FLUX, device=local)
+        s.set_state(u0)
+        s.rk4_steps(0.0, dt, args.accuracy_steps)
+        states[f2] = s.get_state()
+        if f2 == "fp64":
+            res["fp64_energy_final"] = s.monitors()[0]
+        s.close()
+    ref = states["fp64"]
+    for f2 in ("mixed", "fp32"):
+        per = [float(np.linalg.norm(states[f2][q] - ref[q]) / np.linalg.norm(ref[q])) for q in range(nq)]
+        res[f2] = {"rel_l2_vs_fp64": max(per), "per_field": per}
+    res["steps"] = args.accuracy_steps
+    res["rel_l2_vs_fp64"] = res[args.form]["rel_l2_vs_fp64"] if args.form != "fp64" else 0.0
+    res["fp64_vs_oracle"] = "FP64 GPU form matches the CPU oracle to <=1e-10 relative L2 (tests/test_gpu_parity.py)"
+    return res
 
 
 def main():
@@ -431,6 +458,7 @@ def main():
     ap.add_argument("--cells", type=int, default=NCELL, help="cube cells per side (profiling cases)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--form", choices=["mixed", "fp32", "fp64"], default="mixed")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least three untimed warm-up steps
     world, rank, local, pg = dist_init()

@@ -1,0 +1,192 @@
+// dgalerkin mesh.msh config.conf -- the reference's command line
+// (src/dgalerkin.cpp:11-63) on the GB300 path.
+//
+// Same flow: read the mesh and the configuration, build the Mesh
+// precompute, set the Gaussian initial conditions (dgalerkin.cpp:37-50), run
+// the time loop of solver::rungeKutta (src/solver.cpp:216-286) with its
+// t / tDisplay accumulation and save cadence, and write the Pressure,
+// Density (p / c0^2) and Velocity views as ElementNodeData to saveFile
+// (solver.cpp:185-191, 225-238, 289-291).  The right-hand side runs through
+// the C ABI of include/dgcuda.h; steps between two saves are one
+// dg_rk4_steps call.  Options the reference does not read: precision
+// (fp64 | fp32 | mixed) and fluxSign (reference | upwind) in the .conf.
+#include <cerrno>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include "../../../include/dgcuda.h"
+#include "config.h"
+#include "mesh_io.h"
+#include "precompute.h"
+
+namespace {
+
+struct Frame {
+    double t;
+    int step;
+    std::vector<double> u;  // [4][ndof]
+};
+
+void log(const std::string &s) { std::printf("Info    : %s\n", s.c_str()); }
+
+bool write_views(const std::string &path, const dg::RawMesh &mesh, const dg::Precomp &pre, const dg::Config &cfg,
+                 const std::vector<Frame> &frames) {
+    std::string err = dg::write_msh(mesh, path);
+    if (!err.empty()) {
+        std::fprintf(stderr, "Error   : %s\n", err.c_str());
+        return false;
+    }
+    FILE *f = std::fopen(path.c_str(), "a");
+    if (!f) return false;
+    const int K = pre.K, np = pre.np;
+    const size_t ndof = (size_t)K * np;
+    const char *names[3] = {"Pressure", "Density", "Velocity"};
+    for (int v = 0; v < 3; ++v) {
+        for (const Frame &fr : frames) {
+            int ncomp = v == 2 ? 3 : 1;
+            std::fprintf(f, "$ElementNodeData\n1\n\"%s\"\n1\n%.17g\n3\n%d\n%d\n%d\n", names[v], fr.t, fr.step, ncomp,
+                         K);
+            for (int e = 0; e < K; ++e) {
+                std::fprintf(f, "%d %d", mesh.el_tags[e], np);
+                for (int n = 0; n < np; ++n) {
+                    size_t i = (size_t)e * np + n;
+                    if (v == 0) std::fprintf(f, " %.17g", fr.u[i]);
+                    else if (v == 1) std::fprintf(f, " %.17g", fr.u[i] / (cfg.c0 * cfg.c0));
+                    else
+                        std::fprintf(f, " %.17g %.17g %.17g", fr.u[ndof + i], fr.u[2 * ndof + i], fr.u[3 * ndof + i]);
+                }
+                std::fprintf(f, "\n");
+            }
+            std::fprintf(f, "$EndElementNodeData\n");
+        }
+    }
+    std::fclose(f);
+    return true;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    if (argc != 3) return E2BIG;
+    const std::string msh = argv[1], conf = argv[2];
+    dg::RawMesh mesh;
+    std::string err = dg::read_msh(msh, mesh);
+    if (!err.empty()) {
+        std::fprintf(stderr, "Error   : %s\n", err.c_str());
+        return EXIT_FAILURE;
+    }
+    dg::Config cfg;
+    err = dg::parse_config(conf, mesh, cfg);
+    if (!err.empty()) {
+        std::fprintf(stderr, "Error   : %s\n", err.c_str());
+        return EXIT_FAILURE;
+    }
+    for (auto &w : cfg.warnings) log(w);
+    std::remove(cfg.saveFile.c_str());
+    log("Config loaded : " + conf);
+    std::vector<std::pair<int, bool>> bcs(cfg.physBCs.begin(), cfg.physBCs.end());
+    dg::Precomp pre;
+    err = dg::precompute(mesh, bcs, pre);
+    if (!err.empty()) {
+        std::fprintf(stderr, "Error   : %s\n", err.c_str());
+        return EXIT_FAILURE;
+    }
+    log("Number of Elements : " + std::to_string(pre.K));
+    log("Element dimension : " + std::to_string(pre.dim));
+    log("Element Order : " + std::to_string(pre.order));
+    log("Number of Faces : " + std::to_string(pre.F));
+    const size_t ndof = (size_t)pre.K * pre.np;
+
+    // initial conditions (dgalerkin.cpp:37-50)
+    std::vector<double> u(4 * ndof, 0.0);
+    for (auto &ic : cfg.initConditions)
+        for (size_t n = 0; n < ndof; ++n) {
+            const double *c = &pre.dof_xyz[n * 3];
+            u[n] += ic[5] * std::exp(-((c[0] - ic[1]) * (c[0] - ic[1]) + (c[1] - ic[2]) * (c[1] - ic[2]) +
+                                       (c[2] - ic[3]) * (c[2] - ic[3])) /
+                                     ic[4]);
+        }
+
+    if (cfg.timeIntMethod != "Runge-Kutta") {
+        std::fprintf(stderr, "Error   : time integration method '%s' is not available on this path (Runge-Kutta)\n",
+                     cfg.timeIntMethod.c_str());
+        return EXIT_FAILURE;
+    }
+    dg_mesh_desc desc;
+    desc.dim = pre.dim; desc.order = pre.order; desc.num_el = pre.K; desc.el_num_nodes = pre.np;
+    desc.f_num = pre.F; desc.f_num_per_el = pre.nf; desc.f_num_nodes = pre.nfp; desc.fc = pre.fc;
+    desc.el_jacobians = pre.el_jac.data(); desc.el_jacobian_dets = pre.el_detj.data();
+    desc.f_normals = pre.f_normal.data(); desc.f_jacobian_dets = pre.f_detj.data();
+    desc.el_f_ids = pre.el_f_ids.data(); desc.el_f_orientation = pre.el_f_orient.data();
+    desc.f_nbr_el_ids = pre.f_nbr.data(); desc.f_n_to_el_n_ids = pre.f_n_to_el_n.data();
+    desc.f_bc = pre.f_bc.data(); desc.f_is_boundary = pre.f_is_bnd.data();
+    dg_phys_desc phys;
+    phys.c0 = cfg.c0; phys.rho0 = cfg.rho0;
+    for (int k = 0; k < 3; ++k) phys.v0[k] = cfg.v0[k];
+    dg_opts opts;
+    dg_default_opts(&opts);
+    opts.precision = cfg.precision == "fp32" ? DG_PREC_FP32 : cfg.precision == "mixed" ? DG_PREC_MIXED : DG_PREC_FP64;
+    opts.flux_sign = cfg.fluxSign == "upwind" ? DG_FLUX_UPWIND : DG_FLUX_REFERENCE;
+    dg_ctx *ctx = nullptr;
+    if (dg_create(&desc, &phys, &opts, &ctx) != DG_OK) {
+        std::fprintf(stderr, "Error   : %s\n", dg_last_error());
+        return EXIT_FAILURE;
+    }
+    const double *uq[4] = {&u[0], &u[ndof], &u[2 * ndof], &u[3 * ndof]};
+    double *uo[4] = {&u[0], &u[ndof], &u[2 * ndof], &u[3 * ndof]};
+    int rc = dg_set_state(ctx, uq);
+    // sources (solver.cpp:197-210)
+    if (rc == DG_OK && !cfg.sources.empty()) {
+        std::vector<int> off(1, 0), idx;
+        std::vector<double> par;
+        for (auto &s : cfg.sources) {
+            for (size_t n = 0; n < ndof; ++n) {
+                const double *c = &pre.dof_xyz[n * 3];
+                if (std::pow(c[0] - s[1], 2) + std::pow(c[1] - s[2], 2) + std::pow(c[2] - s[3], 2) < std::pow(s[4], 2))
+                    idx.push_back((int)n);
+            }
+            off.push_back((int)idx.size());
+            par.insert(par.end(), {s[5], s[6], s[7], s[8]});
+        }
+        if (idx.empty()) idx.push_back(0);
+        rc = dg_set_sources(ctx, (int)cfg.sources.size(), off.data(), idx.data(), par.data());
+    }
+    // time loop (solver.cpp:216-286): saves happen before the step at t
+    std::vector<Frame> frames;
+    auto start = std::chrono::system_clock::now();
+    double t_run = cfg.timeStart;  // time at the start of the pending steps
+    int pending = 0;
+    double t = cfg.timeStart, step = 0, tDisplay = 0;
+    for (; rc == DG_OK && t <= cfg.timeEnd; t += cfg.timeStep, tDisplay += cfg.timeStep, ++step) {
+        if (tDisplay >= cfg.timeRate || step == 0) {
+            tDisplay = 0;
+            if (pending) {
+                rc = dg_rk4_steps(ctx, &t_run, cfg.timeStep, pending);
+                pending = 0;
+                if (rc != DG_OK) break;
+            }
+            rc = dg_get_state(ctx, uo);
+            if (rc != DG_OK) break;
+            frames.push_back({t, (int)step, u});
+            auto el = std::chrono::duration_cast<std::chrono::seconds>(std::chrono::system_clock::now() - start);
+            log("[" + std::to_string(t) + "/" + std::to_string(cfg.timeEnd) + "s] Step number : " +
+                std::to_string((int)step) + ", Elapsed time: " + std::to_string(el.count()) + "s");
+            t_run = t;
+        }
+        ++pending;
+    }
+    if (rc == DG_OK && pending) rc = dg_rk4_steps(ctx, &t_run, cfg.timeStep, pending);
+    if (rc != DG_OK) {
+        std::fprintf(stderr, "Error   : %s\n", dg_last_error());
+        dg_destroy(ctx);
+        return EXIT_FAILURE;
+    }
+    dg_destroy(ctx);
+    if (!write_views(cfg.saveFile, mesh, pre, cfg, frames)) return EXIT_FAILURE;
+    log("Views written to " + cfg.saveFile);
+    return EXIT_SUCCESS;
+}

@@ -59,11 +59,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 // Waits for the phase with the given parity; gives up after max_iter polls
-// (each poll itself suspends for a bounded time) and returns false.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t max_iter) {
-    for (uint32_t it = 0; it < max_iter; ++it)
+// or timeout_ns of wall-clock time, whichever comes first, and returns false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t max_iter,
+                                                  uint64_t timeout_ns = 2000000000ull) {
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t it = 0; it < max_iter; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
+        if (globaltimer_ns() - t0 > timeout_ns) return false;
+    }
     return false;
 }
 

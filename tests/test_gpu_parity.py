@@ -105,14 +105,15 @@ def test_fp32_close_to_oracle(dim, order):
         assert rel_l2(got[q], ref[q]) <= FP32_TOL
 
 
-MIXED_TOL = 1e-7
+MIXED_TOL = 1e-6
 
 
 @pytest.mark.parametrize("dim,order", [(2, 1), (2, 2), (2, 3), (2, 4), (2, 5), (3, 1), (3, 2), (3, 3), (3, 4)])
 @pytest.mark.parametrize("bc", ["refl", "mixed"])
 def test_mixed_form_matches_oracle(dim, order, bc):
     """Tensor-core form: FP32 stage data, exact contraction, state as an FP32
-    pair -- close to FP64 over a short run (tolerance 1e-7 relative L2)."""
+    pair -- close to FP64 over a short run (tolerance 1e-6 relative L2: the
+    stage inputs are rounded to FP32)."""
     got, ref, dim = run_pair(dim, order, bc, precision="mixed", flux="upwind", v0=(30.0, -20.0, 10.0))
     for q in range(dim + 1):
         assert rel_l2(got[q], ref[q]) <= MIXED_TOL, (q, rel_l2(got[q], ref[q]))
