@@ -89,6 +89,12 @@ class LayoutView(C.Structure):
                 ("mass", P_d)]
 
 
+class DeviceLayout(C.Structure):
+    _fields_ = [("dim", C.c_int), ("order", C.c_int), ("num_el", C.c_int), ("c0", C.c_double),
+                ("rho0", C.c_double), ("v0", C.c_double * 3), ("geo", C.c_void_p), ("fgeo", C.c_void_p),
+                ("conn", C.c_void_p), ("ops", C.c_void_p), ("tabs", C.c_void_p)]
+
+
 class RawView(C.Structure):
     _fields_ = [("dim", C.c_int), ("order", C.c_int), ("el_type", C.c_int), ("np", C.c_int),
                 ("num_nodes", C.c_int), ("node_tags", P_i), ("xyz", P_d), ("num_el", C.c_int),
@@ -128,6 +134,8 @@ def _declare(L: C.CDLL) -> None:
         "dg_layout_get": (C.c_int, [vp, C.POINTER(LayoutView)]),
         "dg_layout_free": (None, [vp]),
         "dg_tc_selftest": (C.c_int, [C.c_int, P_d]),
+        "dg_rk4_steps_noalloc": (C.c_int, [C.POINTER(DeviceLayout), C.c_void_p, P_d, C.c_double, C.c_int,
+                                           C.c_void_p]),
         "dgm_read_msh": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
         "dgm_write_msh": (C.c_int, [vp, C.c_char_p]),
         "dgm_box_tri": (C.c_int, [C.c_int, C.c_int, P_d, P_d, C.c_int, C.POINTER(C.c_char_p), C.POINTER(vp)]),

@@ -166,6 +166,37 @@ int dg_layout_build(const dg_mesh_desc *mesh, int flux_sign, dg_layout **out);
 int dg_layout_get(const dg_layout *layout, dg_layout_view *view);
 void dg_layout_free(dg_layout *layout);
 
+/* RK4 steps that allocate no device memory (no counterpart in the reference).
+ *
+ * For callers that must not call cudaMalloc: code inside an application that
+ * hands all device memory out of its own pool (a private cudaMalloc would
+ * fail once the pool has taken the memory, or fragment it), and time loops
+ * that cannot afford the implicit device synchronisation an allocation or a
+ * free may cause.  The caller
+ * owns every array it passes: the FP64 device layout (the arrays
+ * dg_layout_build returns, copied to the device) and the state u (device,
+ * [dim+1][num_el*np], field-major, updated in place).  The three RK4 stage
+ * buffers live in one fixed device array inside the library, 24 MiB, which
+ * every GPU that loads the library holds until the process exits; states of
+ * more than 1,048,576 values (fields x element nodes) are rejected with
+ * DG_ERR_UNSUPPORTED.  Work is enqueued on `stream` (a cudaStream_t, 0 for
+ * the default stream) and not waited for; *t advances by dt per step.
+ * The first call on a device looks up the array's device address (done once
+ * per device, with that device current); make that first call before any
+ * stream capture.  All calls share the one array, which keeps the previous
+ * call's contents (nothing in it needs to start at zero): calls whose work
+ * overlaps on the GPU race on it. */
+typedef struct dg_device_layout {
+    int dim, order, num_el;
+    double c0, rho0, v0[3];
+    const double *geo;          /* device [num_el][dim*dim] */
+    const double *fgeo;         /* device [num_el][nf][4] */
+    const int *conn;            /* device [num_el][nf][2] */
+    const double *ops;          /* device, D then LIFT as in dg_layout_view */
+    const unsigned char *tabs;  /* device face masks then permutations */
+} dg_device_layout;
+int dg_rk4_steps_noalloc(const dg_device_layout *layout, double *u, double *t, double dt, int nsteps, void *stream);
+
 /* Self-test of the tensor-core primitives of the mixed form (no counterpart
  * in the reference): a 128x32x112 BF16 GEMM with A in tensor memory and B in
  * shared memory on the given device; *max_abs_err = 0 when the FP32 result
