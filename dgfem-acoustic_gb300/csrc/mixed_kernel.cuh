@@ -17,14 +17,19 @@
 // epilogue adds the three in double-FP32, scales by 2^(ea+eb-16) dt and
 // applies the RK4 stage update with the state u kept as an FP32 pair.
 //
-// Roles: all threads stage the tile's state and compute the face values into
-// shared memory; warps 0-3 (one thread per row, warp w <-> tensor-memory lanes
-// 32w..32w+31) build their A row, store the slices with tcgen05.st, and after
-// the MMAs read the accumulators with tcgen05.ld for the epilogue; one thread
-// issues the 13 x KSTEPS tcgen05.mma and commits them to an mbarrier.
-// Every wait is bounded; on timeout the kernel records an error and stops.
+// Roles (256 threads, one CTA per SM, persistent over tiles): all threads
+// stage the tile's state, then build the A rows in shared memory (one task per
+// element node for the volume fluxes, one per face slot for the face values).
+// Row r is then sliced by lane r%32 of warps r/32 and r/32+4 (warp w may only
+// touch tensor-memory lanes 32(w%4)..32(w%4)+31), each taking half of the
+// K-steps, and stored with tcgen05.st.  One thread issues the 13 x KSTEPS
+// tcgen05.mma and commits them to an mbarrier; both warp halves then read the
+// accumulators of their row with tcgen05.ld, split by output node, for the
+// epilogue.  Every wait is bounded; on timeout the kernel records an error,
+// waits once more for the MMAs in flight, frees tensor memory and stops.
 #pragma once
 #include <cuda_runtime.h>
+#include <cuda_bf16.h>
 #include <stdint.h>
 
 #include "stage_kernel.cuh"
@@ -50,11 +55,17 @@ struct MixedShape {
     static constexpr int BTILE = NPAD * 32;         // bytes of one (slice, K-step) B tile
     static constexpr int BBYTES = 4 * KSTEPS * BTILE;
     static constexpr int QS = NP + 1;               // padded element stride in the state tile
+    static constexpr int KSTR = KPAD + 1;           // padded row stride of the staged A rows (odd)
+    static constexpr int KS_HALF = (KSTEPS + 1) / 2;  // K-steps sliced by warps 0-3 (rest by 4-7)
+    static constexpr int NHALF = (NP + 1) / 2;      // output nodes per epilogue half
+    static constexpr int NCH = (NHALF + 7) / 8;     // 8-column tensor-memory loads per accumulator
+    static_assert(ACC + 2 * NPAD + NHALF + 8 * NCH <= TMEM_COLS, "epilogue loads stay inside the allocation");
     // shared memory layout (bytes)
     static constexpr int OFF_B = 0;
     static constexpr int OFF_Q = OFF_B + BBYTES;
-    static constexpr int OFF_FN = OFF_Q + NQ * ELEMS * QS * 4;
-    static constexpr int OFF_TAB = OFF_FN + ELEMS * NSLOT * 4 * 4;
+    static constexpr int OFF_A = OFF_Q + NQ * ELEMS * QS * 4;
+    static constexpr int OFF_MAX = OFF_A + 128 * KSTR * 4;
+    static constexpr int OFF_TAB = OFF_MAX + 2 * 128 * 4;
     static constexpr int OFF_EB = (OFF_TAB + S::NTAB + 15) / 16 * 16;
     static constexpr int OFF_BAR = OFF_EB + NPAD * 4;
     static constexpr int SMEM = OFF_BAR + 16;
@@ -75,16 +86,50 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
+// Exponent e with |x| < 2^e for the largest |x| of a row (frexp convention);
+// 0 for a zero row.
+__device__ __forceinline__ int row_exponent(float amax) {
+    const unsigned bits = __float_as_uint(amax);
+    if (amax == 0.0f) return 0;
+    const int ef = (int)((bits >> 23) & 0xffu);
+    return ef == 0 ? -126 : ef - 126;
+}
+
+// 2^k as a float for -126 <= k <= 127.
+__device__ __forceinline__ float exp2i(int k) { return __uint_as_float((unsigned)(k + 127) << 23); }
+
+// Four BF16 fixed-point slices of x*scale (|x*scale| < 256): m0 + m1 2^-8 +
+// m2 2^-16 + m3 2^-24, each m an integer of at most 8 significant bits.
+__device__ __forceinline__ void slice4(float x, float scale, float (&m)[4]) {
+    float y = x * scale;
+    m[0] = rintf(y);
+    y = (y - m[0]) * 256.0f;
+    m[1] = rintf(y);
+    y = (y - m[1]) * 256.0f;
+    m[2] = rintf(y);
+    y = (y - m[2]) * 256.0f;
+    m[3] = rintf(y);
+    m[1] *= 0.00390625f;
+    m[2] *= 1.52587890625e-05f;
+    m[3] *= 5.9604644775390625e-08f;
+}
+
+__device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+
 template <int DIM, int P, int STAGE>
 __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) {
     using MS = MixedShape<DIM, P>;
     constexpr int NP = MS::NP, NF = MS::NF, NFP = MS::NFP, NQ = MS::NQ, NSLOT = MS::NSLOT;
-    constexpr int ELEMS = MS::ELEMS, QS = MS::QS, KTOT = MS::KTOT, KPAD = MS::KPAD, KSTEPS = MS::KSTEPS;
-    constexpr int NPAD = MS::NPAD, ACOLS = MS::ACOLS;
+    constexpr int ELEMS = MS::ELEMS, QS = MS::QS, KTOT = MS::KTOT, KSTEPS = MS::KSTEPS, KSTR = MS::KSTR;
+    constexpr int NPAD = MS::NPAD, ACOLS = MS::ACOLS, NHALF = MS::NHALF, KS_HALF = MS::KS_HALF;
     static_assert(MS::FITS, "tile does not fit in tensor memory");
     extern __shared__ __align__(1024) unsigned char smem[];
     float *sQ = reinterpret_cast<float *>(smem + MS::OFF_Q);
-    float *sFn = reinterpret_cast<float *>(smem + MS::OFF_FN);
+    float *sA = reinterpret_cast<float *>(smem + MS::OFF_A);
+    float *sMax = reinterpret_cast<float *>(smem + MS::OFF_MAX);
     uint8_t *sTab = smem + MS::OFF_TAB;
     int *sEb = reinterpret_cast<int *>(smem + MS::OFF_EB);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + MS::OFF_BAR);
@@ -93,7 +138,7 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
     const uint8_t *sFmask = sTab;
     const uint8_t *sPerm = sTab + NF * NFP;
 
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0) {
         dgtc::tmem_alloc(sTmem, MS::TMEM_COLS);
         dgtc::tmem_relinquish();
@@ -117,6 +162,10 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
     const uint32_t tbase = *sTmem;
     const uint32_t idesc = dgtc::idesc_bf16_f32(128, NPAD);
     const uint32_t sB = dgtc::smem_u32(smem + MS::OFF_B);
+    // row of this thread in phases 3 and 5, and which half of the work
+    const int r = (warp & 3) * 32 + lane;
+    const int half = warp >> 2;
+    const int rf = r / ELEMS, rle = r - rf * ELEMS;
     bool alive = true;
     uint32_t phase = 0;
 
@@ -131,7 +180,35 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
             sQ[(f * ELEMS + le) * QS + j] = ok ? a.win[f * a.fstride + ebase * NP + rem] : 0.0f;
         }
         __syncthreads();
-        // 2. face values, negated and scaled: -(detJf/detJe) Fn
+        // 2a. contravariant fluxes, one task per element node
+        for (int task = tid; task < ELEMS * NP; task += 256) {
+            const int le = task / NP, j = task - le * NP;
+            const long long e = ebase + le;
+            float Bg[DIM][DIM];
+            const bool ok = e < a.K;
+#pragma unroll
+            for (int x = 0; x < DIM; ++x)
+#pragma unroll
+                for (int u = 0; u < DIM; ++u) Bg[x][u] = ok ? (float)__ldg(&a.geo[e * DIM * DIM + x * DIM + u]) : 0.0f;
+            float q[NQ];
+#pragma unroll
+            for (int f = 0; f < NQ; ++f) q[f] = sQ[(f * ELEMS + le) * QS + j];
+#pragma unroll
+            for (int u = 0; u < DIM; ++u) {
+                float au = 0.0f, w = 0.0f;
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) {
+                    au = fmaf(Bg[x][u], a.v0[x], au);
+                    w = fmaf(Bg[x][u], q[1 + x], w);
+                }
+                sA[(0 * ELEMS + le) * KSTR + u * NP + j] = fmaf(au, q[0], a.rc2 * w);
+                const float pr = a.inv_rho * q[0];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    sA[((1 + d) * ELEMS + le) * KSTR + u * NP + j] = fmaf(au, q[1 + d], pr * Bg[d][u]);
+            }
+        }
+        // 2b. face values, negated and scaled: -(detJf/detJe) Fn
         for (int task = tid; task < ELEMS * NSLOT; task += 256) {
             const int le = task / NSLOT, s = task - le * NSLOT;
             const int lf = s / NFP, k = s - lf * NFP;
@@ -198,88 +275,54 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
                 }
             }
 #pragma unroll
-            for (int f = 0; f < NQ; ++f) sFn[(le * NSLOT + s) * 4 + f] = -scale * Fn[f];
+            for (int f = 0; f < NQ; ++f) sA[(f * ELEMS + le) * KSTR + DIM * NP + s] = -scale * Fn[f];
         }
         __syncthreads();
 
-        // 3. A rows: contravariant fluxes and face values, sliced into tensor memory
-        const int r = tid;                      // row (warps 0-3)
-        const int f = r / ELEMS, le = r - f * ELEMS;
-        const bool row_ok = (warp < 4) && (f < NQ) && (ebase + le < a.K);
-        int ea = 0;
-        float Bg[DIM][DIM], au[DIM];
-        if (warp < 4) {
-            const long long e = ebase + le;
-#pragma unroll
-            for (int x = 0; x < DIM; ++x)
-#pragma unroll
-                for (int u = 0; u < DIM; ++u) Bg[x][u] = row_ok ? (float)a.geo[e * DIM * DIM + x * DIM + u] : 0.0f;
-#pragma unroll
-            for (int u = 0; u < DIM; ++u) {
-                float s = 0.0f;
-#pragma unroll
-                for (int x = 0; x < DIM; ++x) s = fmaf(Bg[x][u], a.v0[x], s);
-                au[u] = s;
-            }
+        // 3. slices of the A rows into tensor memory; warps 0-3 take the first
+        //    K-steps of rows 0..127, warps 4-7 the rest of the same rows
+        const bool row_ok = (rf < NQ) && (ebase + rle < a.K);
+        const int ks0 = half ? KS_HALF : 0, ks1 = half ? KSTEPS : KS_HALF;
+        const float *arow = &sA[r * KSTR];
+        {
+            float m = 0.0f;
+            if (row_ok)
+                for (int k = ks0 * 16; k < ks1 * 16 && k < KTOT; ++k) m = fmaxf(m, fabsf(arow[k]));
+            sMax[half * 128 + r] = m;
         }
-        // value of A[r][k]
-        auto aval = [&](int k) -> float {
-            if (!row_ok || k >= KTOT) return 0.0f;
-            if (k < DIM * NP) {
-                const int u = k / NP, j = k - u * NP;
-                const float *q = &sQ[le * QS + j];
-                const float p = q[0];
-                if (f == 0) {
-                    float w = 0.0f;
+        __syncthreads();
+        const int ea = row_exponent(fmaxf(sMax[r], sMax[128 + r]));
+        // rows below 2^-110 are treated as zero (their contribution is far
+        // below the FP32 resolution of any non-negligible row)
+        const bool live = row_ok && ea > -110;
+        const float sc = live ? exp2i(8 - ea) : 0.0f;
+#pragma unroll 1
+        for (int c = ks0; c < ks1; ++c) {
+            uint32_t w[4][8];
 #pragma unroll
-                    for (int x = 0; x < DIM; ++x) w = fmaf(Bg[x][u], q[(1 + x) * ELEMS * QS], w);
-                    return fmaf(au[u], p, a.rc2 * w);
-                }
-                const float vd = q[f * ELEMS * QS];
-                return fmaf(au[u], vd, a.inv_rho * p * Bg[f - 1][u]);
+            for (int h = 0; h < 8; ++h) {
+                const int k = c * 16 + 2 * h;
+                const float x0 = (live && k < KTOT) ? arow[k] : 0.0f;
+                const float x1 = (live && k + 1 < KTOT) ? arow[k + 1] : 0.0f;
+                float m0[4], m1[4];
+                slice4(x0, sc, m0);
+                slice4(x1, sc, m1);
+#pragma unroll
+                for (int sl = 0; sl < 4; ++sl) w[sl][h] = bf16x2_bits(m0[sl], m1[sl]);
             }
-            return sFn[(le * NSLOT + (k - DIM * NP)) * 4 + f];
-        };
-        if (warp < 4) {
-            float amax = 0.0f;
-            for (int k = 0; k < KTOT; ++k) amax = fmaxf(amax, fabsf(aval(k)));
-            if (amax > 0.0f) frexpf(amax, &ea);
-            for (int c = 0; c < KSTEPS; ++c) {
-                uint32_t w[4][8];
+            __syncwarp();
 #pragma unroll
-                for (int h = 0; h < 8; ++h) {
-                    float m[2][4];
-#pragma unroll
-                    for (int t = 0; t < 2; ++t) {
-                        float x = ldexpf(aval(c * 16 + 2 * h + t), -ea) * 256.0f;
-#pragma unroll
-                        for (int sl = 0; sl < 4; ++sl) {
-                            const float mi = rintf(x);
-                            m[t][sl] = mi;
-                            x = (x - mi) * 256.0f;
-                        }
-                    }
-#pragma unroll
-                    for (int sl = 0; sl < 4; ++sl) {
-                        const float sc = sl == 0 ? 1.0f : sl == 1 ? 0.00390625f : sl == 2 ? 1.52587890625e-05f
-                                                                                        : 5.9604644775390625e-08f;
-                        w[sl][h] = dgtc::pack_bf16(m[0][sl] * sc, m[1][sl] * sc);
-                    }
-                }
-                __syncwarp();
-#pragma unroll
-                for (int sl = 0; sl < 4; ++sl)
-                    dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, sl * ACOLS + c * 8), w[sl]);
-            }
-            dgtc::tmem_st_wait();
+            for (int sl = 0; sl < 4; ++sl)
+                dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, sl * ACOLS + c * 8), w[sl]);
         }
+        dgtc::tmem_st_wait();
         dgtc::fence_before_sync();
         __syncthreads();
 
         // 4. tensor-core contraction: 13 slice pairs x KSTEPS
-        if (tid == 128) {
+        if (tid == 0) {
             dgtc::fence_after_sync();
-            bool first[3] = {true, true, true};
+            unsigned started = 0;  // bit per accumulator slot
 #pragma unroll 1
             for (int pi = 0; pi < 13; ++pi) {
                 const int ia = kPairA[pi], jb = kPairB[pi];
@@ -288,40 +331,45 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
 #pragma unroll 1
                 for (int t = 0; t < KSTEPS; ++t) {
                     const uint64_t bd = dgtc::desc_kmajor(sB + (jb * KSTEPS + t) * MS::BTILE, 128, 256);
-                    dgtc::mma_bf16_ts(d, tbase + ia * ACOLS + t * 8, bd, idesc, first[slot] ? 0u : 1u);
-                    first[slot] = false;
+                    dgtc::mma_bf16_ts(d, tbase + ia * ACOLS + t * 8, bd, idesc, (started >> slot) & 1u);
+                    started |= 1u << slot;
                 }
             }
             dgtc::mma_commit(bar);
         }
         __syncwarp();
 
-        // 5. epilogue: combine the accumulators, RK4 stage update
-        if (warp < 4 && !dgtc::mbar_wait_bounded(bar, phase, 1u << 24)) *sFail = 1;
+        // 5. epilogue: accumulators -> stage increment, RK4 stage update;
+        //    warps 0-3 take output nodes [0, NHALF), warps 4-7 the rest
+        if (!dgtc::mbar_wait_bounded(bar, phase, 1u << 30)) *sFail = 1;
         phase ^= 1u;
         __syncthreads();
         if (*sFail) {
             alive = false;
-        } else if (warp < 4) {
+        } else {
             dgtc::fence_after_sync();
-            const long long base = f * a.fstride + (ebase + le) * NP;
-#pragma unroll 1
-            for (int c = 0; c < NPAD; c += 16) {
-                uint32_t v0[16], v1[16], v2[16];
-                __syncwarp();
-                dgtc::tmem_ld16(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 0 * NPAD + c), v0);
-                dgtc::tmem_ld16(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 1 * NPAD + c), v1);
-                dgtc::tmem_ld16(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 2 * NPAD + c), v2);
-                dgtc::tmem_ld_wait();
-#pragma unroll 4
-                for (int t = 0; t < 16; ++t) {
-                    const int i = c + t;
-                    if (!row_ok || i >= NP) break;
+            const int i0 = half * NHALF;
+            constexpr int NCH = MS::NCH;
+            uint32_t v0[8 * NCH], v1[8 * NCH], v2[8 * NCH];
+#pragma unroll
+            for (int c = 0; c < NCH; ++c) {
+                dgtc::tmem_ld8(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 0 * NPAD + i0 + 8 * c), v0 + 8 * c);
+                dgtc::tmem_ld8(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 1 * NPAD + i0 + 8 * c), v1 + 8 * c);
+                dgtc::tmem_ld8(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 2 * NPAD + i0 + 8 * c), v2 + 8 * c);
+            }
+            dgtc::tmem_ld_wait();
+            if (row_ok) {
+                const long long base = rf * a.fstride + (ebase + rle) * NP;
+                const float sdt = live ? a.dt * exp2i(ea - 16) : 0.0f;
+#pragma unroll
+                for (int t = 0; t < NHALF; ++t) {
+                    const int i = i0 + t;
+                    if (i >= NP) break;
                     float hi, lo;
                     two_sum(__uint_as_float(v0[t]), __uint_as_float(v1[t]), hi, lo);
                     lo += __uint_as_float(v2[t]);
-                    const float sc = ldexpf(a.dt, ea + sEb[i] - 16);
-                    const float rr = fmaf(sc, hi, sc * lo);
+                    const float scl = sdt * exp2i(sEb[i]);
+                    const float rr = fmaf(scl, hi, scl * lo);
                     const long long idx = base + i;
                     if (STAGE == 1) {
                         a.acc[idx] = rr;
@@ -347,13 +395,11 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
         dgtc::fence_before_sync();
         __syncthreads();
     }
-    if (!alive) {
+    if (!alive && tid == 0) {
         // the MMAs of the failed tile may still be in flight: wait once more
         // (bounded) before releasing tensor memory
-        if (tid == 0) {
-            atomicExch(a.err, 1);
-            dgtc::mbar_wait_bounded(bar, phase ^ 1u, 1u << 24);
-        }
+        atomicExch(a.err, 1);
+        dgtc::mbar_wait_bounded(bar, phase ^ 1u, 1u << 30);
     }
     dgtc::fence_after_sync();
     __syncthreads();
