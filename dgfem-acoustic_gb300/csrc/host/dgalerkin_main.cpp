@@ -111,10 +111,14 @@ int main(int argc, char **argv) {
                                      ic[4]);
         }
 
-    if (cfg.timeIntMethod != "Runge-Kutta") {
-        std::fprintf(stderr, "Error   : time integration method '%s' is not available on this path (Runge-Kutta)\n",
-                     cfg.timeIntMethod.c_str());
-        return EXIT_FAILURE;
+    // integrator dispatch (dgalerkin.cpp:55-58): "Euler1" (the default) or
+    // "Runge-Kutta"; any other name runs no solver and writes no views
+    int (*run_steps)(dg_ctx *, double *, double, int) = nullptr;
+    if (cfg.timeIntMethod == "Euler1") run_steps = dg_euler_steps;
+    else if (cfg.timeIntMethod == "Runge-Kutta") run_steps = dg_rk4_steps;
+    else {
+        log("Solver '" + cfg.timeIntMethod + "' is not a known method: nothing to run");
+        return EXIT_SUCCESS;
     }
     dg_mesh_desc desc;
     desc.dim = pre.dim; desc.order = pre.order; desc.num_el = pre.K; desc.el_num_nodes = pre.np;
@@ -155,7 +159,8 @@ int main(int argc, char **argv) {
         if (idx.empty()) idx.push_back(0);
         rc = dg_set_sources(ctx, (int)cfg.sources.size(), off.data(), idx.data(), par.data());
     }
-    // time loop (solver.cpp:216-286): saves happen before the step at t
+    // time loop (solver.cpp:216-286, and 107-154 for Euler1): saves happen
+    // before the step at t
     std::vector<Frame> frames;
     auto start = std::chrono::system_clock::now();
     double t_run = cfg.timeStart;  // time at the start of the pending steps
@@ -165,7 +170,7 @@ int main(int argc, char **argv) {
         if (tDisplay >= cfg.timeRate || step == 0) {
             tDisplay = 0;
             if (pending) {
-                rc = dg_rk4_steps(ctx, &t_run, cfg.timeStep, pending);
+                rc = run_steps(ctx, &t_run, cfg.timeStep, pending);
                 pending = 0;
                 if (rc != DG_OK) break;
             }
@@ -179,7 +184,7 @@ int main(int argc, char **argv) {
         }
         ++pending;
     }
-    if (rc == DG_OK && pending) rc = dg_rk4_steps(ctx, &t_run, cfg.timeStep, pending);
+    if (rc == DG_OK && pending) rc = run_steps(ctx, &t_run, cfg.timeStep, pending);
     if (rc != DG_OK) {
         std::fprintf(stderr, "Error   : %s\n", dg_last_error());
         dg_destroy(ctx);

@@ -63,6 +63,7 @@ bool fill(MixedKernelSet *ks) {
         ks->stage[1] = (const void *)&mixed_stage_kernel<DIM, P, 2>;
         ks->stage[2] = (const void *)&mixed_stage_kernel<DIM, P, 3>;
         ks->stage[3] = (const void *)&mixed_stage_kernel<DIM, P, 4>;
+        ks->euler = (const void *)&mixed_stage_kernel<DIM, P, kStageEuler>;
         ks->elems_per_tile = MS::ELEMS;
         ks->threads = 256;
         ks->smem = MS::SMEM_LAUNCH;

@@ -11,6 +11,7 @@ namespace dgk {
 
 struct KernelSet {
     const void *stage[4] = {nullptr, nullptr, nullptr, nullptr};
+    const void *euler = nullptr;  // forward-Euler step kernel
     const void *inject = nullptr;
     int epb = 0;        // elements per block
     int threads = 0;    // threads per block (epb * np)
@@ -32,6 +33,7 @@ namespace dgk {
 // Mixed-precision (tensor-core) stage kernels of one (dimension, order).
 struct MixedKernelSet {
     const void *stage[4] = {nullptr, nullptr, nullptr, nullptr};
+    const void *euler = nullptr;  // forward-Euler step kernel
     int elems_per_tile = 0;
     int threads = 0;
     size_t smem = 0;
@@ -50,6 +52,7 @@ struct MixedArgs {
     float *ulo;            // state, FP32 low part
     float *acc;
     float *wout;           // next stage input (stage 4: u)
+    float *wlo;            // forward-Euler step: low part of the new state
     long long fstride;
     const double *geo;     // [K][DIM*DIM]
     const float *fgeo;     // [K][NF][4]

@@ -20,6 +20,7 @@ bool fill_kernels(KernelSet *ks) {
     ks->stage[1] = (const void *)&stage_kernel<DIM, P, Real, 2, EPB>;
     ks->stage[2] = (const void *)&stage_kernel<DIM, P, Real, 3, EPB>;
     ks->stage[3] = (const void *)&stage_kernel<DIM, P, Real, 4, EPB>;
+    ks->euler = (const void *)&stage_kernel<DIM, P, Real, kStageEuler, EPB>;
     ks->inject = (const void *)&inject_kernel<Real>;
     ks->epb = EPB;
     ks->threads = EPB * Shape<DIM, P>::NP;

@@ -172,12 +172,28 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
     const int ntiles = (a.K + ELEMS - 1) / ELEMS;
     for (int tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x) {
         const long long ebase = (long long)tile * ELEMS;
-        // 1. stage the tile's input state
-        for (int idx = tid; idx < NQ * ELEMS * NP; idx += 256) {
-            const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
-            const int le = rem / NP, j = rem - le * NP;
-            const bool ok = ebase + le < a.K;
-            sQ[(f * ELEMS + le) * QS + j] = ok ? a.win[f * a.fstride + ebase * NP + rem] : 0.0f;
+        // 1. stage the tile's input state (every load issued before the stores)
+        {
+            constexpr int TOT1 = NQ * ELEMS * NP, N1 = (TOT1 + 255) / 256;
+            float v[N1];
+#pragma unroll
+            for (int t = 0; t < N1; ++t) {
+                const int idx = tid + 256 * t;
+                v[t] = 0.0f;
+                if (idx < TOT1) {
+                    const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
+                    if (ebase + rem / NP < a.K) v[t] = __ldg(&a.win[f * a.fstride + ebase * NP + rem]);
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < N1; ++t) {
+                const int idx = tid + 256 * t;
+                if (idx < TOT1) {
+                    const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
+                    const int le = rem / NP, j = rem - le * NP;
+                    sQ[(f * ELEMS + le) * QS + j] = v[t];
+                }
+            }
         }
         __syncthreads();
         // 2a. contravariant fluxes, one task per element node
@@ -208,74 +224,109 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
                     sA[((1 + d) * ELEMS + le) * KSTR + u * NP + j] = fmaf(au, q[1 + d], pr * Bg[d][u]);
             }
         }
-        // 2b. face values, negated and scaled: -(detJf/detJe) Fn
-        for (int task = tid; task < ELEMS * NSLOT; task += 256) {
-            const int le = task / NSLOT, s = task - le * NSLOT;
-            const int lf = s / NFP, k = s - lf * NFP;
-            const long long e = ebase + le;
-            float Fn[NQ];
+        // 2b. face values, negated and scaled: -(detJf/detJe) Fn; the tasks of a
+        //     thread go in groups whose connectivity and neighbour loads are all
+        //     issued before the flux arithmetic
+        {
+            constexpr int TOT2 = ELEMS * NSLOT, NT2 = (TOT2 + 255) / 256, G2 = NT2 < 4 ? NT2 : 4;
+#pragma unroll 1
+            for (int t0 = 0; t0 < NT2; t0 += G2) {
+                int2 cn[G2];
+                float4 g4[G2];
+                float o[G2][NQ];
+                bool val[G2];
 #pragma unroll
-            for (int f = 0; f < NQ; ++f) Fn[f] = 0.0f;
-            float scale = 0.0f;
-            if (e < a.K) {
-                const int vi = sFmask[lf * NFP + k];
-                float own[NQ];
-#pragma unroll
-                for (int f = 0; f < NQ; ++f) own[f] = sQ[(f * ELEMS + le) * QS + vi];
-                const int2 cn = a.conn[e * NF + lf];
-                const float4 g4 = *reinterpret_cast<const float4 *>(&a.fgeo[(e * NF + lf) * 4]);
-                const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
-                float n[DIM];
-#pragma unroll
-                for (int x = 0; x < DIM; ++x) n[x] = gg[x];
-                scale = gg[DIM];
-                float vn0 = 0.0f;
-#pragma unroll
-                for (int x = 0; x < DIM; ++x) vn0 = fmaf(a.v0[x], n[x], vn0);
-                const int kind = (cn.y >> 5) & 3;
-                if (kind == kKindInterior) {
-                    const int nlf = cn.y & 3, pm = (cn.y >> 2) & 7;
-                    const float tau = (cn.y & 128) ? -1.0f : 1.0f;
-                    const int nvi = sFmask[nlf * NFP + sPerm[pm * NFP + k]];
-                    const long long nb = (long long)cn.x * NP + nvi;
-                    float o[NQ];
-#pragma unroll
-                    for (int f = 0; f < NQ; ++f) o[f] = __ldg(&a.win[f * a.fstride + nb]);
-                    const float sp = own[0] + o[0];
-                    float svn = 0.0f;
-#pragma unroll
-                    for (int x = 0; x < DIM; ++x) svn = fmaf(own[1 + x] + o[1 + x], n[x], svn);
-                    const float hj = a.half_c0 * tau;
-                    Fn[0] = fmaf(hj, own[0] - o[0], 0.5f * fmaf(vn0, sp, a.rc2 * svn));
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d)
-                        Fn[1 + d] = fmaf(hj, own[1 + d] - o[1 + d],
-                                         0.5f * fmaf(vn0, own[1 + d] + o[1 + d], a.inv_rho * sp * n[d]));
-                } else if (kind == kKindReflecting) {
-                    float vn = 0.0f;
-#pragma unroll
-                    for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
-                    float vw[DIM], vwn = 0.0f;
-#pragma unroll
-                    for (int x = 0; x < DIM; ++x) {
-                        vw[x] = own[1 + x] - vn * n[x];
-                        vwn = fmaf(vw[x], n[x], vwn);
+                for (int g = 0; g < G2; ++g) {
+                    const int task = tid + 256 * (t0 + g);
+                    const int le = task / NSLOT, lf = (task - le * NSLOT) / NFP;
+                    val[g] = (t0 + g < NT2) && task < TOT2 && ebase + le < a.K;
+                    cn[g] = make_int2(0, kKindAbsorbing << 5);
+                    g4[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (val[g]) {
+                        const long long e = ebase + le;
+                        cn[g] = __ldg(&a.conn[e * NF + lf]);
+                        g4[g] = __ldg(reinterpret_cast<const float4 *>(&a.fgeo[(e * NF + lf) * 4]));
                     }
-                    Fn[0] = fmaf(vn0, own[0], a.rc2 * vwn);
+                }
 #pragma unroll
-                    for (int d = 0; d < DIM; ++d) Fn[1 + d] = fmaf(vn0, vw[d], a.inv_rho * own[0] * n[d]);
-                } else {
-                    float vn = 0.0f;
+                for (int g = 0; g < G2; ++g) {
 #pragma unroll
-                    for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
-                    const float q0 = 0.25f * a.c0;
-                    Fn[0] = fmaf(q0, own[0], 0.25f * a.c0 * a.c0 * a.rho * vn);
+                    for (int f = 0; f < NQ; ++f) o[g][f] = 0.0f;
+                    if (val[g] && ((cn[g].y >> 5) & 3) == kKindInterior) {
+                        const int task = tid + 256 * (t0 + g);
+                        const int s = task - (task / NSLOT) * NSLOT;
+                        const int k = s - (s / NFP) * NFP;
+                        const int nlf = cn[g].y & 3, pm = (cn[g].y >> 2) & 7;
+                        const int nvi = sFmask[nlf * NFP + sPerm[pm * NFP + k]];
+                        const long long nb = (long long)cn[g].x * NP + nvi;
 #pragma unroll
-                    for (int d = 0; d < DIM; ++d) Fn[1 + d] = fmaf(0.25f * n[d] * a.inv_rho, own[0], q0 * n[d] * vn);
+                        for (int f = 0; f < NQ; ++f) o[g][f] = __ldg(&a.win[f * a.fstride + nb]);
+                    }
+                }
+#pragma unroll
+                for (int g = 0; g < G2; ++g) {
+                    const int task = tid + 256 * (t0 + g);
+                    if (t0 + g >= NT2 || task >= TOT2) continue;
+                    const int le = task / NSLOT, s = task - le * NSLOT;
+                    const int lf = s / NFP, k = s - lf * NFP;
+                    float Fn[NQ];
+#pragma unroll
+                    for (int f = 0; f < NQ; ++f) Fn[f] = 0.0f;
+                    float scale = 0.0f;
+                    if (val[g]) {
+                        const int vi = sFmask[lf * NFP + k];
+                        float own[NQ];
+#pragma unroll
+                        for (int f = 0; f < NQ; ++f) own[f] = sQ[(f * ELEMS + le) * QS + vi];
+                        const float gg[4] = {g4[g].x, g4[g].y, g4[g].z, g4[g].w};
+                        float n[DIM];
+#pragma unroll
+                        for (int x = 0; x < DIM; ++x) n[x] = gg[x];
+                        scale = gg[DIM];
+                        float vn0 = 0.0f;
+#pragma unroll
+                        for (int x = 0; x < DIM; ++x) vn0 = fmaf(a.v0[x], n[x], vn0);
+                        const int kind = (cn[g].y >> 5) & 3;
+                        if (kind == kKindInterior) {
+                            const float tau = (cn[g].y & 128) ? -1.0f : 1.0f;
+                            const float sp = own[0] + o[g][0];
+                            float svn = 0.0f;
+#pragma unroll
+                            for (int x = 0; x < DIM; ++x) svn = fmaf(own[1 + x] + o[g][1 + x], n[x], svn);
+                            const float hj = a.half_c0 * tau;
+                            Fn[0] = fmaf(hj, own[0] - o[g][0], 0.5f * fmaf(vn0, sp, a.rc2 * svn));
+#pragma unroll
+                            for (int d = 0; d < DIM; ++d)
+                                Fn[1 + d] = fmaf(hj, own[1 + d] - o[g][1 + d],
+                                                 0.5f * fmaf(vn0, own[1 + d] + o[g][1 + d], a.inv_rho * sp * n[d]));
+                        } else if (kind == kKindReflecting) {
+                            float vn = 0.0f;
+#pragma unroll
+                            for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
+                            float vw[DIM], vwn = 0.0f;
+#pragma unroll
+                            for (int x = 0; x < DIM; ++x) {
+                                vw[x] = own[1 + x] - vn * n[x];
+                                vwn = fmaf(vw[x], n[x], vwn);
+                            }
+                            Fn[0] = fmaf(vn0, own[0], a.rc2 * vwn);
+#pragma unroll
+                            for (int d = 0; d < DIM; ++d) Fn[1 + d] = fmaf(vn0, vw[d], a.inv_rho * own[0] * n[d]);
+                        } else {
+                            float vn = 0.0f;
+#pragma unroll
+                            for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
+                            const float q0 = 0.25f * a.c0;
+                            Fn[0] = fmaf(q0, own[0], 0.25f * a.c0 * a.c0 * a.rho * vn);
+#pragma unroll
+                            for (int d = 0; d < DIM; ++d)
+                                Fn[1 + d] = fmaf(0.25f * n[d] * a.inv_rho, own[0], q0 * n[d] * vn);
+                        }
+                    }
+#pragma unroll
+                    for (int f = 0; f < NQ; ++f) sA[(f * ELEMS + le) * KSTR + DIM * NP + s] = -scale * Fn[f];
                 }
             }
-#pragma unroll
-            for (int f = 0; f < NQ; ++f) sA[(f * ELEMS + le) * KSTR + DIM * NP + s] = -scale * Fn[f];
         }
         __syncthreads();
 
@@ -283,6 +334,20 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
         //    K-steps of rows 0..127, warps 4-7 the rest of the same rows
         const bool row_ok = (rf < NQ) && (ebase + rle < a.K);
         const int ks0 = half ? KS_HALF : 0, ks1 = half ? KSTEPS : KS_HALF;
+        // operands of this thread's RK update, loaded now so that their latency
+        // overlaps the slicing and the contraction
+        const int i0 = half * NHALF;
+        const long long rbase = rf * a.fstride + (ebase + rle) * NP;
+        float pu[NHALF], pl[NHALF], pa[NHALF];
+#pragma unroll
+        for (int t = 0; t < NHALF; ++t) {
+            pu[t] = pl[t] = pa[t] = 0.0f;
+            if (row_ok && i0 + t < NP) {
+                pu[t] = a.u[rbase + i0 + t];
+                pl[t] = a.ulo[rbase + i0 + t];
+                if (STAGE > 1 && STAGE < kStageEuler) pa[t] = a.acc[rbase + i0 + t];
+            }
+        }
         const float *arow = &sA[r * KSTR];
         {
             float m = 0.0f;
@@ -348,7 +413,6 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
             alive = false;
         } else {
             dgtc::fence_after_sync();
-            const int i0 = half * NHALF;
             constexpr int NCH = MS::NCH;
             uint32_t v0[8 * NCH], v1[8 * NCH], v2[8 * NCH];
 #pragma unroll
@@ -359,7 +423,6 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
             }
             dgtc::tmem_ld_wait();
             if (row_ok) {
-                const long long base = rf * a.fstride + (ebase + rle) * NP;
                 const float sdt = live ? a.dt * exp2i(ea - 16) : 0.0f;
 #pragma unroll
                 for (int t = 0; t < NHALF; ++t) {
@@ -370,21 +433,28 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
                     lo += __uint_as_float(v2[t]);
                     const float scl = sdt * exp2i(sEb[i]);
                     const float rr = fmaf(scl, hi, scl * lo);
-                    const long long idx = base + i;
+                    const long long idx = rbase + i;
                     if (STAGE == 1) {
                         a.acc[idx] = rr;
-                        a.wout[idx] = a.u[idx] + (a.ulo[idx] + 0.5f * rr);
+                        a.wout[idx] = pu[t] + (pl[t] + 0.5f * rr);
                     } else if (STAGE == 2) {
-                        a.acc[idx] = fmaf(2.0f, rr, a.acc[idx]);
-                        a.wout[idx] = a.u[idx] + (a.ulo[idx] + 0.5f * rr);
+                        a.acc[idx] = fmaf(2.0f, rr, pa[t]);
+                        a.wout[idx] = pu[t] + (pl[t] + 0.5f * rr);
                     } else if (STAGE == 3) {
-                        a.acc[idx] = fmaf(2.0f, rr, a.acc[idx]);
-                        a.wout[idx] = a.u[idx] + (a.ulo[idx] + rr);
-                    } else {
-                        const float dlt = (a.acc[idx] + rr) * (1.0f / 6.0f);
+                        a.acc[idx] = fmaf(2.0f, rr, pa[t]);
+                        a.wout[idx] = pu[t] + (pl[t] + rr);
+                    } else if (STAGE == kStageEuler) {
                         float s, e;
-                        two_sum(a.u[idx], dlt, s, e);
-                        e += a.ulo[idx];
+                        two_sum(pu[t], rr, s, e);
+                        e += pl[t];
+                        const float nh = s + e;
+                        a.wout[idx] = nh;
+                        a.wlo[idx] = e - (nh - s);
+                    } else {
+                        const float dlt = (pa[t] + rr) * (1.0f / 6.0f);
+                        float s, e;
+                        two_sum(pu[t], dlt, s, e);
+                        e += pl[t];
                         const float nh = s + e;
                         a.wout[idx] = nh;
                         a.ulo[idx] = e - (nh - s);

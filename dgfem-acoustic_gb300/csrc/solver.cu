@@ -30,6 +30,10 @@ bool get_kernels(int prec, int dim, int order, KernelSet *out) {
 namespace {
 
 const int kGraphChunk = 32;
+// Time integrators ("Runge-Kutta" and "Euler1" in the reference's config) and
+// the stage index of the forward-Euler kernel in launch_stage.
+const int kMethodRK4 = 0, kMethodEuler = 1;
+const int kEulerStage = 4;
 
 template <typename Real>
 __global__ void cast_kernel(const double *src, Real *dst, long long n) {
@@ -131,6 +135,7 @@ struct dg_ctx {
     cudaGraphExec_t gexec = nullptr;
     double graph_dt = 0;
     int graph_src = -1;
+    int graph_method = -1;
     // events for profiling
     std::vector<cudaEvent_t> events;
 };
@@ -184,7 +189,8 @@ void fill_args(dg_ctx *c, dgk::StageArgs<Real> &a, int stage, double dt) {
         case 0: a.win = u; a.wout = wa; break;
         case 1: a.win = wa; a.wout = wb; break;
         case 2: a.win = wb; a.wout = wa; break;
-        default: a.win = wa; a.wout = u; break;
+        case 3: a.win = wa; a.wout = u; break;
+        default: a.win = u; a.wout = wa; break;  // forward Euler: u -> wa
     }
 }
 
@@ -198,6 +204,7 @@ cudaError_t launch_stage(dg_ctx *c, int stage, double dt) {
         a.ulo = c->d_ulo;
         a.acc = s.acc;
         a.wout = s.wout;
+        a.wlo = stage == kEulerStage ? static_cast<float *>(c->d_acc) : nullptr;
         a.fstride = s.fstride;
         a.geo = s.geo;
         a.fgeo = s.fgeo;
@@ -215,20 +222,21 @@ cudaError_t launch_stage(dg_ctx *c, int stage, double dt) {
         for (int k = 0; k < 3; ++k) a.v0[k] = s.v0[k];
         a.err = c->d_err;
         void *args[] = {&a};
-        return cudaLaunchKernel(c->mks.stage[stage], dim3(c->grid), dim3(c->mks.threads), args, c->mks.smem,
-                                c->stream);
+        const void *fn = stage == kEulerStage ? c->mks.euler : c->mks.stage[stage];
+        return cudaLaunchKernel(fn, dim3(c->grid), dim3(c->mks.threads), args, c->mks.smem, c->stream);
     }
     dim3 grid(c->grid, 1, 1), block(c->ks.threads, 1, 1);
+    const void *fn = stage == kEulerStage ? c->ks.euler : c->ks.stage[stage];
     if (c->prec == DG_PREC_FP64) {
         dgk::StageArgs<double> a;
         fill_args<double>(c, a, stage, dt);
         void *args[] = {&a};
-        return cudaLaunchKernel(c->ks.stage[stage], grid, block, args, c->ks.smem, c->stream);
+        return cudaLaunchKernel(fn, grid, block, args, c->ks.smem, c->stream);
     } else {
         dgk::StageArgs<float> a;
         fill_args<float>(c, a, stage, dt);
         void *args[] = {&a};
-        return cudaLaunchKernel(c->ks.stage[stage], grid, block, args, c->ks.smem, c->stream);
+        return cudaLaunchKernel(fn, grid, block, args, c->ks.smem, c->stream);
     }
 }
 
@@ -244,8 +252,24 @@ cudaError_t launch_inject(dg_ctx *c, int kstep, double dt) {
     return cudaLaunchKernel(c->ks.inject, grid, block, args, 0, c->stream);
 }
 
-cudaError_t launch_step(dg_ctx *c, int kstep, double dt) {
+// Forward-Euler steps ping-pong between (u, ulo) and (wa, acc): after each
+// step the host swaps the roles so that the next launch reads the new state.
+void swap_euler_buffers(dg_ctx *c) {
+    std::swap(c->d_u, c->d_wa);
+    if (c->mixed) {
+        void *lo = c->d_ulo;
+        c->d_ulo = static_cast<float *>(c->d_acc);
+        c->d_acc = lo;
+    }
+}
+
+cudaError_t launch_step(dg_ctx *c, int kstep, double dt, int method) {
     cudaError_t e = launch_inject(c, kstep, dt);
+    if (method == kMethodEuler) {
+        if (e == cudaSuccess) e = launch_stage(c, kEulerStage, dt);
+        swap_euler_buffers(c);
+        return e;
+    }
     for (int s = 0; s < 4 && e == cudaSuccess; ++s) e = launch_stage(c, s, dt);
     return e;
 }
@@ -357,9 +381,9 @@ int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts
         if (!fin(cudaMalloc(&c->d_bad, 8), "cudaMalloc(bad)")) break;
         if (c->prec != DG_PREC_FP64)
             if (!fin(cudaMalloc(&c->d_stage64, (size_t)c->ndof * 8), "cudaMalloc(staging)")) break;
-        for (int s = 0; s < 4; ++s)
-            if (!fin(cudaFuncSetAttribute(c->ks.stage[s], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)c->ks.smem),
+        for (int s = 0; s < 5; ++s)
+            if (!fin(cudaFuncSetAttribute(s < 4 ? c->ks.stage[s] : c->ks.euler,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->ks.smem),
                      "cudaFuncSetAttribute"))
                 break;
         if (rc != DG_OK) break;
@@ -383,9 +407,9 @@ int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts
                 break;
             if (!fin(cudaMalloc(&c->d_err, sizeof(int)), "cudaMalloc(err)")) break;
             if (!fin(cudaMemset(c->d_err, 0, sizeof(int)), "cudaMemset(err)")) break;
-            for (int s = 0; s < 4; ++s)
-                if (!fin(cudaFuncSetAttribute(c->mks.stage[s], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)c->mks.smem),
+            for (int s = 0; s < 5; ++s)
+                if (!fin(cudaFuncSetAttribute(s < 4 ? c->mks.stage[s] : c->mks.euler,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->mks.smem),
                          "cudaFuncSetAttribute(mixed)"))
                     break;
             if (rc != DG_OK) break;
@@ -503,7 +527,7 @@ int dg_set_sources(dg_ctx *c, int nsrc, const int *offsets, const int *dof_idx, 
 
 namespace {
 // Enqueues nsteps steps on the context stream (graph chunks of kGraphChunk).
-int enqueue_steps(dg_ctx *c, double *t, double dt, int nsteps) {
+int enqueue_steps(dg_ctx *c, double *t, double dt, int nsteps, int method = kMethodRK4) {
     int done = 0;
     while (done < nsteps) {
         int m = std::min(kGraphChunk, nsteps - done);
@@ -514,14 +538,17 @@ int enqueue_steps(dg_ctx *c, double *t, double dt, int nsteps) {
         int with_src = (c->src_nodes && any_source_active(c, t0)) ? 1 : 0;
         CK(cudaMemcpyAsync(c->d_t0, &t0, 8, cudaMemcpyHostToDevice, c->stream));
         if (c->use_graph && m == kGraphChunk) {
-            if (!c->gexec || c->graph_dt != dt || c->graph_src != with_src) {
+            if (!c->gexec || c->graph_dt != dt || c->graph_src != with_src || c->graph_method != method) {
                 if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
                 cudaGraph_t g;
                 CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
                 cudaError_t e = cudaSuccess;
                 int saved = c->src_nodes;
                 if (!with_src) c->src_nodes = 0;
-                for (int k = 0; k < m && e == cudaSuccess; ++k) e = launch_step(c, k, dt);
+                for (int k = 0; k < m; ++k) {
+                    cudaError_t ek = launch_step(c, k, dt, method);
+                    if (e == cudaSuccess) e = ek;
+                }
                 c->src_nodes = saved;
                 cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
                 if (e != cudaSuccess) return cuda_fail(e, "launch during capture");
@@ -531,15 +558,29 @@ int enqueue_steps(dg_ctx *c, double *t, double dt, int nsteps) {
                 if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
                 c->graph_dt = dt;
                 c->graph_src = with_src;
+                c->graph_method = method;
             }
             CK(cudaGraphLaunch(c->gexec, c->stream));
         } else {
             int saved = c->src_nodes;
             if (!with_src) c->src_nodes = 0;
             cudaError_t e = cudaSuccess;
-            for (int k = 0; k < m && e == cudaSuccess; ++k) e = launch_step(c, k, dt);
+            for (int k = 0; k < m; ++k) {
+                cudaError_t ek = launch_step(c, k, dt, method);
+                if (e == cudaSuccess) e = ek;
+            }
             c->src_nodes = saved;
             if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+            if (method == kMethodEuler && (m & 1)) {
+                // an odd number of Euler steps leaves the state in the other
+                // buffer pair: copy it back so the state pointers stay fixed
+                swap_euler_buffers(c);
+                const size_t fb = (size_t)c->ndof * c->rsize * c->nq;
+                CK(cudaMemcpyAsync(c->d_u, c->d_wa, fb, cudaMemcpyDeviceToDevice, c->stream));
+                if (c->mixed)
+                    CK(cudaMemcpyAsync(c->d_ulo, c->d_acc, (size_t)c->ndof * 4 * c->nq, cudaMemcpyDeviceToDevice,
+                                       c->stream));
+            }
         }
         // t0 lives on the host stack: a pageable copy is staged before return
         *t = tend;
@@ -565,6 +606,16 @@ int check_device_error(dg_ctx *c) {
 }  // namespace
 
 extern "C" {
+
+int dg_euler_steps(dg_ctx *c, double *t, double dt, int nsteps) {
+    if (!c || !t || nsteps < 0) return fail(DG_ERR_ARG, "bad step arguments");
+    if (!(dt > 0) || !std::isfinite(dt)) return fail(DG_ERR_ARG, "dt must be positive and finite");
+    CK(cudaSetDevice(c->device));
+    int rc = enqueue_steps(c, t, dt, nsteps, kMethodEuler);
+    if (rc != DG_OK) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return check_device_error(c);
+}
 
 int dg_rk4_steps(dg_ctx *c, double *t, double dt, int nsteps) {
     if (!c || !t || nsteps < 0) return fail(DG_ERR_ARG, "bad step arguments");

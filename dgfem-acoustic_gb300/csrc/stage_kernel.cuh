@@ -47,6 +47,7 @@ struct Shape {
 // 2-4 face permutation, 5-6 kind (0 interior, 1 reflecting, 2 absorbing),
 // 7 negative jump sign.
 enum : int { kKindInterior = 0, kKindReflecting = 1, kKindAbsorbing = 2 };
+enum : int { kStageEuler = 5 };
 
 template <typename Real>
 struct StageArgs {
@@ -95,6 +96,8 @@ __device__ __forceinline__ void load4<double>(const double *p, double (&v)[4]) {
     v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
 }
 
+// STAGE 1-4: the classical RK4 stages; kStageEuler: one forward-Euler step
+// wout = win + dt*RHS(win) (the reference's numStep with beta = 1).
 template <int DIM, int P, typename Real, int STAGE, int EPB>
 __global__ void __launch_bounds__(EPB *Shape<DIM, P>::NP)
     stage_kernel(const StageArgs<Real> a) {
@@ -287,6 +290,8 @@ __global__ void __launch_bounds__(EPB *Shape<DIM, P>::NP)
                 } else if (STAGE == 3) {
                     acc[idx] = fma(Real(2), r, acc[idx]);
                     wout[idx] = uu[idx] + r;
+                } else if (STAGE == kStageEuler) {
+                    wout[idx] = q[f] + r;
                 } else {
                     wout[idx] = uu[idx] + (acc[idx] + r) * (Real(1) / Real(6));
                 }

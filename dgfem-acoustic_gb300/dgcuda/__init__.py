@@ -134,6 +134,7 @@ def _declare(L: C.CDLL) -> None:
         "dg_layout_get": (C.c_int, [vp, C.POINTER(LayoutView)]),
         "dg_layout_free": (None, [vp]),
         "dg_tc_selftest": (C.c_int, [C.c_int, P_d]),
+        "dg_euler_steps": (C.c_int, [vp, P_d, C.c_double, C.c_int]),
         "dg_rk4_steps_noalloc": (C.c_int, [C.POINTER(DeviceLayout), C.c_void_p, P_d, C.c_double, C.c_int,
                                            C.c_void_p]),
         "dgm_read_msh": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
@@ -435,6 +436,12 @@ class Solver:
     def rk4_steps(self, t: float, dt: float, nsteps: int) -> float:
         tt = C.c_double(t)
         _check(lib().dg_rk4_steps(self._h, C.byref(tt), dt, nsteps))
+        return tt.value
+
+    def euler_steps(self, t: float, dt: float, nsteps: int) -> float:
+        """Forward-Euler steps (the reference's "Euler1" integrator)."""
+        tt = C.c_double(t)
+        _check(lib().dg_euler_steps(self._h, C.byref(tt), dt, nsteps))
         return tt.value
 
     def rk4_steps_timed(self, t: float, dt: float, nsteps: int) -> tuple[float, float]:

@@ -120,6 +120,11 @@ int dg_set_sources(dg_ctx *ctx, int nsrc, const int *offsets, const int *dof_idx
  * t += dt in double, as the reference loop does. */
 int dg_rk4_steps(dg_ctx *ctx, double *t, double dt, int nsteps);
 
+/* nsteps forward-Euler steps starting at *t (sources, then u += dt*RHS(u)),
+ * the loop body of solver::forwardEuler (src/solver.cpp:138-153), selected by
+ * timeIntMethod = Euler1 (src/dgalerkin.cpp:55-56; the reference's default). */
+int dg_euler_steps(dg_ctx *ctx, double *t, double dt, int nsteps);
+
 /* dg_rk4_steps bracketed by CUDA events on the solver stream; *ms = device
  * time of the whole run. */
 int dg_rk4_steps_timed(dg_ctx *ctx, double *t, double dt, int nsteps, double *ms);

@@ -15,6 +15,7 @@
 //   updateFlux            src/Mesh.cpp:569-674
 //   numStep               src/solver.cpp:35-52
 //   rungeKutta loop body  src/solver.cpp:197-210, 247-285
+//   forwardEuler body     src/solver.cpp:138-153
 // with the same loops, data layouts (vector-of-vector Flux, per-element
 // gradient tables, per-element inverse mass matrices) and OpenMP pragmas.
 //
@@ -841,7 +842,11 @@ struct Solver {
         u.assign(4, std::vector<double>(numNodes, 0.0));
     }
 
-    // One iteration of the time loop body (sources, then RK4).
+    // Time integrator: 0 = "Runge-Kutta" (solver.cpp:171-292), 1 = "Euler1"
+    // (solver.cpp:61-161).
+    int method = 0;
+
+    // One iteration of the time loop body (sources, then the integrator).
     void step(double t) {
         for (size_t src = 0; src < config.sources.size(); ++src) {
             double amp = config.sources[src][5], freq = config.sources[src][6];
@@ -849,6 +854,12 @@ struct Solver {
             if (t < duration)
                 for (size_t n = 0; n < srcIndices[src].size(); ++n)
                     u[0][srcIndices[src][n]] = amp * std::sin(2 * M_PI * freq * t + phase);
+        }
+        if (method == 1) {
+            // first-order Euler in place: solver.cpp:152-153 (numStep with beta = 1)
+            mesh->updateFlux(u, Flux, config.v0, config.c0, config.rho0);
+            numStep(u, 1);
+            return;
         }
         k1 = k2 = k3 = k4 = u;
         mesh->updateFlux(k1, Flux, config.v0, config.c0, config.rho0);
@@ -959,6 +970,13 @@ void *oracle_create(const oracle_input *in, char *err, int errlen) {
 }
 
 void oracle_destroy(void *p) { delete (Handle *)p; }
+
+// 0 = classical RK4 ("Runge-Kutta"), 1 = forward Euler ("Euler1").
+int oracle_set_method(void *p, int method) {
+    if (method != 0 && method != 1) return -1;
+    ((Handle *)p)->solver.method = method;
+    return 0;
+}
 
 int oracle_num_dofs(void *p) { return ((Handle *)p)->solver.numNodes; }
 

@@ -61,6 +61,7 @@ def lib() -> C.CDLL:
         L.oracle_mesh.argtypes = [C.c_void_p, C.POINTER(MeshView)]
         L.oracle_face_maps.argtypes = [C.c_void_p, P_i, P_i]
         L.oracle_rhs.argtypes = [C.c_void_p, P_d, P_d]
+        L.oracle_set_method.argtypes = [C.c_void_p, C.c_int]
         _lib = L
     return _lib
 
@@ -131,6 +132,12 @@ class Oracle:
         u = np.empty(4 * self.ndof)
         lib().oracle_get_state(self._h, u.ctypes.data_as(P_d))
         return u.reshape(4, self.ndof)
+
+    def set_method(self, method: str) -> None:
+        """"Runge-Kutta" (classical RK4) or "Euler1" (forward Euler), the two
+        timeIntMethod values the reference's main dispatches on."""
+        code = {"Runge-Kutta": 0, "Euler1": 1}[method]
+        lib().oracle_set_method(self._h, code)
 
     def run(self, t: float, nsteps: int, dedup: bool = False) -> tuple[float, float]:
         tt, sec = C.c_double(t), C.c_double()

@@ -18,7 +18,7 @@ timeEnd={tend}
 timeStep={dt}
 timeRate={rate}
 elementType=Lagrange
-timeIntMethod=Runge-Kutta
+timeIntMethod={method}
 Reflecting = Reflecting
 Absorbing = Absorbing
 numThreads=1
@@ -59,7 +59,7 @@ def test_cli_matches_oracle(tmp_path):
     conf = tmp_path / "c.conf"
     save = tmp_path / "out.msh"
     conf.write_text(CONF.format(tend=(30 - 0.5) * dt, dt=repr(dt), rate=repr(10 * dt * 0.999), sdur=repr(12 * dt),
-                                save=save))
+                                save=save, method="Runge-Kutta"))
     exe = D.PKG / "lib" / "dgalerkin"
     r = subprocess.run([str(exe), str(msh), str(conf)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -85,3 +85,38 @@ def test_cli_argument_count():
     exe = D.PKG / "lib" / "dgalerkin"
     r = subprocess.run([str(exe), "only-one"], capture_output=True)
     assert r.returncode != 0
+
+
+def test_cli_forward_euler_and_unknown_method(tmp_path):
+    """timeIntMethod = Euler1 runs forward Euler (dgalerkin.cpp:55-56); a name
+    the reference does not know runs nothing and writes no views."""
+    mesh = D.Mesh.box_tri(4, 4, (-1, -1), (1, 1), order=3,
+                          side_names=("Reflecting", "Absorbing", "Reflecting", "Absorbing"))
+    msh = tmp_path / "box.msh"
+    mesh.write_msh(msh)
+    m2 = D.Mesh.read_msh(msh)
+    pre = D.Precomp(m2)
+    dt = 0.2 * D.cfl_dt(pre, 340.0)
+    exe = D.PKG / "lib" / "dgalerkin"
+    conf = tmp_path / "e.conf"
+    save = tmp_path / "euler.msh"
+    conf.write_text(CONF.format(tend=(20 - 0.5) * dt, dt=repr(dt), rate=repr(7 * dt * 0.999), sdur=repr(5 * dt),
+                                save=save, method="Euler1"))
+    r = subprocess.run([str(exe), str(msh), str(conf)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    step, t, ncomp, p = read_views(save)["Pressure"][2]
+    cfg = D.Config.parse(conf, m2)
+    orc = O.Oracle(m2.raw(), dt, 340.0, 1.225, bcs=cfg.bcs, sources=cfg.sources)
+    orc.set_method("Euler1")
+    orc.set_state(pre.initial_state(cfg.ics))
+    orc.run(0.0, step)
+    ref = orc.get_state()[0].reshape(pre.num_el, pre.np)
+    assert np.linalg.norm(p - ref) <= 1e-10 * np.linalg.norm(ref)
+
+    conf2 = tmp_path / "u.conf"
+    save2 = tmp_path / "none.msh"
+    conf2.write_text(CONF.format(tend=5 * dt, dt=repr(dt), rate=repr(dt), sdur="0", save=save2,
+                                 method="Leapfrog"))
+    r = subprocess.run([str(exe), str(msh), str(conf2)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert not save2.exists()

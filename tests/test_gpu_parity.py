@@ -33,10 +33,10 @@ def make_mesh(dim, order, bc):
 
 
 def run_pair(dim, order, bc, v0=(0.0, 0.0, 0.0), flux="reference", nsteps=12, precision="fp64",
-             sources=None, seed=0, use_graph=True):
+             sources=None, seed=0, use_graph=True, method="Runge-Kutta", dt_scale=1.0):
     mesh = make_mesh(dim, order, bc)
     pre = D.Precomp(mesh)
-    dt = D.cfl_dt(pre, C0, v0)
+    dt = dt_scale * D.cfl_dt(pre, C0, v0)
     rng = np.random.default_rng(seed)
     centre = pre.dof_coords().mean(axis=0)
     u0 = pre.initial_state([(0, *centre, 0.02, 1.0)])
@@ -50,9 +50,11 @@ def run_pair(dim, order, bc, v0=(0.0, 0.0, 0.0), flux="reference", nsteps=12, pr
             lst.append((pre.source_dofs(x, y, z, size), amp, f, ph, dur))
         sol.set_sources(lst)
         src_cfg = np.array([[0, x, y, z, size, amp, f, ph, dur] for (x, y, z, size, amp, f, ph, dur) in sources])
-    t = sol.rk4_steps(0.0, dt, nsteps)
+    steps = sol.euler_steps if method == "Euler1" else sol.rk4_steps
+    t = steps(0.0, dt, nsteps)
     got = sol.get_state()
     orc = O.Oracle(mesh.raw(), dt, C0, RHO0, v0=v0, bcs=mesh.bcs(), upwind=(flux == "upwind"), sources=src_cfg)
+    orc.set_method(method)
     orc.set_state(u0)
     t_ref, _ = orc.run(0.0, nsteps)
     ref = orc.get_state()
@@ -143,3 +145,55 @@ def test_mixed_form_long_run_against_fp64():
         out[prec] = s.get_state()
     for q in range(4):
         assert rel_l2(out["mixed"][q], out["fp64"][q]) <= 1e-5
+
+
+# Forward Euler ("Euler1", the reference's default integrator).  37 steps =
+# one captured 32-step graph chunk plus an odd remainder, which exercises the
+# state buffer swap; dt at a fifth of the RK4 CFL value keeps Euler bounded.
+@pytest.mark.parametrize("dim,order,bc", [(2, 3, "mixed"), (3, 2, "mixed"), (3, 3, "abs")])
+def test_fp64_euler_matches_oracle(dim, order, bc):
+    got, ref, dim = run_pair(dim, order, bc, nsteps=37, method="Euler1", dt_scale=0.2, v0=(20.0, 10.0, 0.0))
+    for q in range(dim + 1):
+        assert rel_l2(got[q], ref[q]) <= FP64_TOL, (q, rel_l2(got[q], ref[q]))
+
+
+def test_fp64_euler_with_sources_direct_launches():
+    srcs = [(0.2, 0.1, 0.0, 0.3, 2.0, 1500.0, 0.0, 1e-3)]
+    got, ref, dim = run_pair(2, 3, "refl", sources=srcs, nsteps=21, method="Euler1", dt_scale=0.2,
+                             use_graph=False)
+    for q in range(3):
+        assert rel_l2(got[q], ref[q]) <= FP64_TOL
+
+
+@pytest.mark.parametrize("precision,tol", [("fp32", FP32_TOL), ("mixed", MIXED_TOL)])
+@pytest.mark.parametrize("dim,order", [(2, 3), (3, 3)])
+def test_reduced_precision_euler(precision, tol, dim, order):
+    got, ref, dim = run_pair(dim, order, "mixed", precision=precision, flux="upwind", nsteps=37,
+                             method="Euler1", dt_scale=0.2)
+    for q in range(dim + 1):
+        assert rel_l2(got[q], ref[q]) <= tol, (q, rel_l2(got[q], ref[q]))
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+def test_euler_then_rk4_in_one_context(precision, tol):
+    """An odd number of Euler steps followed by RK4 steps on the same context
+    (the state must be back in its own buffers between calls)."""
+    mesh = make_mesh(2, 3, "mixed")
+    pre = D.Precomp(mesh)
+    dt = 0.2 * D.cfl_dt(pre, C0, (0.0, 0.0, 0.0))
+    u0 = pre.initial_state([(0, 0.1, -0.2, 0.0, 0.02, 1.0)])
+    sol = D.Solver(pre, C0, RHO0, (0.0, 0.0, 0.0), precision=precision, flux="upwind")
+    sol.set_state(u0)
+    t = sol.euler_steps(0.0, dt, 5)
+    t = sol.rk4_steps(t, dt, 33)
+    got = sol.get_state()
+    orc = O.Oracle(mesh.raw(), dt, C0, RHO0, bcs=mesh.bcs(), upwind=True)
+    orc.set_state(u0)
+    orc.set_method("Euler1")
+    tr, _ = orc.run(0.0, 5)
+    orc.set_method("Runge-Kutta")
+    tr, _ = orc.run(tr, 33)
+    ref = orc.get_state()
+    assert t == tr
+    for q in range(3):
+        assert rel_l2(got[q], ref[q]) <= tol

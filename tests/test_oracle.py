@@ -154,3 +154,22 @@ def test_nested_and_deduplicated_face_loops_agree():
     b.set_state(u0)
     b.run(0.0, 5, dedup=True)
     assert np.array_equal(a.get_state(), b.get_state())
+
+
+def test_forward_euler_step_is_state_plus_rhs():
+    """timeIntMethod = Euler1 (solver.cpp:152-153): one step from u gives
+    u + dt M^-1 (S - F) evaluated at u, which oracle_rhs returns."""
+    mesh = D.Mesh.box_tri(4, 3, (-1.0, -1.0), (1.0, 1.0), order=3,
+                          side_names=("Reflecting", "Absorbing", "Reflecting", "Absorbing"))
+    pre = D.Precomp(mesh)
+    dt = 0.2 * D.cfl_dt(pre, 340.0, (0.0, 0.0, 0.0))
+    u0 = pre.initial_state([(0, 0.1, 0.2, 0.0, 0.05, 1.0)])
+    u0[1:3] += 1e-3 * np.random.default_rng(3).standard_normal((2, pre.ndof))
+    orc = O.Oracle(mesh.raw(), dt, 340.0, 1.225, bcs=mesh.bcs())
+    rhs = orc.rhs(u0)
+    orc.set_state(u0)
+    orc.set_method("Euler1")
+    t, _ = orc.run(0.0, 1)
+    got = orc.get_state()
+    assert t == dt
+    assert np.allclose(got, u0 + rhs, rtol=0, atol=1e-13 * np.abs(u0).max())
