@@ -7,6 +7,10 @@
 #include "kernels.h"
 #include "mixed_kernel.cuh"
 
+#ifndef MIXED_WG
+#define MIXED_WG 4
+#endif
+
 namespace dgk {
 
 namespace {
@@ -53,19 +57,27 @@ void b_image(const double *ops, std::vector<uint8_t> &img, std::vector<int> &eb)
     }
 }
 
+// Warp groups per CTA: 4 (512 threads) where the per-thread state fits in
+// 128 registers, else 2.
+template <int DIM, int P>
+struct MixedWarpGroups {
+    static constexpr int value = MIXED_WG;
+};
+
 template <int DIM, int P>
 bool fill(MixedKernelSet *ks) {
     using MS = MixedShape<DIM, P>;
     if constexpr (!MS::FITS) {
         return false;
     } else {
-        ks->stage[0] = (const void *)&mixed_stage_kernel<DIM, P, 1>;
-        ks->stage[1] = (const void *)&mixed_stage_kernel<DIM, P, 2>;
-        ks->stage[2] = (const void *)&mixed_stage_kernel<DIM, P, 3>;
-        ks->stage[3] = (const void *)&mixed_stage_kernel<DIM, P, 4>;
-        ks->euler = (const void *)&mixed_stage_kernel<DIM, P, kStageEuler>;
+        constexpr int W = MixedWarpGroups<DIM, P>::value;
+        ks->stage[0] = (const void *)&mixed_stage_kernel<DIM, P, 1, W>;
+        ks->stage[1] = (const void *)&mixed_stage_kernel<DIM, P, 2, W>;
+        ks->stage[2] = (const void *)&mixed_stage_kernel<DIM, P, 3, W>;
+        ks->stage[3] = (const void *)&mixed_stage_kernel<DIM, P, 4, W>;
+        ks->euler = (const void *)&mixed_stage_kernel<DIM, P, kStageEuler, W>;
         ks->elems_per_tile = MS::ELEMS;
-        ks->threads = 256;
+        ks->threads = 128 * W;
         ks->smem = MS::SMEM_LAUNCH;
         ks->b_image = &b_image<DIM, P>;
         ks->npad = MS::NPAD;

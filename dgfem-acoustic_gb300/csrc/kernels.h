@@ -13,6 +13,7 @@ struct KernelSet {
     const void *stage[4] = {nullptr, nullptr, nullptr, nullptr};
     const void *euler = nullptr;  // forward-Euler step kernel
     const void *inject = nullptr;
+    const void *record = nullptr;
     int epb = 0;        // elements per block
     int threads = 0;    // threads per block (epb * np)
     size_t smem = 0;    // dynamic shared memory per block
@@ -54,6 +55,8 @@ struct MixedArgs {
     float *wout;           // next stage input (stage 4: u)
     float *wlo;            // forward-Euler step: low part of the new state
     long long fstride;
+    long long bstride;     // distance between batch members
+    int nbatch;            // batch members (sources) on the mesh
     const double *geo;     // [K][DIM*DIM]
     const float *fgeo;     // [K][NF][4]
     const int2 *conn;      // [K][NF]

@@ -22,6 +22,7 @@ bool fill_kernels(KernelSet *ks) {
     ks->stage[3] = (const void *)&stage_kernel<DIM, P, Real, 4, EPB>;
     ks->euler = (const void *)&stage_kernel<DIM, P, Real, kStageEuler, EPB>;
     ks->inject = (const void *)&inject_kernel<Real>;
+    ks->record = (const void *)&record_kernel<Real>;
     ks->epb = EPB;
     ks->threads = EPB * Shape<DIM, P>::NP;
     ks->smem = StageSmem<DIM, P, Real, EPB>::total;

@@ -17,15 +17,17 @@
 // epilogue adds the three in double-FP32, scales by 2^(ea+eb-16) dt and
 // applies the RK4 stage update with the state u kept as an FP32 pair.
 //
-// Roles (256 threads, one CTA per SM, persistent over tiles): all threads
-// stage the tile's state, then build the A rows in shared memory (one task per
-// element node for the volume fluxes, one per face slot for the face values).
-// Row r is then sliced by lane r%32 of warps r/32 and r/32+4 (warp w may only
-// touch tensor-memory lanes 32(w%4)..32(w%4)+31), each taking half of the
-// K-steps, and stored with tcgen05.st.  One thread issues the 13 x KSTEPS
-// tcgen05.mma and commits them to an mbarrier; both warp halves then read the
-// accumulators of their row with tcgen05.ld, split by output node, for the
-// epilogue.  Every wait is bounded; on timeout the kernel records an error,
+// Roles (128*NWG threads, one CTA per SM, persistent over tiles): cp.async copies
+// bring a tile's state, geometry, connectivity and neighbour traces into
+// shared memory one tile ahead; all threads build the A rows in shared memory
+// (one task per element node for the volume fluxes, one per face slot for the
+// face values).
+// Row r is then sliced by lane r%32 of warps r/32 + 4g of every warp group g
+// (warp w may only touch tensor-memory lanes 32(w%4)..32(w%4)+31), each
+// group taking a share of the K-steps, and stored with tcgen05.st.  One
+// thread issues the 13 x KSTEPS tcgen05.mma and commits them to an mbarrier;
+// the warp groups then read the accumulators of their row with tcgen05.ld,
+// split by output node, for the epilogue.  Every wait is bounded; on timeout the kernel records an error,
 // waits once more for the MMAs in flight, frees tensor memory and stops.
 #pragma once
 #include <cuda_runtime.h>
@@ -56,19 +58,22 @@ struct MixedShape {
     static constexpr int BBYTES = 4 * KSTEPS * BTILE;
     static constexpr int QS = NP + 1;               // padded element stride in the state tile
     static constexpr int KSTR = KPAD + 1;           // padded row stride of the staged A rows (odd)
-    static constexpr int KS_HALF = (KSTEPS + 1) / 2;  // K-steps sliced by warps 0-3 (rest by 4-7)
-    static constexpr int NHALF = (NP + 1) / 2;      // output nodes per epilogue half
-    static constexpr int NCH = (NHALF + 7) / 8;     // 8-column tensor-memory loads per accumulator
-    static_assert(ACC + 2 * NPAD + NHALF + 8 * NCH <= TMEM_COLS, "epilogue loads stay inside the allocation");
+    static constexpr int MAX_WG = 4;                // warp groups per CTA (4 warps each), at most
     // shared memory layout (bytes)
-    static constexpr int OFF_B = 0;
-    static constexpr int OFF_Q = OFF_B + BBYTES;
-    static constexpr int OFF_A = OFF_Q + NQ * ELEMS * QS * 4;
-    static constexpr int OFF_MAX = OFF_A + 128 * KSTR * 4;
-    static constexpr int OFF_TAB = OFF_MAX + 2 * 128 * 4;
-    static constexpr int OFF_EB = (OFF_TAB + S::NTAB + 15) / 16 * 16;
+    static constexpr int r16(int x) { return (x + 15) / 16 * 16; }
+    static constexpr int OFF_B = 0;                                   // sliced operator image
+    static constexpr int OFF_Q = OFF_B + BBYTES;                      // state tile [f][le][QS]
+    static constexpr int OFF_A = r16(OFF_Q + NQ * ELEMS * QS * 4);    // FP32 A rows [128][KSTR]
+    static constexpr int OFF_NBR = r16(OFF_A + 128 * KSTR * 4);       // neighbour traces [task][4]
+    static constexpr int OFF_GEO = OFF_NBR + ELEMS * NSLOT * 16;      // [le][DIM*DIM] doubles
+    static constexpr int OFF_CONN = r16(OFF_GEO + ELEMS * DIM * DIM * 8);  // [le][NF] int2
+    static constexpr int OFF_FGEO = r16(OFF_CONN + ELEMS * NF * 8);   // [le][NF] float4
+    static constexpr int OFF_MAX = OFF_FGEO + ELEMS * NF * 16;
+    static constexpr int OFF_TAB = OFF_MAX + MAX_WG * 128 * 4;
+    static constexpr int OFF_EB = r16(OFF_TAB + S::NTAB);
     static constexpr int OFF_BAR = OFF_EB + NPAD * 4;
     static constexpr int SMEM = OFF_BAR + 16;
+    static_assert(SMEM <= 227 * 1024, "tile does not fit in shared memory");
     // at least half of the SM's shared memory, so one CTA (the tensor-memory
     // owner) runs per SM
     static constexpr int SMEM_LAUNCH = SMEM < 118 * 1024 ? 118 * 1024 : SMEM;
@@ -119,16 +124,81 @@ __device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
-template <int DIM, int P, int STAGE>
-__global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) {
+// Issues the cp.async copies of a tile's element data: state, inverse
+// Jacobians, connectivity words and face geometry (zero-filled past K).
+template <int DIM, int P, int NT>
+__device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned char *smem, long long ebase,
+                                                  long long moff, int tid) {
+    using MS = MixedShape<DIM, P>;
+    constexpr int NP = MS::NP, NF = MS::NF, NQ = MS::NQ, ELEMS = MS::ELEMS, QS = MS::QS;
+    float *sQ = reinterpret_cast<float *>(smem + MS::OFF_Q);
+    double *sGeo = reinterpret_cast<double *>(smem + MS::OFF_GEO);
+    int2 *sConn = reinterpret_cast<int2 *>(smem + MS::OFF_CONN);
+    float4 *sFgeo = reinterpret_cast<float4 *>(smem + MS::OFF_FGEO);
+    for (int idx = tid; idx < NQ * ELEMS * NP; idx += NT) {
+        const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
+        const int le = rem / NP, j = rem - le * NP;
+        const bool ok = ebase + le < a.K;
+        const float *src = ok ? &a.win[moff + f * a.fstride + ebase * NP + rem] : a.win;
+        dgtc::cp_async4(&sQ[(f * ELEMS + le) * QS + j], src, ok ? 4u : 0u);
+    }
+    for (int idx = tid; idx < ELEMS * DIM * DIM; idx += NT) {
+        const bool ok = ebase + idx / (DIM * DIM) < a.K;
+        dgtc::cp_async8(&sGeo[idx], ok ? &a.geo[ebase * DIM * DIM + idx] : a.geo, ok ? 8u : 0u);
+    }
+    for (int idx = tid; idx < ELEMS * NF; idx += NT) {
+        const bool ok = ebase + idx / NF < a.K;
+        dgtc::cp_async8(&sConn[idx], ok ? &a.conn[ebase * NF + idx] : a.conn, ok ? 8u : 0u);
+        dgtc::cp_async16(&sFgeo[idx], ok ? &a.fgeo[(ebase * NF + idx) * 4] : a.fgeo, ok ? 16u : 0u);
+    }
+}
+
+// Issues the cp.async gathers of the neighbour traces of a tile's interior
+// face slots (reads the tile's connectivity words from shared memory); the
+// calling threads take tasks first, first + stride, ...
+template <int DIM, int P>
+__device__ __forceinline__ void issue_neighbour_copies(const MixedArgs &a, unsigned char *smem, long long ebase,
+                                                       long long moff, int first, int stride) {
+    using MS = MixedShape<DIM, P>;
+    constexpr int NP = MS::NP, NF = MS::NF, NFP = MS::NFP, NQ = MS::NQ, NSLOT = MS::NSLOT, ELEMS = MS::ELEMS;
+    float *sNbr = reinterpret_cast<float *>(smem + MS::OFF_NBR);
+    const int2 *sConn = reinterpret_cast<const int2 *>(smem + MS::OFF_CONN);
+    const uint8_t *sFmask = smem + MS::OFF_TAB;
+    const uint8_t *sPerm = sFmask + NF * NFP;
+    for (int task = first; task < ELEMS * NSLOT; task += stride) {
+        const int le = task / NSLOT, s = task - le * NSLOT;
+        const int lf = s / NFP, k = s - lf * NFP;
+        if (ebase + le >= a.K) continue;
+        const int2 cn = sConn[le * NF + lf];
+        if (((cn.y >> 5) & 3) != kKindInterior) continue;
+        const int nlf = cn.y & 3, pm = (cn.y >> 2) & 7;
+        const long long nb = (long long)cn.x * NP + sFmask[nlf * NFP + sPerm[pm * NFP + k]];
+#pragma unroll
+        for (int f = 0; f < NQ; ++f) dgtc::cp_async4(&sNbr[task * 4 + f], &a.win[moff + f * a.fstride + nb], 4u);
+    }
+}
+
+template <int DIM, int P, int STAGE, int NWG>
+__global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedArgs a) {
     using MS = MixedShape<DIM, P>;
     constexpr int NP = MS::NP, NF = MS::NF, NFP = MS::NFP, NQ = MS::NQ, NSLOT = MS::NSLOT;
     constexpr int ELEMS = MS::ELEMS, QS = MS::QS, KTOT = MS::KTOT, KSTEPS = MS::KSTEPS, KSTR = MS::KSTR;
-    constexpr int NPAD = MS::NPAD, ACOLS = MS::ACOLS, NHALF = MS::NHALF, KS_HALF = MS::KS_HALF;
+    constexpr int NPAD = MS::NPAD, ACOLS = MS::ACOLS;
+    constexpr int NT = 128 * NWG;                       // threads
+    constexpr int KSP = (KSTEPS + NWG - 1) / NWG;       // K-steps sliced per warp group
+    constexpr int NPP = (NP + NWG - 1) / NWG;           // output nodes per warp group in the epilogue
+    constexpr int NCH = (NPP + 7) / 8;                  // 8-column tensor-memory loads per accumulator
     static_assert(MS::FITS, "tile does not fit in tensor memory");
+    static_assert(NWG >= 1 && NWG <= MS::MAX_WG, "warp groups");
+    static_assert(MS::ACC + 2 * NPAD + (NWG - 1) * NPP + 8 * NCH <= MS::TMEM_COLS,
+                  "epilogue loads stay inside the allocation");
     extern __shared__ __align__(1024) unsigned char smem[];
-    float *sQ = reinterpret_cast<float *>(smem + MS::OFF_Q);
+    const float *sQ = reinterpret_cast<const float *>(smem + MS::OFF_Q);
     float *sA = reinterpret_cast<float *>(smem + MS::OFF_A);
+    const float4 *sNbr = reinterpret_cast<const float4 *>(smem + MS::OFF_NBR);
+    const double *sGeo = reinterpret_cast<const double *>(smem + MS::OFF_GEO);
+    const int2 *sConn = reinterpret_cast<const int2 *>(smem + MS::OFF_CONN);
+    const float4 *sFgeo = reinterpret_cast<const float4 *>(smem + MS::OFF_FGEO);
     float *sMax = reinterpret_cast<float *>(smem + MS::OFF_MAX);
     uint8_t *sTab = smem + MS::OFF_TAB;
     int *sEb = reinterpret_cast<int *>(smem + MS::OFF_EB);
@@ -136,7 +206,6 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
     uint32_t *sTmem = reinterpret_cast<uint32_t *>(smem + MS::OFF_BAR + 8);
     int *sFail = reinterpret_cast<int *>(smem + MS::OFF_BAR + 12);
     const uint8_t *sFmask = sTab;
-    const uint8_t *sPerm = sTab + NF * NFP;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0) {
@@ -151,9 +220,9 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
     {
         const uint4 *src = reinterpret_cast<const uint4 *>(a.bimg);
         uint4 *dst = reinterpret_cast<uint4 *>(smem + MS::OFF_B);
-        for (int k = tid; k < MS::BBYTES / 16; k += 256) dst[k] = src[k];
-        for (int k = tid; k < Shape<DIM, P>::NTAB; k += 256) sTab[k] = a.tabs[k];
-        for (int k = tid; k < NPAD; k += 256) sEb[k] = a.beb[k];
+        for (int k = tid; k < MS::BBYTES / 16; k += NT) dst[k] = src[k];
+        for (int k = tid; k < Shape<DIM, P>::NTAB; k += NT) sTab[k] = a.tabs[k];
+        for (int k = tid; k < NPAD; k += NT) sEb[k] = a.beb[k];
     }
     dgtc::fence_proxy_async_smem();
     dgtc::fence_before_sync();
@@ -162,50 +231,49 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
     const uint32_t tbase = *sTmem;
     const uint32_t idesc = dgtc::idesc_bf16_f32(128, NPAD);
     const uint32_t sB = dgtc::smem_u32(smem + MS::OFF_B);
-    // row of this thread in phases 3 and 5, and which half of the work
+    // row of this thread in phases 3 and 5, and which part of the row's work
+    // (K-steps when slicing, output nodes in the epilogue) its warp group takes
     const int r = (warp & 3) * 32 + lane;
-    const int half = warp >> 2;
+    const int part = warp >> 2;
     const int rf = r / ELEMS, rle = r - rf * ELEMS;
     bool alive = true;
     uint32_t phase = 0;
 
-    const int ntiles = (a.K + ELEMS - 1) / ELEMS;
-    for (int tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x) {
-        const long long ebase = (long long)tile * ELEMS;
-        // 1. stage the tile's input state (every load issued before the stores)
-        {
-            constexpr int TOT1 = NQ * ELEMS * NP, N1 = (TOT1 + 255) / 256;
-            float v[N1];
-#pragma unroll
-            for (int t = 0; t < N1; ++t) {
-                const int idx = tid + 256 * t;
-                v[t] = 0.0f;
-                if (idx < TOT1) {
-                    const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
-                    if (ebase + rem / NP < a.K) v[t] = __ldg(&a.win[f * a.fstride + ebase * NP + rem]);
-                }
-            }
-#pragma unroll
-            for (int t = 0; t < N1; ++t) {
-                const int idx = tid + 256 * t;
-                if (idx < TOT1) {
-                    const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
-                    const int le = rem / NP, j = rem - le * NP;
-                    sQ[(f * ELEMS + le) * QS + j] = v[t];
-                }
-            }
-        }
+    // Software pipeline over the CTA's tiles: the element data of tile t+1
+    // are copied while tile t is sliced, and its neighbour traces while tile
+    // t's contraction and epilogue run.  Tile T covers element block T / nbatch
+    // of batch member T % nbatch (members of one block are adjacent, so the
+    // block's geometry is reused from L2).
+    const long long ntiles = (long long)((a.K + ELEMS - 1) / ELEMS) * a.nbatch;
+    auto tile_base = [&](long long T, long long &eb, long long &mo) {
+        const long long et = T / a.nbatch;
+        eb = et * ELEMS;
+        mo = (T - et * a.nbatch) * a.bstride;
+    };
+    if ((long long)blockIdx.x < ntiles) {
+        long long eb, mo;
+        tile_base(blockIdx.x, eb, mo);
+        issue_tile_copies<DIM, P, NT>(a, smem, eb, mo, tid);
+        dgtc::cp_async_wait_all();
+        __syncthreads();
+        issue_neighbour_copies<DIM, P>(a, smem, eb, mo, tid, NT);
+    }
+    for (long long tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x) {
+        long long ebase, moff;
+        tile_base(tile, ebase, moff);
+        const long long next = tile + gridDim.x;
+        long long nebase = 0, nmoff = 0;
+        if (next < ntiles) tile_base(next, nebase, nmoff);
+        dgtc::cp_async_wait_all();
         __syncthreads();
         // 2a. contravariant fluxes, one task per element node
-        for (int task = tid; task < ELEMS * NP; task += 256) {
+        for (int task = tid; task < ELEMS * NP; task += NT) {
             const int le = task / NP, j = task - le * NP;
-            const long long e = ebase + le;
             float Bg[DIM][DIM];
-            const bool ok = e < a.K;
 #pragma unroll
             for (int x = 0; x < DIM; ++x)
 #pragma unroll
-                for (int u = 0; u < DIM; ++u) Bg[x][u] = ok ? (float)__ldg(&a.geo[e * DIM * DIM + x * DIM + u]) : 0.0f;
+                for (int u = 0; u < DIM; ++u) Bg[x][u] = (float)sGeo[le * DIM * DIM + x * DIM + u];
             float q[NQ];
 #pragma unroll
             for (int f = 0; f < NQ; ++f) q[f] = sQ[(f * ELEMS + le) * QS + j];
@@ -224,123 +292,86 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
                     sA[((1 + d) * ELEMS + le) * KSTR + u * NP + j] = fmaf(au, q[1 + d], pr * Bg[d][u]);
             }
         }
-        // 2b. face values, negated and scaled: -(detJf/detJe) Fn; the tasks of a
-        //     thread go in groups whose connectivity and neighbour loads are all
-        //     issued before the flux arithmetic
-        {
-            constexpr int TOT2 = ELEMS * NSLOT, NT2 = (TOT2 + 255) / 256, G2 = NT2 < 4 ? NT2 : 4;
-#pragma unroll 1
-            for (int t0 = 0; t0 < NT2; t0 += G2) {
-                int2 cn[G2];
-                float4 g4[G2];
-                float o[G2][NQ];
-                bool val[G2];
+        // 2b. face values, negated and scaled: -(detJf/detJe) Fn
+        for (int task = tid; task < ELEMS * NSLOT; task += NT) {
+            const int le = task / NSLOT, s = task - le * NSLOT;
+            const int lf = s / NFP, k = s - lf * NFP;
+            float Fn[NQ];
 #pragma unroll
-                for (int g = 0; g < G2; ++g) {
-                    const int task = tid + 256 * (t0 + g);
-                    const int le = task / NSLOT, lf = (task - le * NSLOT) / NFP;
-                    val[g] = (t0 + g < NT2) && task < TOT2 && ebase + le < a.K;
-                    cn[g] = make_int2(0, kKindAbsorbing << 5);
-                    g4[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    if (val[g]) {
-                        const long long e = ebase + le;
-                        cn[g] = __ldg(&a.conn[e * NF + lf]);
-                        g4[g] = __ldg(reinterpret_cast<const float4 *>(&a.fgeo[(e * NF + lf) * 4]));
+            for (int f = 0; f < NQ; ++f) Fn[f] = 0.0f;
+            float scale = 0.0f;
+            if (ebase + le < a.K) {
+                const int vi = sFmask[lf * NFP + k];
+                float own[NQ];
+#pragma unroll
+                for (int f = 0; f < NQ; ++f) own[f] = sQ[(f * ELEMS + le) * QS + vi];
+                const int2 cn = sConn[le * NF + lf];
+                const float4 g4 = sFgeo[le * NF + lf];
+                const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
+                float n[DIM];
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) n[x] = gg[x];
+                scale = gg[DIM];
+                float vn0 = 0.0f;
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) vn0 = fmaf(a.v0[x], n[x], vn0);
+                const int kind = (cn.y >> 5) & 3;
+                if (kind == kKindInterior) {
+                    const float4 o4 = sNbr[task];
+                    const float o[4] = {o4.x, o4.y, o4.z, o4.w};
+                    const float tau = (cn.y & 128) ? -1.0f : 1.0f;
+                    const float sp = own[0] + o[0];
+                    float svn = 0.0f;
+#pragma unroll
+                    for (int x = 0; x < DIM; ++x) svn = fmaf(own[1 + x] + o[1 + x], n[x], svn);
+                    const float hj = a.half_c0 * tau;
+                    Fn[0] = fmaf(hj, own[0] - o[0], 0.5f * fmaf(vn0, sp, a.rc2 * svn));
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d)
+                        Fn[1 + d] = fmaf(hj, own[1 + d] - o[1 + d],
+                                         0.5f * fmaf(vn0, own[1 + d] + o[1 + d], a.inv_rho * sp * n[d]));
+                } else if (kind == kKindReflecting) {
+                    float vn = 0.0f;
+#pragma unroll
+                    for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
+                    float vw[DIM], vwn = 0.0f;
+#pragma unroll
+                    for (int x = 0; x < DIM; ++x) {
+                        vw[x] = own[1 + x] - vn * n[x];
+                        vwn = fmaf(vw[x], n[x], vwn);
                     }
-                }
+                    Fn[0] = fmaf(vn0, own[0], a.rc2 * vwn);
 #pragma unroll
-                for (int g = 0; g < G2; ++g) {
+                    for (int d = 0; d < DIM; ++d) Fn[1 + d] = fmaf(vn0, vw[d], a.inv_rho * own[0] * n[d]);
+                } else {
+                    float vn = 0.0f;
 #pragma unroll
-                    for (int f = 0; f < NQ; ++f) o[g][f] = 0.0f;
-                    if (val[g] && ((cn[g].y >> 5) & 3) == kKindInterior) {
-                        const int task = tid + 256 * (t0 + g);
-                        const int s = task - (task / NSLOT) * NSLOT;
-                        const int k = s - (s / NFP) * NFP;
-                        const int nlf = cn[g].y & 3, pm = (cn[g].y >> 2) & 7;
-                        const int nvi = sFmask[nlf * NFP + sPerm[pm * NFP + k]];
-                        const long long nb = (long long)cn[g].x * NP + nvi;
+                    for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
+                    const float q0 = 0.25f * a.c0;
+                    Fn[0] = fmaf(q0, own[0], 0.25f * a.c0 * a.c0 * a.rho * vn);
 #pragma unroll
-                        for (int f = 0; f < NQ; ++f) o[g][f] = __ldg(&a.win[f * a.fstride + nb]);
-                    }
-                }
-#pragma unroll
-                for (int g = 0; g < G2; ++g) {
-                    const int task = tid + 256 * (t0 + g);
-                    if (t0 + g >= NT2 || task >= TOT2) continue;
-                    const int le = task / NSLOT, s = task - le * NSLOT;
-                    const int lf = s / NFP, k = s - lf * NFP;
-                    float Fn[NQ];
-#pragma unroll
-                    for (int f = 0; f < NQ; ++f) Fn[f] = 0.0f;
-                    float scale = 0.0f;
-                    if (val[g]) {
-                        const int vi = sFmask[lf * NFP + k];
-                        float own[NQ];
-#pragma unroll
-                        for (int f = 0; f < NQ; ++f) own[f] = sQ[(f * ELEMS + le) * QS + vi];
-                        const float gg[4] = {g4[g].x, g4[g].y, g4[g].z, g4[g].w};
-                        float n[DIM];
-#pragma unroll
-                        for (int x = 0; x < DIM; ++x) n[x] = gg[x];
-                        scale = gg[DIM];
-                        float vn0 = 0.0f;
-#pragma unroll
-                        for (int x = 0; x < DIM; ++x) vn0 = fmaf(a.v0[x], n[x], vn0);
-                        const int kind = (cn[g].y >> 5) & 3;
-                        if (kind == kKindInterior) {
-                            const float tau = (cn[g].y & 128) ? -1.0f : 1.0f;
-                            const float sp = own[0] + o[g][0];
-                            float svn = 0.0f;
-#pragma unroll
-                            for (int x = 0; x < DIM; ++x) svn = fmaf(own[1 + x] + o[g][1 + x], n[x], svn);
-                            const float hj = a.half_c0 * tau;
-                            Fn[0] = fmaf(hj, own[0] - o[g][0], 0.5f * fmaf(vn0, sp, a.rc2 * svn));
-#pragma unroll
-                            for (int d = 0; d < DIM; ++d)
-                                Fn[1 + d] = fmaf(hj, own[1 + d] - o[g][1 + d],
-                                                 0.5f * fmaf(vn0, own[1 + d] + o[g][1 + d], a.inv_rho * sp * n[d]));
-                        } else if (kind == kKindReflecting) {
-                            float vn = 0.0f;
-#pragma unroll
-                            for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
-                            float vw[DIM], vwn = 0.0f;
-#pragma unroll
-                            for (int x = 0; x < DIM; ++x) {
-                                vw[x] = own[1 + x] - vn * n[x];
-                                vwn = fmaf(vw[x], n[x], vwn);
-                            }
-                            Fn[0] = fmaf(vn0, own[0], a.rc2 * vwn);
-#pragma unroll
-                            for (int d = 0; d < DIM; ++d) Fn[1 + d] = fmaf(vn0, vw[d], a.inv_rho * own[0] * n[d]);
-                        } else {
-                            float vn = 0.0f;
-#pragma unroll
-                            for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
-                            const float q0 = 0.25f * a.c0;
-                            Fn[0] = fmaf(q0, own[0], 0.25f * a.c0 * a.c0 * a.rho * vn);
-#pragma unroll
-                            for (int d = 0; d < DIM; ++d)
-                                Fn[1 + d] = fmaf(0.25f * n[d] * a.inv_rho, own[0], q0 * n[d] * vn);
-                        }
-                    }
-#pragma unroll
-                    for (int f = 0; f < NQ; ++f) sA[(f * ELEMS + le) * KSTR + DIM * NP + s] = -scale * Fn[f];
+                    for (int d = 0; d < DIM; ++d) Fn[1 + d] = fmaf(0.25f * n[d] * a.inv_rho, own[0], q0 * n[d] * vn);
                 }
             }
+#pragma unroll
+            for (int f = 0; f < NQ; ++f) sA[(f * ELEMS + le) * KSTR + DIM * NP + s] = -scale * Fn[f];
         }
         __syncthreads();
+        // the tile's element data are consumed: start copying the next tile's
+        if (next < ntiles) issue_tile_copies<DIM, P, NT>(a, smem, nebase, nmoff, tid);
 
-        // 3. slices of the A rows into tensor memory; warps 0-3 take the first
-        //    K-steps of rows 0..127, warps 4-7 the rest of the same rows
+        // 3. slices of the A rows into tensor memory; warp group g takes
+        //    K-steps [g*KSP, (g+1)*KSP) of rows 0..127
         const bool row_ok = (rf < NQ) && (ebase + rle < a.K);
-        const int ks0 = half ? KS_HALF : 0, ks1 = half ? KSTEPS : KS_HALF;
+        const int ks0 = part * KSP < KSTEPS ? part * KSP : KSTEPS;
+        const int ks1 = ks0 + KSP < KSTEPS ? ks0 + KSP : KSTEPS;
         // operands of this thread's RK update, loaded now so that their latency
         // overlaps the slicing and the contraction
-        const int i0 = half * NHALF;
-        const long long rbase = rf * a.fstride + (ebase + rle) * NP;
-        float pu[NHALF], pl[NHALF], pa[NHALF];
+        const int i0 = part * NPP;
+        const long long rbase = moff + rf * a.fstride + (ebase + rle) * NP;
+        float pu[NPP], pl[NPP], pa[NPP];
 #pragma unroll
-        for (int t = 0; t < NHALF; ++t) {
+        for (int t = 0; t < NPP; ++t) {
             pu[t] = pl[t] = pa[t] = 0.0f;
             if (row_ok && i0 + t < NP) {
                 pu[t] = a.u[rbase + i0 + t];
@@ -353,10 +384,13 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
             float m = 0.0f;
             if (row_ok)
                 for (int k = ks0 * 16; k < ks1 * 16 && k < KTOT; ++k) m = fmaxf(m, fabsf(arow[k]));
-            sMax[half * 128 + r] = m;
+            sMax[part * 128 + r] = m;
         }
         __syncthreads();
-        const int ea = row_exponent(fmaxf(sMax[r], sMax[128 + r]));
+        float rmax = sMax[r];
+#pragma unroll
+        for (int g = 1; g < NWG; ++g) rmax = fmaxf(rmax, sMax[g * 128 + r]);
+        const int ea = row_exponent(rmax);
         // rows below 2^-110 are treated as zero (their contribution is far
         // below the FP32 resolution of any non-negligible row)
         const bool live = row_ok && ea > -110;
@@ -382,9 +416,12 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
         }
         dgtc::tmem_st_wait();
         dgtc::fence_before_sync();
+        // the next tile's element data have landed once every thread's copies are done
+        dgtc::cp_async_wait_all();
         __syncthreads();
 
-        // 4. tensor-core contraction: 13 slice pairs x KSTEPS
+        // 4. tensor-core contraction: 13 slice pairs x KSTEPS, issued by thread
+        //    0 while warps 1.. start gathering the next tile's neighbour traces
         if (tid == 0) {
             dgtc::fence_after_sync();
             unsigned started = 0;  // bit per accumulator slot
@@ -403,9 +440,10 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
             dgtc::mma_commit(bar);
         }
         __syncwarp();
+        if (warp > 0 && next < ntiles) issue_neighbour_copies<DIM, P>(a, smem, nebase, nmoff, tid - 32, NT - 32);
 
         // 5. epilogue: accumulators -> stage increment, RK4 stage update;
-        //    warps 0-3 take output nodes [0, NHALF), warps 4-7 the rest
+        //    warp group g takes output nodes [g*NPP, (g+1)*NPP)
         if (!dgtc::mbar_wait_bounded(bar, phase, 1u << 30)) *sFail = 1;
         phase ^= 1u;
         __syncthreads();
@@ -413,7 +451,6 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
             alive = false;
         } else {
             dgtc::fence_after_sync();
-            constexpr int NCH = MS::NCH;
             uint32_t v0[8 * NCH], v1[8 * NCH], v2[8 * NCH];
 #pragma unroll
             for (int c = 0; c < NCH; ++c) {
@@ -425,7 +462,7 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
             if (row_ok) {
                 const float sdt = live ? a.dt * exp2i(ea - 16) : 0.0f;
 #pragma unroll
-                for (int t = 0; t < NHALF; ++t) {
+                for (int t = 0; t < NPP; ++t) {
                     const int i = i0 + t;
                     if (i >= NP) break;
                     float hi, lo;
@@ -465,6 +502,8 @@ __global__ void __launch_bounds__(256, 1) mixed_stage_kernel(const MixedArgs a) 
         dgtc::fence_before_sync();
         __syncthreads();
     }
+    // no copy may still be writing shared memory when the CTA exits
+    dgtc::cp_async_wait_all();
     if (!alive && tid == 0) {
         // the MMAs of the failed tile may still be in flight: wait once more
         // (bounded) before releasing tensor memory

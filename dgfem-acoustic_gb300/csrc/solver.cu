@@ -102,6 +102,8 @@ __global__ void monitor_kernel(const Real *u, long long fstride, int K, int np, 
 struct dg_ctx {
     int dim = 0, order = 0, np = 0, nf = 0, nfp = 0, nq = 0, K = 0;
     long long ndof = 0;  // K * np
+    int nbatch = 1;       // independent states (sources) on the mesh
+    long long bstride = 0;  // values per batch member: nq * ndof
     int prec = 0, flux_sign = 0, device = 0, use_graph = 1;
     size_t rsize = 8;
     double c0 = 1, rho0 = 1, v0[3] = {0, 0, 0};
@@ -117,11 +119,18 @@ struct dg_ctx {
     double *d_stage64 = nullptr;  // FP64 staging (FP32 contexts)
     double *d_mass = nullptr, *d_detj = nullptr, *d_mon = nullptr;
     unsigned long long *d_bad = nullptr;
-    // sources
+    // sources: node j is the field-0 value at d_src_at[j] (member folded in)
     int src_nodes = 0;
-    int *d_src_dof = nullptr, *d_src_off = nullptr, *d_src_list = nullptr;
-    double *d_src_params = nullptr;
+    long long *d_src_at = nullptr;
+    int *d_src_off = nullptr, *d_src_list = nullptr;
+    double *d_src_w = nullptr, *d_src_params = nullptr;
     std::vector<double> src_duration;
+    // receivers
+    int rec_n = 0, rec_max = 0;
+    long long rec_done = 0;  // steps recorded so far
+    int *d_rec_dof = nullptr;
+    double *d_trace = nullptr;
+    long long *d_step0 = nullptr;
     dgk::KernelSet ks;
     int grid = 0;
     // mixed form
@@ -156,9 +165,10 @@ void free_ctx(dg_ctx *c) {
     if (c->device >= 0) cudaSetDevice(c->device);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     for (auto ev : c->events) cudaEventDestroy(ev);
-    void *ptrs[] = {c->d_state, c->d_geo, c->d_fgeo, c->d_conn, c->d_ops, c->d_tabs, c->d_t0, c->d_stage64,
-                    c->d_mass, c->d_detj, c->d_mon, c->d_bad, c->d_src_dof, c->d_src_off, c->d_src_list,
-                    c->d_src_params, c->d_ulo, c->d_bimg, c->d_beb, c->d_err};
+    void *ptrs[] = {c->d_state, c->d_geo,     c->d_fgeo,    c->d_conn,    c->d_ops,     c->d_tabs,
+                    c->d_t0,    c->d_stage64, c->d_mass,    c->d_detj,    c->d_mon,     c->d_bad,
+                    c->d_src_at, c->d_src_off, c->d_src_list, c->d_src_w, c->d_src_params, c->d_ulo,
+                    c->d_bimg,  c->d_beb,     c->d_err,     c->d_rec_dof, c->d_trace,   c->d_step0};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -168,7 +178,7 @@ void free_ctx(dg_ctx *c) {
 template <typename Real>
 void fill_args(dg_ctx *c, dgk::StageArgs<Real> &a, int stage, double dt) {
     a.fstride = c->ndof;
-    a.bstride = 0;
+    a.bstride = c->bstride;
     a.geo = c->d_geo;
     a.fgeo = reinterpret_cast<const Real *>(c->d_fgeo);
     a.conn = c->d_conn;
@@ -206,6 +216,8 @@ cudaError_t launch_stage(dg_ctx *c, int stage, double dt) {
         a.wout = s.wout;
         a.wlo = stage == kEulerStage ? static_cast<float *>(c->d_acc) : nullptr;
         a.fstride = s.fstride;
+        a.bstride = c->bstride;
+        a.nbatch = c->nbatch;
         a.geo = s.geo;
         a.fgeo = s.fgeo;
         a.conn = s.conn;
@@ -225,7 +237,7 @@ cudaError_t launch_stage(dg_ctx *c, int stage, double dt) {
         const void *fn = stage == kEulerStage ? c->mks.euler : c->mks.stage[stage];
         return cudaLaunchKernel(fn, dim3(c->grid), dim3(c->mks.threads), args, c->mks.smem, c->stream);
     }
-    dim3 grid(c->grid, 1, 1), block(c->ks.threads, 1, 1);
+    dim3 grid(c->grid, c->nbatch, 1), block(c->ks.threads, 1, 1);
     const void *fn = stage == kEulerStage ? c->ks.euler : c->ks.stage[stage];
     if (c->prec == DG_PREC_FP64) {
         dgk::StageArgs<double> a;
@@ -243,13 +255,23 @@ cudaError_t launch_stage(dg_ctx *c, int stage, double dt) {
 cudaError_t launch_inject(dg_ctx *c, int kstep, double dt) {
     if (!c->src_nodes) return cudaSuccess;
     dim3 grid((c->src_nodes + 127) / 128, 1, 1), block(128, 1, 1);
-    long long bstride = 0;
-    void *p = c->d_u;  // field 0 of u
+    void *p = c->d_u;  // field 0 of member 0 of u
     int nn = c->src_nodes;
     void *plo = c->d_ulo;  // null unless the state is kept as a pair
-    void *args[] = {&p, &bstride, &c->d_src_dof, &c->d_src_off, &c->d_src_list, &c->d_src_params, &c->d_t0,
+    void *args[] = {&p, &c->d_src_at, &c->d_src_off, &c->d_src_list, &c->d_src_w, &c->d_src_params, &c->d_t0,
                     &kstep, &dt, &nn, &plo};
     return cudaLaunchKernel(c->ks.inject, grid, block, args, 0, c->stream);
+}
+
+cudaError_t launch_record(dg_ctx *c, int kstep) {
+    if (!c->rec_n) return cudaSuccess;
+    const int n = c->rec_n * c->nbatch;
+    dim3 grid((n + 127) / 128, 1, 1), block(128, 1, 1);
+    void *p = c->d_u;
+    void *plo = c->d_ulo;
+    void *args[] = {&p, &plo, &c->bstride, &c->d_rec_dof, &c->rec_n, &c->nbatch, &c->d_trace, &c->rec_max,
+                    &c->d_step0, &kstep};
+    return cudaLaunchKernel(c->ks.record, grid, block, args, 0, c->stream);
 }
 
 // Forward-Euler steps ping-pong between (u, ulo) and (wa, acc): after each
@@ -268,9 +290,10 @@ cudaError_t launch_step(dg_ctx *c, int kstep, double dt, int method) {
     if (method == kMethodEuler) {
         if (e == cudaSuccess) e = launch_stage(c, kEulerStage, dt);
         swap_euler_buffers(c);
-        return e;
+    } else {
+        for (int s = 0; s < 4 && e == cudaSuccess; ++s) e = launch_stage(c, s, dt);
     }
-    for (int s = 0; s < 4 && e == cudaSuccess; ++s) e = launch_stage(c, s, dt);
+    if (e == cudaSuccess) e = launch_record(c, kstep);
     return e;
 }
 
@@ -294,7 +317,13 @@ void dg_default_opts(dg_opts *o) {
 }
 
 int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts_in, dg_ctx **out) {
+    return dg_create_batch(m, ph, opts_in, 1, out);
+}
+
+int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts_in, int nbatch,
+                    dg_ctx **out) {
     if (!m || !ph || !out) return fail(DG_ERR_ARG, "null argument");
+    if (nbatch < 1 || nbatch > 65535) return fail(DG_ERR_ARG, "batch size must be in 1..65535");
     *out = nullptr;
     dg_opts opts;
     if (opts_in) opts = *opts_in;
@@ -321,6 +350,8 @@ int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts
     dg_ctx *c = new dg_ctx();
     c->dim = dim; c->order = m->order; c->np = np; c->nf = nf; c->nfp = nfp; c->nq = dim + 1; c->K = K;
     c->ndof = (long long)K * np;
+    c->nbatch = nbatch;
+    c->bstride = c->ndof * c->nq;
     c->prec = opts.precision; c->flux_sign = opts.flux_sign; c->device = opts.device; c->use_graph = opts.use_graph;
     c->rsize = c->prec == DG_PREC_FP64 ? 8 : 4;
     c->c0 = ph->c0; c->rho0 = ph->rho0;
@@ -344,7 +375,7 @@ int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts
         if (!fin(cudaSetDevice(c->device), "cudaSetDevice")) break;
         if (!fin(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate")) break;
         size_t field_bytes = (size_t)c->ndof * c->rsize;
-        size_t state_bytes = field_bytes * c->nq;
+        size_t state_bytes = field_bytes * c->nq * c->nbatch;  // every member
         if (!fin(cudaMalloc(&c->d_state, 4 * state_bytes), "cudaMalloc(state)")) break;
         c->d_u = c->d_state;
         c->d_acc = c->d_state + state_bytes;
@@ -379,6 +410,7 @@ int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts
             break;
         if (!fin(cudaMalloc(&c->d_mon, 8 * 8), "cudaMalloc(mon)")) break;
         if (!fin(cudaMalloc(&c->d_bad, 8), "cudaMalloc(bad)")) break;
+        if (!fin(cudaMalloc(&c->d_step0, 8), "cudaMalloc(step0)")) break;
         if (c->prec != DG_PREC_FP64)
             if (!fin(cudaMalloc(&c->d_stage64, (size_t)c->ndof * 8), "cudaMalloc(staging)")) break;
         for (int s = 0; s < 5; ++s)
@@ -393,10 +425,12 @@ int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts
             break;
         if (!fin(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device), "attribute")) break;
         int ntiles = (K + c->ks.epb - 1) / c->ks.epb;
-        c->grid = std::max(1, std::min(ntiles, std::max(per_sm, 1) * nsm));
+        // resident blocks spread over the members (grid.y = member)
+        const int resident = std::max(per_sm, 1) * nsm;
+        c->grid = std::max(1, std::min(ntiles, (resident + nbatch - 1) / nbatch));
         if (c->mixed) {
-            if (!fin(cudaMalloc(&c->d_ulo, field_bytes * c->nq), "cudaMalloc(ulo)")) break;
-            if (!fin(cudaMemsetAsync(c->d_ulo, 0, field_bytes * c->nq, c->stream), "cudaMemset")) break;
+            if (!fin(cudaMalloc(&c->d_ulo, state_bytes), "cudaMalloc(ulo)")) break;
+            if (!fin(cudaMemsetAsync(c->d_ulo, 0, state_bytes, c->stream), "cudaMemset")) break;
             std::vector<uint8_t> img;
             std::vector<int> eb;
             c->mks.b_image(lay.ops.data(), img, eb);
@@ -414,8 +448,8 @@ int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts
                     break;
             if (rc != DG_OK) break;
             // one CTA per SM: each owns the SM's tensor memory
-            int mtiles = (K + c->mks.elems_per_tile - 1) / c->mks.elems_per_tile;
-            c->grid = std::max(1, std::min(mtiles, nsm));
+            long long mtiles = (long long)((K + c->mks.elems_per_tile - 1) / c->mks.elems_per_tile) * nbatch;
+            c->grid = (int)std::max(1LL, std::min(mtiles, (long long)nsm));
         }
         if (!fin(cudaStreamSynchronize(c->stream), "sync")) break;
     } while (0);
@@ -429,8 +463,12 @@ int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts
 
 void dg_destroy(dg_ctx *c) { free_ctx(c); }
 
-int dg_set_state(dg_ctx *c, const double *const u[4]) {
+}  // extern "C"
+
+namespace {
+int set_member(dg_ctx *c, int member, const double *const u[4]) {
     if (!c || !u) return fail(DG_ERR_ARG, "null argument");
+    if (member < 0 || member >= c->nbatch) return fail(DG_ERR_ARG, "batch member out of range");
     for (int f = 0; f < c->nq; ++f)
         if (!u[f]) return fail(DG_ERR_ARG, "null field");
     if (c->dim == 2 && u[3]) {
@@ -438,16 +476,16 @@ int dg_set_state(dg_ctx *c, const double *const u[4]) {
             if (u[3][i] != 0.0) return fail(DG_ERR_UNSUPPORTED, "2D meshes carry vz == 0; got a nonzero vz");
     }
     CK(cudaSetDevice(c->device));
-    size_t fb = (size_t)c->ndof * c->rsize;
+    const long long moff = (long long)member * c->bstride;  // values
     for (int f = 0; f < c->nq; ++f) {
-        char *dst = (char *)c->d_u + f * fb;
+        const long long off = moff + f * c->ndof;
+        char *dst = (char *)c->d_u + off * c->rsize;
         if (c->prec == DG_PREC_FP64) {
-            CK(cudaMemcpyAsync(dst, u[f], fb, cudaMemcpyHostToDevice, c->stream));
+            CK(cudaMemcpyAsync(dst, u[f], (size_t)c->ndof * 8, cudaMemcpyHostToDevice, c->stream));
         } else {
             CK(cudaMemcpyAsync(c->d_stage64, u[f], (size_t)c->ndof * 8, cudaMemcpyHostToDevice, c->stream));
             if (c->mixed)
-                split_kernel<<<1024, 256, 0, c->stream>>>(c->d_stage64, (float *)dst, c->d_ulo + f * c->ndof,
-                                                          c->ndof);
+                split_kernel<<<1024, 256, 0, c->stream>>>(c->d_stage64, (float *)dst, c->d_ulo + off, c->ndof);
             else
                 cast_kernel<float><<<1024, 256, 0, c->stream>>>(c->d_stage64, (float *)dst, c->ndof);
             CK(cudaGetLastError());
@@ -457,19 +495,20 @@ int dg_set_state(dg_ctx *c, const double *const u[4]) {
     return DG_OK;
 }
 
-int dg_get_state(dg_ctx *c, double *const u[4]) {
+int get_member(dg_ctx *c, int member, double *const u[4]) {
     if (!c || !u) return fail(DG_ERR_ARG, "null argument");
+    if (member < 0 || member >= c->nbatch) return fail(DG_ERR_ARG, "batch member out of range");
     CK(cudaSetDevice(c->device));
-    size_t fb = (size_t)c->ndof * c->rsize;
+    const long long moff = (long long)member * c->bstride;
     for (int f = 0; f < c->nq; ++f) {
         if (!u[f]) continue;
-        const char *src = (const char *)c->d_u + f * fb;
+        const long long off = moff + f * c->ndof;
+        const char *src = (const char *)c->d_u + off * c->rsize;
         if (c->prec == DG_PREC_FP64) {
-            CK(cudaMemcpyAsync(u[f], src, fb, cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaMemcpyAsync(u[f], src, (size_t)c->ndof * 8, cudaMemcpyDeviceToHost, c->stream));
         } else {
             if (c->mixed)
-                join_kernel<<<1024, 256, 0, c->stream>>>((const float *)src, c->d_ulo + f * c->ndof, c->d_stage64,
-                                                         c->ndof);
+                join_kernel<<<1024, 256, 0, c->stream>>>((const float *)src, c->d_ulo + off, c->d_stage64, c->ndof);
             else
                 uncast_kernel<float><<<1024, 256, 0, c->stream>>>((const float *)src, c->d_stage64, c->ndof);
             CK(cudaGetLastError());
@@ -481,45 +520,142 @@ int dg_get_state(dg_ctx *c, double *const u[4]) {
     return DG_OK;
 }
 
-int dg_set_sources(dg_ctx *c, int nsrc, const int *offsets, const int *dof_idx, const double *params) {
-    if (!c || nsrc < 0 || (nsrc > 0 && (!offsets || !params))) return fail(DG_ERR_ARG, "bad source arguments");
+// Uploads a source set: entries (member, node, source, weight) grouped by
+// state value, sources of a value kept in order.
+int upload_sources(dg_ctx *c, int nsrc, const double *params, const std::vector<long long> &at_of_entry,
+                   const std::vector<int> &src_of_entry, const std::vector<double> &w_of_entry) {
     CK(cudaSetDevice(c->device));
     CK(cudaStreamSynchronize(c->stream));
-    for (int *p : {c->d_src_dof, c->d_src_off, c->d_src_list})
+    if (c->d_src_at) cudaFree(c->d_src_at);
+    for (int *p : {c->d_src_off, c->d_src_list})
         if (p) cudaFree(p);
-    if (c->d_src_params) cudaFree(c->d_src_params);
-    c->d_src_dof = c->d_src_off = c->d_src_list = nullptr;
-    c->d_src_params = nullptr;
+    for (double *p : {c->d_src_w, c->d_src_params})
+        if (p) cudaFree(p);
+    c->d_src_at = nullptr;
+    c->d_src_off = c->d_src_list = nullptr;
+    c->d_src_w = c->d_src_params = nullptr;
     c->src_nodes = 0;
     c->src_duration.clear();
     if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
-    if (nsrc == 0) return DG_OK;
-    std::map<int, std::vector<int>> per_dof;  // dof -> sources in order
-    for (int s = 0; s < nsrc; ++s) {
-        if (offsets[s + 1] < offsets[s]) return fail(DG_ERR_ARG, "source offsets must be non-decreasing");
-        for (int k = offsets[s]; k < offsets[s + 1]; ++k) {
-            int d = dof_idx[k];
-            if (d < 0 || d >= c->ndof) return fail(DG_ERR_ARG, "source node index out of range");
-            per_dof[d].push_back(s);
+    for (int s = 0; s < nsrc; ++s) c->src_duration.push_back(params[s * 4 + 3]);
+    std::map<long long, std::vector<size_t>> per_value;  // state offset -> entries in order
+    for (size_t k = 0; k < at_of_entry.size(); ++k) per_value[at_of_entry[k]].push_back(k);
+    std::vector<long long> at;
+    std::vector<int> off(1, 0), lst;
+    std::vector<double> w;
+    for (auto &kv : per_value) {
+        at.push_back(kv.first);
+        for (size_t k : kv.second) {
+            lst.push_back(src_of_entry[k]);
+            w.push_back(w_of_entry[k]);
         }
-        c->src_duration.push_back(params[s * 4 + 3]);
-    }
-    std::vector<int> dofs, off(1, 0), lst;
-    for (auto &kv : per_dof) {
-        dofs.push_back(kv.first);
-        lst.insert(lst.end(), kv.second.begin(), kv.second.end());
         off.push_back((int)lst.size());
     }
-    c->src_nodes = (int)dofs.size();
+    c->src_nodes = (int)at.size();
     if (!c->src_nodes) return DG_OK;
-    CK(cudaMalloc(&c->d_src_dof, dofs.size() * 4));
+    CK(cudaMalloc(&c->d_src_at, at.size() * 8));
     CK(cudaMalloc(&c->d_src_off, off.size() * 4));
     CK(cudaMalloc(&c->d_src_list, lst.size() * 4));
+    CK(cudaMalloc(&c->d_src_w, w.size() * 8));
     CK(cudaMalloc(&c->d_src_params, (size_t)nsrc * 4 * 8));
-    CK(cudaMemcpy(c->d_src_dof, dofs.data(), dofs.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->d_src_at, at.data(), at.size() * 8, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->d_src_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->d_src_list, lst.data(), lst.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->d_src_w, w.data(), w.size() * 8, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->d_src_params, params, (size_t)nsrc * 4 * 8, cudaMemcpyHostToDevice));
+    return DG_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int dg_set_state(dg_ctx *c, const double *const u[4]) {
+    if (!c) return fail(DG_ERR_ARG, "null argument");
+    for (int m = 0; m < c->nbatch; ++m) {
+        int rc = set_member(c, m, u);
+        if (rc != DG_OK) return rc;
+    }
+    return DG_OK;
+}
+
+int dg_get_state(dg_ctx *c, double *const u[4]) { return get_member(c, 0, u); }
+
+int dg_set_state_member(dg_ctx *c, int member, const double *const u[4]) { return set_member(c, member, u); }
+
+int dg_get_state_member(dg_ctx *c, int member, double *const u[4]) { return get_member(c, member, u); }
+
+int dg_set_sources(dg_ctx *c, int nsrc, const int *offsets, const int *dof_idx, const double *params) {
+    if (!c || nsrc < 0 || (nsrc > 0 && (!offsets || !params))) return fail(DG_ERR_ARG, "bad source arguments");
+    std::vector<long long> at;
+    std::vector<int> src;
+    std::vector<double> w;
+    for (int m = 0; m < c->nbatch; ++m)
+        for (int s = 0; s < nsrc; ++s) {
+            if (offsets[s + 1] < offsets[s]) return fail(DG_ERR_ARG, "source offsets must be non-decreasing");
+            for (int k = offsets[s]; k < offsets[s + 1]; ++k) {
+                const int d = dof_idx[k];
+                if (d < 0 || d >= c->ndof) return fail(DG_ERR_ARG, "source node index out of range");
+                at.push_back((long long)m * c->bstride + d);
+                src.push_back(s);
+                w.push_back(1.0);
+            }
+        }
+    return upload_sources(c, nsrc, params, at, src, w);
+}
+
+int dg_set_batch_sources(dg_ctx *c, int nsrc, const int *member, const int *offsets, const int *dof_idx,
+                         const double *weights, const double *params) {
+    if (!c || nsrc < 0 || (nsrc > 0 && (!member || !offsets || !params)))
+        return fail(DG_ERR_ARG, "bad source arguments");
+    std::vector<long long> at;
+    std::vector<int> src;
+    std::vector<double> w;
+    for (int s = 0; s < nsrc; ++s) {
+        if (member[s] < 0 || member[s] >= c->nbatch) return fail(DG_ERR_ARG, "source member out of range");
+        if (offsets[s + 1] < offsets[s]) return fail(DG_ERR_ARG, "source offsets must be non-decreasing");
+        for (int k = offsets[s]; k < offsets[s + 1]; ++k) {
+            const int d = dof_idx[k];
+            if (d < 0 || d >= c->ndof) return fail(DG_ERR_ARG, "source node index out of range");
+            at.push_back((long long)member[s] * c->bstride + d);
+            src.push_back(s);
+            w.push_back(weights ? weights[k] : 1.0);
+        }
+    }
+    return upload_sources(c, nsrc, params, at, src, w);
+}
+
+int dg_set_receivers(dg_ctx *c, int nrec, const int *dof_idx, int max_steps) {
+    if (!c || nrec < 0 || max_steps < 0 || (nrec > 0 && !dof_idx)) return fail(DG_ERR_ARG, "bad receiver arguments");
+    for (int r = 0; r < nrec; ++r)
+        if (dof_idx[r] < 0 || dof_idx[r] >= c->ndof) return fail(DG_ERR_ARG, "receiver node index out of range");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->d_rec_dof) cudaFree(c->d_rec_dof);
+    if (c->d_trace) cudaFree(c->d_trace);
+    c->d_rec_dof = nullptr;
+    c->d_trace = nullptr;
+    c->rec_n = 0;
+    c->rec_max = 0;
+    c->rec_done = 0;
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+    if (nrec == 0 || max_steps == 0) return DG_OK;
+    const size_t tb = (size_t)nrec * c->nbatch * max_steps * 8;
+    CK(cudaMalloc(&c->d_rec_dof, (size_t)nrec * 4));
+    CK(cudaMalloc(&c->d_trace, tb));
+    CK(cudaMemcpy(c->d_rec_dof, dof_idx, (size_t)nrec * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemset(c->d_trace, 0, tb));
+    c->rec_n = nrec;
+    c->rec_max = max_steps;
+    return DG_OK;
+}
+
+int dg_get_traces(dg_ctx *c, double *out, int *steps) {
+    if (!c || !out) return fail(DG_ERR_ARG, "null argument");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    if (steps) *steps = (int)std::min<long long>(c->rec_done, c->rec_max);
+    if (!c->rec_n) return DG_OK;
+    CK(cudaMemcpy(out, c->d_trace, (size_t)c->rec_n * c->nbatch * c->rec_max * 8, cudaMemcpyDeviceToHost));
     return DG_OK;
 }
 
@@ -537,6 +673,11 @@ int enqueue_steps(dg_ctx *c, double *t, double dt, int nsteps, int method = kMet
         for (int k = 0; k < m; ++k) tend += dt;
         int with_src = (c->src_nodes && any_source_active(c, t0)) ? 1 : 0;
         CK(cudaMemcpyAsync(c->d_t0, &t0, 8, cudaMemcpyHostToDevice, c->stream));
+        if (c->rec_n) {
+            // pageable copy of a host value: staged before cudaMemcpyAsync returns
+            const long long s0 = c->rec_done;
+            CK(cudaMemcpyAsync(c->d_step0, &s0, 8, cudaMemcpyHostToDevice, c->stream));
+        }
         if (c->use_graph && m == kGraphChunk) {
             if (!c->gexec || c->graph_dt != dt || c->graph_src != with_src || c->graph_method != method) {
                 if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
@@ -575,16 +716,17 @@ int enqueue_steps(dg_ctx *c, double *t, double dt, int nsteps, int method = kMet
                 // an odd number of Euler steps leaves the state in the other
                 // buffer pair: copy it back so the state pointers stay fixed
                 swap_euler_buffers(c);
-                const size_t fb = (size_t)c->ndof * c->rsize * c->nq;
+                const size_t fb = (size_t)c->bstride * c->nbatch * c->rsize;
                 CK(cudaMemcpyAsync(c->d_u, c->d_wa, fb, cudaMemcpyDeviceToDevice, c->stream));
                 if (c->mixed)
-                    CK(cudaMemcpyAsync(c->d_ulo, c->d_acc, (size_t)c->ndof * 4 * c->nq, cudaMemcpyDeviceToDevice,
-                                       c->stream));
+                    CK(cudaMemcpyAsync(c->d_ulo, c->d_acc, (size_t)c->bstride * c->nbatch * 4,
+                                       cudaMemcpyDeviceToDevice, c->stream));
             }
         }
         // t0 lives on the host stack: a pageable copy is staged before return
         *t = tend;
         done += m;
+        c->rec_done += m;
     }
     return DG_OK;
 }
@@ -734,7 +876,7 @@ int dg_info(dg_ctx *c, long long *dofs, int *fields, long long *state_bytes) {
     if (!c) return fail(DG_ERR_ARG, "null context");
     if (dofs) *dofs = c->ndof;
     if (fields) *fields = c->nq;
-    if (state_bytes) *state_bytes = (long long)c->ndof * c->nq * c->rsize * 4;
+    if (state_bytes) *state_bytes = c->bstride * c->nbatch * (long long)c->rsize * 4;
     return DG_OK;
 }
 

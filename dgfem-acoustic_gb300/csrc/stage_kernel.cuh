@@ -96,218 +96,229 @@ __device__ __forceinline__ void load4<double>(const double *p, double (&v)[4]) {
     v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
 }
 
+// One tile of EPB elements: stages the state, evaluates the right-hand side
+// and applies the stage update.  sQ, sFn are the tile buffers; sOps, sTab
+// hold the reference operators and the face tables of order P.  Threads
+// with tid >= EPB*NP only take part in the barriers.
+template <int DIM, int P, typename Real, int STAGE, int EPB>
+__device__ __forceinline__ void stage_tile(const StageArgs<Real> &a, long long boff, int tile, Real *sQ, Real *sFn,
+                                           const Real *sOps, const uint8_t *sTab, int tid) {
+    using S = Shape<DIM, P>;
+    constexpr int NP = S::NP, NF = S::NF, NFP = S::NFP, NQ = S::NQ, NSLOT = S::NSLOT;
+    constexpr int NT = EPB * NP;
+    const Real *sD = sOps;
+    const Real *sL = sOps + DIM * NP * NP;
+    const uint8_t *sFmask = sTab;
+    const uint8_t *sPerm = sTab + NF * NFP;
+    const int le = tid / NP;
+    const int i = tid - le * NP;
+    const Real *win = a.win + boff;
+    const int e = tile * EPB + le;
+    const bool valid = (tid < NT) && (e < a.K);
+    const long long base = (long long)e * NP + i;
+    Real q[NQ];
+#pragma unroll
+    for (int f = 0; f < NQ; ++f) {
+        q[f] = valid ? win[f * a.fstride + base] : Real(0);
+        sQ[(le * NP + i) * 4 + f] = q[f];
+    }
+    __syncthreads();
+
+    // Reference-space derivatives of the primitive fields.
+    Real dq[NQ][DIM];
+#pragma unroll
+    for (int f = 0; f < NQ; ++f)
+#pragma unroll
+        for (int u = 0; u < DIM; ++u) dq[f][u] = Real(0);
+#pragma unroll 2
+    for (int j = 0; j < NP; ++j) {
+        Real qj[4];
+        load4<Real>(&sQ[(le * NP + j) * 4], qj);
+#pragma unroll
+        for (int u = 0; u < DIM; ++u) {
+            const Real d = sD[(u * NP + j) * NP + i];
+#pragma unroll
+            for (int f = 0; f < NQ; ++f) dq[f][u] = fma(d, qj[f], dq[f][u]);
+        }
+    }
+    // Physical derivatives and the volume term.
+    Real V[NQ];
+    {
+        Real B[DIM][DIM];
+#pragma unroll
+        for (int x = 0; x < DIM; ++x)
+#pragma unroll
+            for (int u = 0; u < DIM; ++u)
+                B[x][u] = valid ? Real(a.geo[(long long)e * DIM * DIM + x * DIM + u]) : Real(0);
+        Real g[NQ][DIM];
+#pragma unroll
+        for (int f = 0; f < NQ; ++f)
+#pragma unroll
+            for (int x = 0; x < DIM; ++x) {
+                Real s = Real(0);
+#pragma unroll
+                for (int u = 0; u < DIM; ++u) s = fma(B[x][u], dq[f][u], s);
+                g[f][x] = s;
+            }
+        Real div = Real(0), adv_p = Real(0);
+#pragma unroll
+        for (int x = 0; x < DIM; ++x) {
+            div += g[1 + x][x];
+            adv_p = fma(a.v0[x], g[0][x], adv_p);
+        }
+        V[0] = fma(a.rc2, div, adv_p);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            Real adv = Real(0);
+#pragma unroll
+            for (int x = 0; x < DIM; ++x) adv = fma(a.v0[x], g[1 + d][x], adv);
+            V[1 + d] = fma(a.inv_rho, g[0][d], adv);
+        }
+    }
+
+    // Face values at the element's face nodes.
+    for (int s = i; s < NSLOT; s += NP) {
+        const int lf = s / NFP;
+        const int k = s - lf * NFP;
+        const int vi = sFmask[lf * NFP + k];
+        Real own[4];
+        load4<Real>(&sQ[(le * NP + vi) * 4], own);
+        Real Fn[NQ];
+#pragma unroll
+        for (int f = 0; f < NQ; ++f) Fn[f] = Real(0);
+        Real scale = Real(0);
+        if (valid) {
+            const int2 cn = a.conn[(long long)e * NF + lf];
+            Real g4[4];
+            load4<Real>(&a.fgeo[((long long)e * NF + lf) * 4], g4);
+            Real n[DIM];
+#pragma unroll
+            for (int x = 0; x < DIM; ++x) n[x] = g4[x];
+            scale = g4[DIM];
+            Real vn0 = Real(0);
+#pragma unroll
+            for (int x = 0; x < DIM; ++x) vn0 = fma(a.v0[x], n[x], vn0);
+            const int kind = (cn.y >> 5) & 3;
+            if (kind == kKindInterior) {
+                const int nlf = cn.y & 3;
+                const int pm = (cn.y >> 2) & 7;
+                const Real tau = (cn.y & 128) ? Real(-1) : Real(1);
+                const int nvi = sFmask[nlf * NFP + sPerm[pm * NFP + k]];
+                const long long nb = (long long)cn.x * NP + nvi;
+                Real o[NQ];
+#pragma unroll
+                for (int f = 0; f < NQ; ++f) o[f] = __ldg(&win[f * a.fstride + nb]);
+                const Real sp = own[0] + o[0];
+                Real svn = Real(0);
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) svn = fma(own[1 + x] + o[1 + x], n[x], svn);
+                const Real hj = a.half_c0 * tau;
+                Fn[0] = fma(hj, own[0] - o[0], Real(0.5) * fma(vn0, sp, a.rc2 * svn));
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    Fn[1 + d] = fma(hj, own[1 + d] - o[1 + d],
+                                    Real(0.5) * fma(vn0, own[1 + d] + o[1 + d], a.inv_rho * sp * n[d]));
+            } else if (kind == kKindReflecting) {
+                Real vn = Real(0);
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) vn = fma(own[1 + x], n[x], vn);
+                Real vw[DIM];
+                Real vwn = Real(0);
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) {
+                    vw[x] = own[1 + x] - vn * n[x];
+                    vwn = fma(vw[x], n[x], vwn);
+                }
+                Fn[0] = fma(vn0, own[0], a.rc2 * vwn);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) Fn[1 + d] = fma(vn0, vw[d], a.inv_rho * own[0] * n[d]);
+            } else {
+                Real vn = Real(0);
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) vn = fma(own[1 + x], n[x], vn);
+                const Real q0 = Real(0.25) * a.c0;
+                Fn[0] = fma(q0, own[0], Real(0.25) * a.c0 * a.c0 * a.rho * vn);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    Fn[1 + d] = fma(Real(0.25) * n[d] * a.inv_rho, own[0], q0 * n[d] * vn);
+            }
+        }
+#pragma unroll
+        for (int f = 0; f < NQ; ++f) sFn[(le * NSLOT + s) * 4 + f] = scale * Fn[f];
+    }
+    __syncthreads();
+
+    // Lift and stage update.
+    Real L[NQ];
+#pragma unroll
+    for (int f = 0; f < NQ; ++f) L[f] = Real(0);
+#pragma unroll 4
+    for (int s = 0; s < NSLOT; ++s) {
+        const Real l = sL[s * NP + i];
+        Real fn[4];
+        load4<Real>(&sFn[(le * NSLOT + s) * 4], fn);
+#pragma unroll
+        for (int f = 0; f < NQ; ++f) L[f] = fma(l, fn[f], L[f]);
+    }
+    if (valid) {
+        Real *acc = a.acc + boff;
+        Real *wout = a.wout + boff;
+        const Real *uu = a.u + boff;
+#pragma unroll
+        for (int f = 0; f < NQ; ++f) {
+            const long long idx = f * a.fstride + base;
+            const Real r = a.dt * (V[f] - L[f]);
+            if (STAGE == 1) {
+                acc[idx] = r;
+                wout[idx] = fma(Real(0.5), r, q[f]);
+            } else if (STAGE == 2) {
+                acc[idx] = fma(Real(2), r, acc[idx]);
+                wout[idx] = fma(Real(0.5), r, uu[idx]);
+            } else if (STAGE == 3) {
+                acc[idx] = fma(Real(2), r, acc[idx]);
+                wout[idx] = uu[idx] + r;
+            } else if (STAGE == kStageEuler) {
+                wout[idx] = q[f] + r;
+            } else {
+                wout[idx] = uu[idx] + (acc[idx] + r) * (Real(1) / Real(6));
+            }
+        }
+    }
+    __syncthreads();
+}
+
 // STAGE 1-4: the classical RK4 stages; kStageEuler: one forward-Euler step
 // wout = win + dt*RHS(win) (the reference's numStep with beta = 1).
 template <int DIM, int P, typename Real, int STAGE, int EPB>
 __global__ void __launch_bounds__(EPB *Shape<DIM, P>::NP)
     stage_kernel(const StageArgs<Real> a) {
     using S = Shape<DIM, P>;
-    constexpr int NP = S::NP, NF = S::NF, NFP = S::NFP, NQ = S::NQ, NSLOT = S::NSLOT;
+    constexpr int NP = S::NP;
     constexpr int NT = EPB * NP;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Real *sOps = reinterpret_cast<Real *>(smem_raw);
     Real *sQ = sOps + S::NOPS_PAD;
     Real *sFn = sQ + EPB * NP * 4;
-    uint8_t *sTab = reinterpret_cast<uint8_t *>(sFn + EPB * NSLOT * 4);
-    const Real *sD = sOps;
-    const Real *sL = sOps + DIM * NP * NP;
-    const uint8_t *sFmask = sTab;
-    const uint8_t *sPerm = sTab + NF * NFP;
-
+    uint8_t *sTab = reinterpret_cast<uint8_t *>(sFn + EPB * S::NSLOT * 4);
     const int tid = threadIdx.x;
-    const int le = tid / NP;
-    const int i = tid - le * NP;
     const long long boff = (long long)blockIdx.y * a.bstride;
-    const Real *win = a.win + boff;
-
     for (int k = tid; k < S::NOPS; k += NT) sOps[k] = a.ops[k];
     for (int k = tid; k < S::NTAB; k += NT) sTab[k] = a.tabs[k];
     __syncthreads();
-
     const int ntiles = (a.K + EPB - 1) / EPB;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int e = tile * EPB + le;
-        const bool valid = (tid < NT) && (e < a.K);
-        const long long base = (long long)e * NP + i;
-        Real q[NQ];
-#pragma unroll
-        for (int f = 0; f < NQ; ++f) {
-            q[f] = valid ? win[f * a.fstride + base] : Real(0);
-            sQ[(le * NP + i) * 4 + f] = q[f];
-        }
-        __syncthreads();
-
-        // Reference-space derivatives of the primitive fields.
-        Real dq[NQ][DIM];
-#pragma unroll
-        for (int f = 0; f < NQ; ++f)
-#pragma unroll
-            for (int u = 0; u < DIM; ++u) dq[f][u] = Real(0);
-#pragma unroll 2
-        for (int j = 0; j < NP; ++j) {
-            Real qj[4];
-            load4<Real>(&sQ[(le * NP + j) * 4], qj);
-#pragma unroll
-            for (int u = 0; u < DIM; ++u) {
-                const Real d = sD[(u * NP + j) * NP + i];
-#pragma unroll
-                for (int f = 0; f < NQ; ++f) dq[f][u] = fma(d, qj[f], dq[f][u]);
-            }
-        }
-        // Physical derivatives and the volume term.
-        Real V[NQ];
-        {
-            Real B[DIM][DIM];
-#pragma unroll
-            for (int x = 0; x < DIM; ++x)
-#pragma unroll
-                for (int u = 0; u < DIM; ++u)
-                    B[x][u] = valid ? Real(a.geo[(long long)e * DIM * DIM + x * DIM + u]) : Real(0);
-            Real g[NQ][DIM];
-#pragma unroll
-            for (int f = 0; f < NQ; ++f)
-#pragma unroll
-                for (int x = 0; x < DIM; ++x) {
-                    Real s = Real(0);
-#pragma unroll
-                    for (int u = 0; u < DIM; ++u) s = fma(B[x][u], dq[f][u], s);
-                    g[f][x] = s;
-                }
-            Real div = Real(0), adv_p = Real(0);
-#pragma unroll
-            for (int x = 0; x < DIM; ++x) {
-                div += g[1 + x][x];
-                adv_p = fma(a.v0[x], g[0][x], adv_p);
-            }
-            V[0] = fma(a.rc2, div, adv_p);
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                Real adv = Real(0);
-#pragma unroll
-                for (int x = 0; x < DIM; ++x) adv = fma(a.v0[x], g[1 + d][x], adv);
-                V[1 + d] = fma(a.inv_rho, g[0][d], adv);
-            }
-        }
-
-        // Face values at the element's face nodes.
-        for (int s = i; s < NSLOT; s += NP) {
-            const int lf = s / NFP;
-            const int k = s - lf * NFP;
-            const int vi = sFmask[lf * NFP + k];
-            Real own[4];
-            load4<Real>(&sQ[(le * NP + vi) * 4], own);
-            Real Fn[NQ];
-#pragma unroll
-            for (int f = 0; f < NQ; ++f) Fn[f] = Real(0);
-            Real scale = Real(0);
-            if (valid) {
-                const int2 cn = a.conn[(long long)e * NF + lf];
-                Real g4[4];
-                load4<Real>(&a.fgeo[((long long)e * NF + lf) * 4], g4);
-                Real n[DIM];
-#pragma unroll
-                for (int x = 0; x < DIM; ++x) n[x] = g4[x];
-                scale = g4[DIM];
-                Real vn0 = Real(0);
-#pragma unroll
-                for (int x = 0; x < DIM; ++x) vn0 = fma(a.v0[x], n[x], vn0);
-                const int kind = (cn.y >> 5) & 3;
-                if (kind == kKindInterior) {
-                    const int nlf = cn.y & 3;
-                    const int pm = (cn.y >> 2) & 7;
-                    const Real tau = (cn.y & 128) ? Real(-1) : Real(1);
-                    const int nvi = sFmask[nlf * NFP + sPerm[pm * NFP + k]];
-                    const long long nb = (long long)cn.x * NP + nvi;
-                    Real o[NQ];
-#pragma unroll
-                    for (int f = 0; f < NQ; ++f) o[f] = __ldg(&win[f * a.fstride + nb]);
-                    const Real sp = own[0] + o[0];
-                    Real svn = Real(0);
-#pragma unroll
-                    for (int x = 0; x < DIM; ++x) svn = fma(own[1 + x] + o[1 + x], n[x], svn);
-                    const Real hj = a.half_c0 * tau;
-                    Fn[0] = fma(hj, own[0] - o[0], Real(0.5) * fma(vn0, sp, a.rc2 * svn));
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d)
-                        Fn[1 + d] = fma(hj, own[1 + d] - o[1 + d],
-                                        Real(0.5) * fma(vn0, own[1 + d] + o[1 + d], a.inv_rho * sp * n[d]));
-                } else if (kind == kKindReflecting) {
-                    Real vn = Real(0);
-#pragma unroll
-                    for (int x = 0; x < DIM; ++x) vn = fma(own[1 + x], n[x], vn);
-                    Real vw[DIM];
-                    Real vwn = Real(0);
-#pragma unroll
-                    for (int x = 0; x < DIM; ++x) {
-                        vw[x] = own[1 + x] - vn * n[x];
-                        vwn = fma(vw[x], n[x], vwn);
-                    }
-                    Fn[0] = fma(vn0, own[0], a.rc2 * vwn);
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d) Fn[1 + d] = fma(vn0, vw[d], a.inv_rho * own[0] * n[d]);
-                } else {
-                    Real vn = Real(0);
-#pragma unroll
-                    for (int x = 0; x < DIM; ++x) vn = fma(own[1 + x], n[x], vn);
-                    const Real q0 = Real(0.25) * a.c0;
-                    Fn[0] = fma(q0, own[0], Real(0.25) * a.c0 * a.c0 * a.rho * vn);
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d)
-                        Fn[1 + d] = fma(Real(0.25) * n[d] * a.inv_rho, own[0], q0 * n[d] * vn);
-                }
-            }
-#pragma unroll
-            for (int f = 0; f < NQ; ++f) sFn[(le * NSLOT + s) * 4 + f] = scale * Fn[f];
-        }
-        __syncthreads();
-
-        // Lift and stage update.
-        Real L[NQ];
-#pragma unroll
-        for (int f = 0; f < NQ; ++f) L[f] = Real(0);
-#pragma unroll 4
-        for (int s = 0; s < NSLOT; ++s) {
-            const Real l = sL[s * NP + i];
-            Real fn[4];
-            load4<Real>(&sFn[(le * NSLOT + s) * 4], fn);
-#pragma unroll
-            for (int f = 0; f < NQ; ++f) L[f] = fma(l, fn[f], L[f]);
-        }
-        if (valid) {
-            Real *acc = a.acc + boff;
-            Real *wout = a.wout + boff;
-            const Real *uu = a.u + boff;
-#pragma unroll
-            for (int f = 0; f < NQ; ++f) {
-                const long long idx = f * a.fstride + base;
-                const Real r = a.dt * (V[f] - L[f]);
-                if (STAGE == 1) {
-                    acc[idx] = r;
-                    wout[idx] = fma(Real(0.5), r, q[f]);
-                } else if (STAGE == 2) {
-                    acc[idx] = fma(Real(2), r, acc[idx]);
-                    wout[idx] = fma(Real(0.5), r, uu[idx]);
-                } else if (STAGE == 3) {
-                    acc[idx] = fma(Real(2), r, acc[idx]);
-                    wout[idx] = uu[idx] + r;
-                } else if (STAGE == kStageEuler) {
-                    wout[idx] = q[f] + r;
-                } else {
-                    wout[idx] = uu[idx] + (acc[idx] + r) * (Real(1) / Real(6));
-                }
-            }
-        }
-        __syncthreads();
-    }
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+        stage_tile<DIM, P, Real, STAGE, EPB>(a, boff, tile, sQ, sFn, sOps, sTab, tid);
 }
 
 // Hard sources (solver.cpp:248-256): p = amp sin(2 pi f t + phase) while
-// t < duration.  Thread per source node; the node's sources are applied in
-// order so the last active one wins, as in the reference's loop.  t is the
-// reference's accumulated time: t0 plus k additions of dt.
+// t < duration, scaled by a per-(source, node) weight (1 for the reference's
+// sources).  Thread per source node; node j is the state value at offset
+// at[j] (batch member and node folded in) and its sources are applied in
+// order, so a later active source overwrites an earlier one (the reference's
+// loop order).  t = t0 + kstep*dt by repeated addition, as the host loop.
 template <typename Real>
-__global__ void inject_kernel(Real *p, long long bstride, const int *node_dof, const int *node_src_off,
-                              const int *node_src, const double *params, const double *t0, int kstep, double dt,
+__global__ void inject_kernel(Real *p, const long long *at, const int *node_src_off, const int *node_src,
+                              const double *node_w, const double *params, const double *t0, int kstep, double dt,
                               int nnodes, Real *plo) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nnodes) return;
@@ -318,16 +329,31 @@ __global__ void inject_kernel(Real *p, long long bstride, const int *node_dof, c
     for (int s = node_src_off[j]; s < node_src_off[j + 1]; ++s) {
         const double *pr = params + 4 * node_src[s];
         if (t < pr[3]) {
-            val = pr[0] * sin(2 * M_PI * pr[1] * t + pr[2]);
+            val = node_w[s] * (pr[0] * sin(2 * M_PI * pr[1] * t + pr[2]));
             set = true;
         }
     }
     if (set) {
-        const long long at = (long long)blockIdx.y * bstride + node_dof[j];
-        p[at] = Real(val);
+        p[at[j]] = Real(val);
         // state kept as a pair: low part of the injected value
-        if (plo) plo[at] = Real(val - double(Real(val)));
+        if (plo) plo[at[j]] = Real(val - double(Real(val)));
     }
+}
+
+// Receivers: the pressure of every batch member at nrec nodes after step
+// (*step0 + kstep), into trace[member][rec][max_steps].
+template <typename Real>
+__global__ void record_kernel(const Real *p, const Real *plo, long long bstride, const int *rec_dof, int nrec,
+                              int nbatch, double *trace, int max_steps, const long long *step0, int kstep) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nrec * nbatch) return;
+    const long long step = *step0 + kstep;
+    if (step >= max_steps) return;
+    const int m = j / nrec, r = j - m * nrec;
+    const long long at = m * bstride + rec_dof[r];
+    double v = double(p[at]);
+    if (plo) v += double(plo[at]);
+    trace[(long long)j * max_steps + step] = v;
 }
 
 }  // namespace dgk

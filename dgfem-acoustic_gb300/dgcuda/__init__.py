@@ -135,6 +135,23 @@ def _declare(L: C.CDLL) -> None:
         "dg_layout_free": (None, [vp]),
         "dg_tc_selftest": (C.c_int, [C.c_int, P_d]),
         "dg_euler_steps": (C.c_int, [vp, P_d, C.c_double, C.c_int]),
+        "dg_multi_create": (C.c_int, [C.c_int, vp, vp, C.POINTER(Opts), C.POINTER(vp)]),
+        "dg_multi_destroy": (None, [vp]),
+        "dg_multi_set_state": (C.c_int, [vp, C.c_int, C.POINTER(P_d)]),
+        "dg_multi_get_state": (C.c_int, [vp, C.c_int, C.POINTER(P_d)]),
+        "dg_multi_set_sources": (C.c_int, [vp, C.c_int, P_i, P_i, P_i, P_d, P_d]),
+        "dg_multi_rk4_steps": (C.c_int, [vp, P_d, P_d, C.c_int]),
+        "dg_multi_rk4_steps_timed": (C.c_int, [vp, P_d, P_d, C.c_int, P_d]),
+        "dg_multi_set_config": (C.c_int, [vp, C.c_int]),
+        "dg_multi_autotune": (C.c_int, [vp, P_d, C.c_int, P_i, P_d]),
+        "dg_multi_info": (C.c_int, [vp, C.POINTER(C.c_longlong), P_i, P_i, P_i]),
+        "dg_create_batch": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(PhysDesc), C.POINTER(Opts), C.c_int,
+                                      C.POINTER(vp)]),
+        "dg_set_state_member": (C.c_int, [vp, C.c_int, C.POINTER(P_d)]),
+        "dg_get_state_member": (C.c_int, [vp, C.c_int, C.POINTER(P_d)]),
+        "dg_set_batch_sources": (C.c_int, [vp, C.c_int, P_i, P_i, P_i, P_d, P_d]),
+        "dg_set_receivers": (C.c_int, [vp, C.c_int, P_i, C.c_int]),
+        "dg_get_traces": (C.c_int, [vp, P_d, C.POINTER(C.c_int)]),
         "dg_rk4_steps_noalloc": (C.c_int, [C.POINTER(DeviceLayout), C.c_void_p, P_d, C.c_double, C.c_int,
                                            C.c_void_p]),
         "dgm_read_msh": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
@@ -379,12 +396,20 @@ class Precomp:
         _check(lib().dgm_source_dofs(self._h, x, y, z, size, _iptr(idx), cnt.value, C.byref(cnt)))
         return idx[:cnt.value]
 
+    def gaussian_source(self, x: float, y: float, z: float, sigma: float) -> tuple[np.ndarray, np.ndarray]:
+        """Nodes within 3 sigma of (x, y, z) and their weights exp(-r^2/(2 sigma^2))
+        (a Gaussian-in-space hard source for dg_set_batch_sources)."""
+        c = self.dof_coords()
+        r2 = (c[:, 0] - x) ** 2 + (c[:, 1] - y) ** 2 + (c[:, 2] - z) ** 2
+        idx = np.nonzero(r2 < (3.0 * sigma) ** 2)[0].astype(np.int32)
+        return idx, np.exp(-r2[idx] / (2 * sigma * sigma))
+
 
 class Solver:
     """GPU RK4 right-hand side context (dg_create ... dg_destroy)."""
 
     def __init__(self, pre: Precomp, c0: float, rho0: float, v0=(0.0, 0.0, 0.0), precision: str = "fp64",
-                 flux: str = "reference", use_graph: bool = True, device: int = 0):
+                 flux: str = "reference", use_graph: bool = True, device: int = 0, nbatch: int = 1):
         d = pre.desc()
         ph = PhysDesc(c0, rho0, (C.c_double * 3)(*v0))
         o = Opts()
@@ -394,8 +419,10 @@ class Solver:
         o.use_graph = 1 if use_graph else 0
         o.device = device
         h = C.c_void_p()
-        _check(lib().dg_create(C.byref(d), C.byref(ph), C.byref(o), C.byref(h)))
+        _check(lib().dg_create_batch(C.byref(d), C.byref(ph), C.byref(o), nbatch, C.byref(h)))
         self._h = h
+        self.nbatch = nbatch
+        self._rec = (0, 0)
         self.pre = pre
         self.dim = pre.dim
         self.ndof = pre.ndof
@@ -408,17 +435,21 @@ class Solver:
 
     __del__ = close
 
-    def set_state(self, u: np.ndarray) -> None:
+    def set_state(self, u: np.ndarray, member: int | None = None) -> None:
+        """Sets every batch member (member=None) or one member to u [4][ndof]."""
         u = np.ascontiguousarray(u, dtype=np.float64)
         assert u.shape == (4, self.ndof)
         ptrs = (P_d * 4)(*[_dptr(u[q]) for q in range(4)])
-        _check(lib().dg_set_state(self._h, ptrs))
+        if member is None:
+            _check(lib().dg_set_state(self._h, ptrs))
+        else:
+            _check(lib().dg_set_state_member(self._h, member, ptrs))
 
-    def get_state(self, out: np.ndarray | None = None) -> np.ndarray:
+    def get_state(self, out: np.ndarray | None = None, member: int = 0) -> np.ndarray:
         if out is None:
             out = np.empty((4, self.ndof))
         ptrs = (P_d * 4)(*[_dptr(out[q]) for q in range(4)])
-        _check(lib().dg_get_state(self._h, ptrs))
+        _check(lib().dg_get_state_member(self._h, member, ptrs))
         return out
 
     def set_sources(self, sources: list[tuple[np.ndarray, float, float, float, float]]) -> None:
@@ -432,6 +463,38 @@ class Solver:
         idx_a = np.concatenate(idx) if idx else np.zeros(1, dtype=np.int32)
         par_a = np.array(par if par else [0.0], dtype=np.float64)
         _check(lib().dg_set_sources(self._h, len(sources), _iptr(off), _iptr(idx_a), _dptr(par_a)))
+
+    def set_batch_sources(self, sources: list) -> None:
+        """sources: (member, dof indices, weights or None, amp, freq, phase,
+        duration); source s acts on its member only."""
+        n = len(sources)
+        off = np.zeros(n + 1, dtype=np.int32)
+        mem = np.zeros(max(n, 1), dtype=np.int32)
+        idx, wts, par = [], [], []
+        for s, (m, dofs, w, amp, freq, phase, dur) in enumerate(sources):
+            mem[s] = m
+            idx.append(np.asarray(dofs, dtype=np.int32))
+            wts.append(np.ones(len(dofs)) if w is None else np.asarray(w, dtype=np.float64))
+            off[s + 1] = off[s] + len(dofs)
+            par += [amp, freq, phase, dur]
+        idx_a = np.concatenate(idx) if idx else np.zeros(1, dtype=np.int32)
+        w_a = np.concatenate(wts) if wts else np.zeros(1)
+        par_a = np.array(par if par else [0.0], dtype=np.float64)
+        _check(lib().dg_set_batch_sources(self._h, n, _iptr(mem), _iptr(off), _iptr(idx_a), _dptr(w_a),
+                                          _dptr(par_a)))
+
+    def set_receivers(self, dofs, max_steps: int) -> None:
+        d = np.ascontiguousarray(dofs, dtype=np.int32)
+        _check(lib().dg_set_receivers(self._h, len(d), _iptr(d) if len(d) else None, max_steps))
+        self._rec = (len(d), max_steps)
+
+    def traces(self) -> np.ndarray:
+        """Pressure at the receivers after each recorded step: [member][rec][step]."""
+        nrec, mx = self._rec
+        out = np.zeros((self.nbatch, nrec, mx))
+        steps = C.c_int()
+        _check(lib().dg_get_traces(self._h, _dptr(out) if out.size else _dptr(np.zeros(1)), C.byref(steps)))
+        return out[:, :, :steps.value]
 
     def rk4_steps(self, t: float, dt: float, nsteps: int) -> float:
         tt = C.c_double(t)
@@ -498,3 +561,94 @@ def cfl_dt(pre: Precomp, c0: float, v0=(0.0, 0.0, 0.0), cfl: float = 0.5) -> flo
     rule used for the generated benchmark configurations)."""
     vmag = float(np.linalg.norm(v0))
     return cfl * 2 * min_inradius(pre) / ((2 * pre.order + 1) * (c0 + vmag))
+
+
+class MultiSolver:
+    """Uneven multi-mesh batch (dg_multi_*): 3D meshes of any sizes and orders
+    stepped together, one persistent launch per RK4 stage."""
+
+    def __init__(self, pres: list, phys: list, precision: str = "fp32", flux: str = "reference",
+                 use_graph: bool = True, device: int = 0):
+        n = len(pres)
+        self._descs = (MeshDesc * n)(*[p.desc() for p in pres])
+        self._phys = (PhysDesc * n)(*[PhysDesc(c0, rho0, (C.c_double * 3)(*v0)) for (c0, rho0, v0) in phys])
+        o = Opts()
+        lib().dg_default_opts(C.byref(o))
+        o.precision = {"fp64": PREC_FP64, "fp32": PREC_FP32}[precision]
+        o.flux_sign = {"reference": FLUX_REFERENCE, "upwind": FLUX_UPWIND}[flux]
+        o.use_graph = 1 if use_graph else 0
+        o.device = device
+        h = C.c_void_p()
+        _check(lib().dg_multi_create(n, C.cast(self._descs, C.c_void_p), C.cast(self._phys, C.c_void_p),
+                                     C.byref(o), C.byref(h)))
+        self._h = h
+        self.pres = pres
+        self.n = n
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.dg_multi_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def set_state(self, mesh: int, u: np.ndarray) -> None:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        ptrs = (P_d * 4)(*[_dptr(u[q]) for q in range(4)])
+        _check(lib().dg_multi_set_state(self._h, mesh, ptrs))
+
+    def get_state(self, mesh: int) -> np.ndarray:
+        out = np.empty((4, self.pres[mesh].ndof))
+        ptrs = (P_d * 4)(*[_dptr(out[q]) for q in range(4)])
+        _check(lib().dg_multi_get_state(self._h, mesh, ptrs))
+        return out
+
+    def set_sources(self, sources: list) -> None:
+        """sources: (mesh, dof indices, weights or None, amp, freq, phase, duration)."""
+        n = len(sources)
+        off = np.zeros(n + 1, dtype=np.int32)
+        mesh = np.zeros(max(n, 1), dtype=np.int32)
+        idx, wts, par = [], [], []
+        for s, (m, dofs, w, amp, freq, phase, dur) in enumerate(sources):
+            mesh[s] = m
+            idx.append(np.asarray(dofs, dtype=np.int32))
+            wts.append(np.ones(len(dofs)) if w is None else np.asarray(w, dtype=np.float64))
+            off[s + 1] = off[s] + len(dofs)
+            par += [amp, freq, phase, dur]
+        idx_a = np.concatenate(idx) if idx else np.zeros(1, dtype=np.int32)
+        w_a = np.concatenate(wts) if wts else np.zeros(1)
+        par_a = np.array(par if par else [0.0], dtype=np.float64)
+        _check(lib().dg_multi_set_sources(self._h, n, _iptr(mesh), _iptr(off), _iptr(idx_a), _dptr(w_a),
+                                          _dptr(par_a)))
+
+    def rk4_steps(self, t, dt, nsteps: int) -> np.ndarray:
+        tt = np.ascontiguousarray(t, dtype=np.float64).copy()
+        d = np.ascontiguousarray(dt, dtype=np.float64)
+        _check(lib().dg_multi_rk4_steps(self._h, _dptr(tt), _dptr(d), nsteps))
+        return tt
+
+    def rk4_steps_timed(self, t, dt, nsteps: int) -> tuple[np.ndarray, float]:
+        tt = np.ascontiguousarray(t, dtype=np.float64).copy()
+        d = np.ascontiguousarray(dt, dtype=np.float64)
+        ms = C.c_double()
+        _check(lib().dg_multi_rk4_steps_timed(self._h, _dptr(tt), _dptr(d), nsteps, C.byref(ms)))
+        return tt, ms.value
+
+    def set_config(self, cfg: int) -> None:
+        _check(lib().dg_multi_set_config(self._h, cfg))
+
+    def autotune(self, dt, trial_steps: int = 4) -> tuple[int, list]:
+        d = np.ascontiguousarray(dt, dtype=np.float64)
+        info = self.info()
+        ms = np.zeros(info["ncfg"])
+        ch = C.c_int()
+        _check(lib().dg_multi_autotune(self._h, _dptr(d), trial_steps, C.byref(ch), _dptr(ms)))
+        return ch.value, ms.tolist()
+
+    def info(self) -> dict:
+        dofs = C.c_longlong()
+        ncfg, cfg = C.c_int(), C.c_int()
+        bt = (C.c_int * 8)()
+        _check(lib().dg_multi_info(self._h, C.byref(dofs), C.byref(ncfg), C.byref(cfg), bt))
+        return {"dofs_per_field": dofs.value, "ncfg": ncfg.value, "cfg": cfg.value,
+                "block_threads": list(bt)[:ncfg.value]}

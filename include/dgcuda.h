@@ -113,8 +113,32 @@ int dg_get_state(dg_ctx *ctx, double *const u[4]);
 /* Hard sources: for source s, nodes dof_idx[offsets[s] .. offsets[s+1]) get
  * p = amp*sin(2*pi*freq*t + phase) while t < duration, at the start of each
  * step.  params[s*4 + 0..3] = amp, freq, phase, duration.  Later sources
- * overwrite earlier ones on shared nodes. */
+ * overwrite earlier ones on shared nodes.  In a batch context every member
+ * gets the same sources. */
 int dg_set_sources(dg_ctx *ctx, int nsrc, const int *offsets, const int *dof_idx, const double *params);
+
+/* Batch contexts (no counterpart in the reference, which runs one source
+ * configuration per process): nbatch independent states on one mesh, stepped
+ * together by every step call (one launch per stage covers all members).
+ * dg_create is dg_create_batch with nbatch = 1.  dg_set_state sets every
+ * member, dg_get_state and dg_monitors read member 0. */
+int dg_create_batch(const dg_mesh_desc *mesh, const dg_phys_desc *phys, const dg_opts *opts, int nbatch,
+                    dg_ctx **out);
+int dg_set_state_member(dg_ctx *ctx, int member, const double *const u[4]);
+int dg_get_state_member(dg_ctx *ctx, int member, double *const u[4]);
+
+/* Per-member sources: source s acts on member[s] only, node k of it with
+ * p = weights[k]*amp*sin(2*pi*freq*t + phase) (weights may be NULL: all 1,
+ * the reference's hard source).  Replaces any earlier source set. */
+int dg_set_batch_sources(dg_ctx *ctx, int nsrc, const int *member, const int *offsets, const int *dof_idx,
+                         const double *weights, const double *params);
+
+/* Receivers: after every step the pressure of every member at nrec nodes is
+ * recorded on the device, for the first max_steps steps after this call.
+ * dg_get_traces copies out[member][rec][max_steps] and the number of steps
+ * recorded. */
+int dg_set_receivers(dg_ctx *ctx, int nrec, const int *dof_idx, int max_steps);
+int dg_get_traces(dg_ctx *ctx, double *out, int *steps);
 
 /* nsteps classical RK4 steps starting at *t; *t is advanced by repeated
  * t += dt in double, as the reference loop does. */
@@ -201,6 +225,31 @@ typedef struct dg_device_layout {
     const unsigned char *tabs;  /* device face masks then permutations */
 } dg_device_layout;
 int dg_rk4_steps_noalloc(const dg_device_layout *layout, double *u, double *t, double dt, int nsteps, void *stream);
+
+/* Uneven multi-mesh batches (no counterpart in the reference, which runs one
+ * mesh per process): nmesh 3D meshes of any sizes and orders 1-5, each with
+ * its own medium and mean flow, stepped together by one persistent launch
+ * per RK4 stage (a list of (mesh, element tile) work items shared by the
+ * CTAs), chunks of steps captured in CUDA graphs.  FP64 or FP32.  Every mesh
+ * has its own time t[i] and step dt[i]. */
+typedef struct dg_multi dg_multi;
+int dg_multi_create(int nmesh, const dg_mesh_desc *meshes, const dg_phys_desc *phys, const dg_opts *opts,
+                    dg_multi **out);
+void dg_multi_destroy(dg_multi *ctx);
+int dg_multi_set_state(dg_multi *ctx, int mesh, const double *const u[4]);
+int dg_multi_get_state(dg_multi *ctx, int mesh, double *const u[4]);
+/* Sources as dg_set_batch_sources, with a mesh index per source. */
+int dg_multi_set_sources(dg_multi *ctx, int nsrc, const int *mesh, const int *offsets, const int *dof_idx,
+                         const double *weights, const double *params);
+int dg_multi_rk4_steps(dg_multi *ctx, double *t, const double *dt, int nsteps);
+int dg_multi_rk4_steps_timed(dg_multi *ctx, double *t, const double *dt, int nsteps, double *ms);
+/* Tile configurations: CTA sizes (block_threads[k]); elements per CTA =
+ * block threads / element nodes for each order.  dg_multi_autotune times
+ * each on trial_steps steps of the batch (the state is restored), keeps the
+ * fastest and reports ms per step of every candidate. */
+int dg_multi_set_config(dg_multi *ctx, int cfg);
+int dg_multi_autotune(dg_multi *ctx, const double *dt, int trial_steps, int *chosen, double *ms_per_step);
+int dg_multi_info(dg_multi *ctx, long long *dofs_per_field, int *ncfg, int *cfg, int *block_threads);
 
 /* Self-test of the tensor-core primitives of the mixed form (no counterpart
  * in the reference): a 128x32x112 BF16 GEMM with A in tensor memory and B in

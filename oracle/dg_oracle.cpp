@@ -804,6 +804,10 @@ struct Solver {
     std::vector<std::vector<std::vector<double>>> Flux;
     std::vector<std::vector<double>> u, k1, k2, k3, k4;
     std::vector<std::vector<int>> srcIndices;
+    // Per-node weights of Gaussian-in-space sources (type 1, not a reference
+    // source type: nodes within 3 sigma, weight exp(-r^2 / (2 sigma^2)),
+    // sigma = the size field); reference sources (type 0) have weight 1.
+    std::vector<std::vector<double>> srcWeights;
 
     void numStep(std::vector<std::vector<double>> &uu, double beta) {
         for (int eq = 0; eq < 4; ++eq) {
@@ -828,16 +832,25 @@ struct Solver {
             4, std::vector<std::vector<double>>(numNodes, std::vector<double>(3)));
         mesh->precomputeMassMatrix();
         srcIndices.clear();
+        srcWeights.clear();
         for (size_t i = 0; i < config.sources.size(); ++i) {
             std::vector<int> indice;
+            std::vector<double> weight;
+            const bool gaussian = config.sources[i][0] == 1.0;
+            const double radius = gaussian ? 3.0 * config.sources[i][4] : config.sources[i][4];
             for (int n = 0; n < numNodes; n++) {
                 const double *coord = mesh->model.getNode(mesh->m_elNodeTags[n]);
-                if (std::pow(coord[0] - config.sources[i][1], 2) + std::pow(coord[1] - config.sources[i][2], 2) +
-                        std::pow(coord[2] - config.sources[i][3], 2) <
-                    std::pow(config.sources[i][4], 2))
+                const double r2 = std::pow(coord[0] - config.sources[i][1], 2) +
+                                  std::pow(coord[1] - config.sources[i][2], 2) +
+                                  std::pow(coord[2] - config.sources[i][3], 2);
+                if (r2 < std::pow(radius, 2)) {
                     indice.push_back(n);
+                    const double sg = config.sources[i][4];
+                    weight.push_back(gaussian ? std::exp(-r2 / (2 * sg * sg)) : 1.0);
+                }
             }
             srcIndices.push_back(indice);
+            srcWeights.push_back(weight);
         }
         u.assign(4, std::vector<double>(numNodes, 0.0));
     }
@@ -853,7 +866,7 @@ struct Solver {
             double phase = config.sources[src][7], duration = config.sources[src][8];
             if (t < duration)
                 for (size_t n = 0; n < srcIndices[src].size(); ++n)
-                    u[0][srcIndices[src][n]] = amp * std::sin(2 * M_PI * freq * t + phase);
+                    u[0][srcIndices[src][n]] = srcWeights[src][n] * (amp * std::sin(2 * M_PI * freq * t + phase));
         }
         if (method == 1) {
             // first-order Euler in place: solver.cpp:152-153 (numStep with beta = 1)

@@ -1,0 +1,126 @@
+"""Uneven multi-mesh batches (dg_multi_*): 3D meshes of different sizes,
+orders, media and mean flows stepped by one persistent launch per stage.
+Every mesh must match its own oracle run (FP64: 1e-10 relative L2 per field;
+FP32: 1e-5), whatever tile configuration runs, and the autotuner must leave
+the state as it found it."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import dgcuda as D
+import oracle_py as O
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / nb if nb > 0 else np.linalg.norm(a - b)
+
+
+SPECS = [  # (cells, order, side names, c0, rho0, v0)
+    ((3, 2, 2), 3, ("Absorbing", "Reflecting") * 3, 340.0, 1.225, (60.0, 0.0, 0.0)),
+    ((2, 2, 2), 5, ("Reflecting",) * 6, 300.0, 1.0, (0.0, 0.0, 0.0)),
+    ((4, 3, 2), 1, ("Absorbing",) * 6, 340.0, 1.225, (0.0, -40.0, 20.0)),
+    ((3, 3, 3), 2, ("Reflecting", "Absorbing") * 3, 400.0, 1.4, (10.0, 10.0, 10.0)),
+    ((2, 3, 2), 4, ("Absorbing",) * 6, 340.0, 1.225, (0.0, 0.0, 100.0)),
+]
+
+
+def build(flux="reference"):
+    meshes, pres, phys, dts, u0s, srcs = [], [], [], [], [], []
+    rng = np.random.default_rng(4)
+    for i, (cells, order, names, c0, rho0, v0) in enumerate(SPECS):
+        hi = (1.0, 0.8 + 0.1 * i, 0.6 + 0.05 * i)
+        mesh = D.Mesh.box_tet(*cells, (0.0, 0.0, 0.0), hi, order=order, side_names=names)
+        pre = D.Precomp(mesh)
+        meshes.append(mesh)
+        pres.append(pre)
+        phys.append((c0, rho0, v0))
+        dts.append(D.cfl_dt(pre, c0, v0))
+        c = rng.uniform(0.3, 0.7, 3) * np.array(hi)
+        u0 = pre.initial_state([(0, *c, 0.03, 1.0)])
+        u0[1:] += 1e-3 * rng.standard_normal((3, pre.ndof))
+        u0s.append(u0)
+        xs = rng.uniform(0.3, 0.7, 3) * np.array(hi)
+        srcs.append((i, xs, 0.25, rng.uniform(500.0, 1500.0)))
+    return meshes, pres, phys, np.array(dts), u0s, srcs
+
+
+def oracle_runs(meshes, phys, dts, u0s, srcs, nsteps, flux):
+    out = []
+    for i, mesh in enumerate(meshes):
+        c0, rho0, v0 = phys[i]
+        _, xs, size, freq = srcs[i]
+        src = np.array([[0.0, *xs, size, 1.5, freq, 0.0, 1.0]]) if i % 2 == 0 else None
+        orc = O.Oracle(mesh.raw(), dts[i], c0, rho0, v0=v0, bcs=mesh.bcs(), upwind=(flux == "upwind"), sources=src)
+        orc.set_state(u0s[i])
+        t, _ = orc.run(0.0, nsteps)
+        out.append((t, orc.get_state()))
+    return out
+
+
+def make_solver(pres, phys, u0s, srcs, precision, flux, use_graph=True):
+    ms = D.MultiSolver(pres, phys, precision=precision, flux=flux, use_graph=use_graph)
+    for i, u0 in enumerate(u0s):
+        ms.set_state(i, u0)
+    lst = []
+    for i, xs, size, freq in srcs:
+        if i % 2 == 0:
+            lst.append((i, pres[i].source_dofs(*xs, size), None, 1.5, freq, 0.0, 1.0))
+    ms.set_sources(lst)
+    return ms
+
+
+@pytest.mark.parametrize("precision,flux,tol", [("fp64", "reference", 1e-10), ("fp32", "upwind", 1e-5)])
+def test_every_mesh_matches_its_oracle_run(precision, flux, tol):
+    meshes, pres, phys, dts, u0s, srcs = build()
+    nsteps = 37
+    ms = make_solver(pres, phys, u0s, srcs, precision, flux)
+    t = ms.rk4_steps(np.zeros(len(pres)), dts, nsteps)
+    refs = oracle_runs(meshes, phys, dts, u0s, srcs, nsteps, flux)
+    for i, (tr, ref) in enumerate(refs):
+        assert t[i] == tr
+        got = ms.get_state(i)
+        for q in range(4):
+            assert rel_l2(got[q], ref[q]) <= tol, (i, q, rel_l2(got[q], ref[q]))
+
+
+def test_tile_configurations_agree_and_autotune_restores_state():
+    meshes, pres, phys, dts, u0s, srcs = build()
+    results = []
+    ncfg = None
+    for cfg in range(3):
+        ms = make_solver(pres, phys, u0s, srcs, "fp64", "reference", use_graph=False)
+        ncfg = ms.info()["ncfg"]
+        ms.set_config(cfg)
+        ms.rk4_steps(np.zeros(len(pres)), dts, 9)
+        results.append([ms.get_state(i) for i in range(len(pres))])
+        ms.close()
+    assert ncfg == 3
+    for cfg in (1, 2):
+        for i in range(len(pres)):
+            assert rel_l2(results[cfg][i], results[0][i]) <= 1e-13
+    ms = make_solver(pres, phys, u0s, srcs, "fp32", "upwind")
+    before = [ms.get_state(i) for i in range(len(pres))]
+    chosen, times = ms.autotune(dts, trial_steps=3)
+    assert 0 <= chosen < 3 and len(times) == 3 and all(x > 0 for x in times)
+    assert ms.info()["cfg"] == chosen
+    for i in range(len(pres)):
+        assert np.array_equal(ms.get_state(i), before[i])
+
+
+def test_fp32_multi_equals_single_mesh_contexts():
+    meshes, pres, phys, dts, u0s, srcs = build()
+    ms = make_solver(pres, phys, u0s, srcs, "fp32", "upwind")
+    ms.rk4_steps(np.zeros(len(pres)), dts, 12)
+    for i, pre in enumerate(pres):
+        c0, rho0, v0 = phys[i]
+        s = D.Solver(pre, c0, rho0, v0, precision="fp32", flux="upwind")
+        s.set_state(u0s[i])
+        _, xs, size, freq = srcs[i]
+        if i % 2 == 0:
+            s.set_sources([(pre.source_dofs(*xs, size), 1.5, freq, 0.0, 1.0)])
+        s.rk4_steps(0.0, dts[i], 12)
+        assert rel_l2(ms.get_state(i), s.get_state()) <= 1e-6
