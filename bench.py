@@ -420,7 +420,108 @@ def ours_arm(args, world, rank, local, pg):
         "gpu_launches": 4 * args.steps,
         "monitors": {"energy": e, "nonfinite": bad},
     }
+    if world == 1 and not args.no_batched:
+        line["batched"] = batched_section(D, args, local)
+    if world == 1 and not args.no_uneven:
+        line["uneven_batch"] = uneven_section(D, args, local)
     print(json.dumps(line), flush=True)
+
+
+def batched_section(D, args, local):
+    """Multi-source batch: unit cube 40^3 x 6 tets, order 4, 64 Gaussian
+    sources (one per batch member) and 16 receivers, zero initial state.  The
+    mixed form and the FP64 form each run the whole batch in one launch per
+    stage; accuracy: the first members of the mixed batch against the FP64
+    batch after acc_steps steps (state and receiver traces)."""
+    from dgcuda import workloads as W
+
+    t0 = time.time()
+    mesh, pre, dt, srcs, recs = W.multi_source(n=args.batched_cells, order=4, nsrc=args.batched_sources, seed=SEED)
+    log(f"[bench] batched: {pre.num_el} tets x {args.batched_sources} sources, {pre.ndof} DOF/field, "
+        f"setup {time.time() - t0:.1f}s")
+    zero = np.zeros((4, pre.ndof))
+    units_per_step = pre.ndof * 4 * 4 * args.batched_sources
+    out = {"workload": f"unit cube {args.batched_cells}^3 hexes x 6 tets ({pre.num_el} tets), order 4 (Np=35), "
+                       f"{args.batched_sources} Gaussian sources (sigma 0.03, f in [2,8], positions in [0.1,0.9]^3, "
+                       f"one per batch member), 16 receivers, zero initial state, absorbing walls",
+           "unit": UNIT, "dofs_per_field": pre.ndof, "members": args.batched_sources, "dt": dt}
+    for form, steps in (("mixed", args.batched_steps), ("fp64", max(2, args.batched_steps // 5))):
+        s = D.Solver(pre, C0, RHO0, (0.0, 0.0, 0.0), precision=form, flux=FLUX, device=local,
+                     nbatch=args.batched_sources)
+        s.set_state(zero)
+        s.set_batch_sources(srcs)
+        s.set_receivers(recs, steps + 3)
+        t = s.rk4_steps(0.0, dt, 3)
+        with ClockSampler(local) as clk:
+            t, ms = s.rk4_steps_timed(t, dt, steps)
+        out[form] = {"value": units_per_step * steps / (ms * 1e-3), "steps": steps, "ms_per_step": ms / steps,
+                     "clocks": clk.summary()}
+        s.close()
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    # accuracy on the first members (same sources, same steps)
+    nacc = min(4, args.batched_sources)
+    states, traces = {}, {}
+    for form in ("fp64", "mixed"):
+        s = D.Solver(pre, C0, RHO0, (0.0, 0.0, 0.0), precision=form, flux=FLUX, device=local, nbatch=nacc)
+        s.set_state(zero)
+        s.set_batch_sources([x for x in srcs if x[0] < nacc])
+        s.set_receivers(recs, args.batched_acc_steps)
+        s.rk4_steps(0.0, dt, args.batched_acc_steps)
+        states[form] = [s.get_state(member=m) for m in range(nacc)]
+        traces[form] = s.traces()
+        s.close()
+    err = max(float(np.linalg.norm(states["mixed"][m][q] - states["fp64"][m][q]) /
+                    np.linalg.norm(states["fp64"][m][q])) for m in range(nacc) for q in range(4))
+    terr = float(np.linalg.norm(traces["mixed"] - traces["fp64"]) / np.linalg.norm(traces["fp64"]))
+    out["accuracy"] = {"members": nacc, "steps": args.batched_acc_steps, "state_rel_l2_vs_fp64_max": err,
+                       "receiver_traces_rel_l2_vs_fp64": terr}
+    return out
+
+
+def uneven_section(D, args, local):
+    """Uneven batch: 32 seeded boxes (5k-300k tets, order 2-5, one Gaussian
+    source each, mixed wall types) in FP32, one persistent launch per stage
+    for all meshes; tile configuration chosen by the autotuner; compared with
+    the same meshes stepped one context at a time."""
+    from dgcuda import workloads as W
+
+    t0 = time.time()
+    meshes, pres, phys, dts, srcs = W.uneven(nmesh=args.uneven_meshes, seed=SEED)
+    tets = [p.num_el for p in pres]
+    orders = [p.order for p in pres]
+    log(f"[bench] uneven: {len(pres)} meshes, {sum(tets)} tets, setup {time.time() - t0:.1f}s")
+    units_per_step = sum(p.ndof for p in pres) * 4 * 4
+    ms_ = D.MultiSolver(pres, phys, precision="fp32", flux=FLUX, device=local)
+    for i, p in enumerate(pres):
+        ms_.set_state(i, np.zeros((4, p.ndof)))
+    ms_.set_sources(srcs)
+    chosen, cand = ms_.autotune(dts, trial_steps=5)
+    t = ms_.rk4_steps(np.zeros(len(pres)), dts, 3)
+    with ClockSampler(local) as clk:
+        t, ms = ms_.rk4_steps_timed(t, dts, args.uneven_steps)
+    info = ms_.info()
+    ms_.close()
+    # the same meshes, one single-mesh context each, stepped one after the other
+    nsep = max(3, args.uneven_steps // 10)
+    sep_ms = 0.0
+    for i, p in enumerate(pres):
+        s = D.Solver(p, *phys[i], precision="fp32", flux=FLUX, device=local)
+        s.set_state(np.zeros((4, p.ndof)))
+        s.set_batch_sources([(0, *srcs[i][1:])])
+        tt = s.rk4_steps(0.0, dts[i], 3)
+        _, m1 = s.rk4_steps_timed(tt, dts[i], nsep)
+        sep_ms += m1 / nsep
+        s.close()
+    value = units_per_step * args.uneven_steps / (ms * 1e-3)
+    return {"workload": f"{len(pres)} seeded boxes, side lengths in [0.5,3], h 0.025 coarsened to keep "
+                       f"{min(tets)}-{max(tets)} tets per mesh ({sum(tets)} tets), orders {sorted(set(orders))}, "
+                       "one Gaussian source each, mixed reflecting/absorbing sides, FP32",
+            "unit": UNIT, "value": value, "steps": args.uneven_steps, "ms_per_step": ms / args.uneven_steps,
+            "tile_config": {"chosen_block_threads": info["block_threads"][chosen],
+                            "candidates_ms_per_step": dict(zip(map(str, info["block_threads"]), cand))},
+            "separate_contexts_ms_per_step": sep_ms,
+            "one_launch_over_separate": sep_ms / (ms / args.uneven_steps),
+            "clocks": clk.summary()}
 
 
 def accuracy_all(D, pre, u0, dt, v0, args, local, nq):
@@ -459,6 +560,14 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--form", choices=["mixed", "fp32", "fp64"], default="mixed")
+    ap.add_argument("--no-batched", action="store_true", help="skip the multi-source batch section")
+    ap.add_argument("--batched-cells", type=int, default=NCELL)
+    ap.add_argument("--batched-sources", type=int, default=64)
+    ap.add_argument("--batched-steps", type=int, default=10)
+    ap.add_argument("--batched-acc-steps", type=int, default=100)
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven multi-mesh section")
+    ap.add_argument("--uneven-meshes", type=int, default=32)
+    ap.add_argument("--uneven-steps", type=int, default=500)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least three untimed warm-up steps
     world, rank, local, pg = dist_init()

@@ -54,6 +54,12 @@ struct MixedShape {
     static constexpr int ACC = 4 * ACOLS;           // first accumulator column
     static constexpr int TMEM_COLS = 512;
     static constexpr bool FITS = ACC + 3 * NPAD <= TMEM_COLS;
+    // accumulators: 0 for the slice pairs with i+j = 0, 1 for i+j = 1 (both
+    // exact), NX more for the ten pairs with i+j >= 2 (spread so that the
+    // MMAs of consecutive pairs do not wait on one another)
+    static constexpr int NACC_FIT = (TMEM_COLS - ACC) / NPAD;
+    static constexpr int NACC = NACC_FIT < 9 ? NACC_FIT : 9;
+    static constexpr int NX = NACC - 2;
     static constexpr int BTILE = NPAD * 32;         // bytes of one (slice, K-step) B tile
     static constexpr int BBYTES = 4 * KSTEPS * BTILE;
     static constexpr int QS = NP + 1;               // padded element stride in the state tile
@@ -66,8 +72,9 @@ struct MixedShape {
     static constexpr int OFF_A = r16(OFF_Q + NQ * ELEMS * QS * 4);    // FP32 A rows [128][KSTR]
     static constexpr int OFF_NBR = r16(OFF_A + 128 * KSTR * 4);       // neighbour traces [task][4]
     static constexpr int OFF_GEO = OFF_NBR + ELEMS * NSLOT * 16;      // [le][DIM*DIM] doubles
-    static constexpr int OFF_CONN = r16(OFF_GEO + ELEMS * DIM * DIM * 8);  // [le][NF] int2
-    static constexpr int OFF_FGEO = r16(OFF_CONN + ELEMS * NF * 8);   // [le][NF] float4
+    static constexpr int OFF_CONN = r16(OFF_GEO + ELEMS * DIM * DIM * 8);  // 2 x [le][NF] int2
+    static constexpr int CONN_BYTES = r16(ELEMS * NF * 8);
+    static constexpr int OFF_FGEO = OFF_CONN + 2 * CONN_BYTES;         // [le][NF] float4
     static constexpr int OFF_MAX = OFF_FGEO + ELEMS * NF * 16;
     static constexpr int OFF_TAB = OFF_MAX + MAX_WG * 128 * 4;
     static constexpr int OFF_EB = r16(OFF_TAB + S::NTAB);
@@ -124,8 +131,21 @@ __device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
+// Issues the cp.async copies of a tile's connectivity words into buffer cb.
+template <int DIM, int P, int NT>
+__device__ __forceinline__ void issue_conn_copies(const MixedArgs &a, unsigned char *smem, long long ebase, int cb,
+                                                  int tid) {
+    using MS = MixedShape<DIM, P>;
+    constexpr int NF = MS::NF, ELEMS = MS::ELEMS;
+    int2 *sConn = reinterpret_cast<int2 *>(smem + MS::OFF_CONN + cb * MS::CONN_BYTES);
+    for (int idx = tid; idx < ELEMS * NF; idx += NT) {
+        const bool ok = ebase + idx / NF < a.K;
+        dgtc::cp_async8(&sConn[idx], ok ? &a.conn[ebase * NF + idx] : a.conn, ok ? 8u : 0u);
+    }
+}
+
 // Issues the cp.async copies of a tile's element data: state, inverse
-// Jacobians, connectivity words and face geometry (zero-filled past K).
+// Jacobians and face geometry (zero-filled past K).
 template <int DIM, int P, int NT>
 __device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned char *smem, long long ebase,
                                                   long long moff, int tid) {
@@ -133,7 +153,6 @@ __device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned c
     constexpr int NP = MS::NP, NF = MS::NF, NQ = MS::NQ, ELEMS = MS::ELEMS, QS = MS::QS;
     float *sQ = reinterpret_cast<float *>(smem + MS::OFF_Q);
     double *sGeo = reinterpret_cast<double *>(smem + MS::OFF_GEO);
-    int2 *sConn = reinterpret_cast<int2 *>(smem + MS::OFF_CONN);
     float4 *sFgeo = reinterpret_cast<float4 *>(smem + MS::OFF_FGEO);
     for (int idx = tid; idx < NQ * ELEMS * NP; idx += NT) {
         const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
@@ -148,21 +167,20 @@ __device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned c
     }
     for (int idx = tid; idx < ELEMS * NF; idx += NT) {
         const bool ok = ebase + idx / NF < a.K;
-        dgtc::cp_async8(&sConn[idx], ok ? &a.conn[ebase * NF + idx] : a.conn, ok ? 8u : 0u);
         dgtc::cp_async16(&sFgeo[idx], ok ? &a.fgeo[(ebase * NF + idx) * 4] : a.fgeo, ok ? 16u : 0u);
     }
 }
 
 // Issues the cp.async gathers of the neighbour traces of a tile's interior
-// face slots (reads the tile's connectivity words from shared memory); the
+// face slots (reads the tile's connectivity words from buffer cb); the
 // calling threads take tasks first, first + stride, ...
 template <int DIM, int P>
 __device__ __forceinline__ void issue_neighbour_copies(const MixedArgs &a, unsigned char *smem, long long ebase,
-                                                       long long moff, int first, int stride) {
+                                                       long long moff, int cb, int first, int stride) {
     using MS = MixedShape<DIM, P>;
     constexpr int NP = MS::NP, NF = MS::NF, NFP = MS::NFP, NQ = MS::NQ, NSLOT = MS::NSLOT, ELEMS = MS::ELEMS;
     float *sNbr = reinterpret_cast<float *>(smem + MS::OFF_NBR);
-    const int2 *sConn = reinterpret_cast<const int2 *>(smem + MS::OFF_CONN);
+    const int2 *sConn = reinterpret_cast<const int2 *>(smem + MS::OFF_CONN + cb * MS::CONN_BYTES);
     const uint8_t *sFmask = smem + MS::OFF_TAB;
     const uint8_t *sPerm = sFmask + NF * NFP;
     for (int task = first; task < ELEMS * NSLOT; task += stride) {
@@ -190,14 +208,15 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     constexpr int NCH = (NPP + 7) / 8;                  // 8-column tensor-memory loads per accumulator
     static_assert(MS::FITS, "tile does not fit in tensor memory");
     static_assert(NWG >= 1 && NWG <= MS::MAX_WG, "warp groups");
-    static_assert(MS::ACC + 2 * NPAD + (NWG - 1) * NPP + 8 * NCH <= MS::TMEM_COLS,
+    constexpr int NX = MS::NX;
+    static_assert(NX >= 1, "at least three accumulators");
+    static_assert(MS::ACC + (MS::NACC - 1) * NPAD + (NWG - 1) * NPP + 8 * NCH <= MS::TMEM_COLS,
                   "epilogue loads stay inside the allocation");
     extern __shared__ __align__(1024) unsigned char smem[];
     const float *sQ = reinterpret_cast<const float *>(smem + MS::OFF_Q);
     float *sA = reinterpret_cast<float *>(smem + MS::OFF_A);
     const float4 *sNbr = reinterpret_cast<const float4 *>(smem + MS::OFF_NBR);
     const double *sGeo = reinterpret_cast<const double *>(smem + MS::OFF_GEO);
-    const int2 *sConn = reinterpret_cast<const int2 *>(smem + MS::OFF_CONN);
     const float4 *sFgeo = reinterpret_cast<const float4 *>(smem + MS::OFF_FGEO);
     float *sMax = reinterpret_cast<float *>(smem + MS::OFF_MAX);
     uint8_t *sTab = smem + MS::OFF_TAB;
@@ -239,11 +258,12 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     bool alive = true;
     uint32_t phase = 0;
 
-    // Software pipeline over the CTA's tiles: the element data of tile t+1
-    // are copied while tile t is sliced, and its neighbour traces while tile
-    // t's contraction and epilogue run.  Tile T covers element block T / nbatch
-    // of batch member T % nbatch (members of one block are adjacent, so the
-    // block's geometry is reused from L2).
+    // Software pipeline over the CTA's tiles (cp.async groups): tile t+1's
+    // connectivity words are copied while tile t's fluxes are built, its state,
+    // geometry and neighbour traces while tile t is sliced, contracted and
+    // written back.  Tile T covers element block T / nbatch of batch member
+    // T % nbatch (members of one block are adjacent, so the block's geometry
+    // is reused from L2).
     const long long ntiles = (long long)((a.K + ELEMS - 1) / ELEMS) * a.nbatch;
     auto tile_base = [&](long long T, long long &eb, long long &mo) {
         const long long et = T / a.nbatch;
@@ -253,19 +273,25 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     if ((long long)blockIdx.x < ntiles) {
         long long eb, mo;
         tile_base(blockIdx.x, eb, mo);
+        issue_conn_copies<DIM, P, NT>(a, smem, eb, 0, tid);
         issue_tile_copies<DIM, P, NT>(a, smem, eb, mo, tid);
         dgtc::cp_async_wait_all();
         __syncthreads();
-        issue_neighbour_copies<DIM, P>(a, smem, eb, mo, tid, NT);
+        issue_neighbour_copies<DIM, P>(a, smem, eb, mo, 0, tid, NT);
+        dgtc::cp_async_commit();
     }
-    for (long long tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x) {
+    int cb = 0;  // connectivity buffer of the current tile
+    for (long long tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x, cb ^= 1) {
         long long ebase, moff;
         tile_base(tile, ebase, moff);
         const long long next = tile + gridDim.x;
         long long nebase = 0, nmoff = 0;
         if (next < ntiles) tile_base(next, nebase, nmoff);
+        const int2 *sConn = reinterpret_cast<const int2 *>(smem + MS::OFF_CONN + cb * MS::CONN_BYTES);
         dgtc::cp_async_wait_all();
         __syncthreads();
+        if (next < ntiles) issue_conn_copies<DIM, P, NT>(a, smem, nebase, cb ^ 1, tid);
+        dgtc::cp_async_commit();
         // 2a. contravariant fluxes, one task per element node
         for (int task = tid; task < ELEMS * NP; task += NT) {
             const int le = task / NP, j = task - le * NP;
@@ -359,6 +385,11 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
         __syncthreads();
         // the tile's element data are consumed: start copying the next tile's
         if (next < ntiles) issue_tile_copies<DIM, P, NT>(a, smem, nebase, nmoff, tid);
+        dgtc::cp_async_commit();
+        // this thread's connectivity copies of the next tile are complete (only
+        // the group just committed may still be pending); the barrier after
+        // the row maxima makes every thread's copies visible
+        dgtc::cp_async_wait_group<1>();
 
         // 3. slices of the A rows into tensor memory; warp group g takes
         //    K-steps [g*KSP, (g+1)*KSP) of rows 0..127
@@ -374,9 +405,9 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
         for (int t = 0; t < NPP; ++t) {
             pu[t] = pl[t] = pa[t] = 0.0f;
             if (row_ok && i0 + t < NP) {
-                pu[t] = a.u[rbase + i0 + t];
-                pl[t] = a.ulo[rbase + i0 + t];
-                if (STAGE > 1 && STAGE < kStageEuler) pa[t] = a.acc[rbase + i0 + t];
+                pu[t] = dgtc::ld_early(a.u + rbase + i0 + t);
+                pl[t] = dgtc::ld_early(a.ulo + rbase + i0 + t);
+                if (STAGE > 1 && STAGE < kStageEuler) pa[t] = dgtc::ld_early(a.acc + rbase + i0 + t);
             }
         }
         const float *arow = &sA[r * KSTR];
@@ -387,6 +418,8 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             sMax[part * 128 + r] = m;
         }
         __syncthreads();
+        if (next < ntiles) issue_neighbour_copies<DIM, P>(a, smem, nebase, nmoff, cb ^ 1, tid, NT);
+        dgtc::cp_async_commit();
         float rmax = sMax[r];
 #pragma unroll
         for (int g = 1; g < NWG; ++g) rmax = fmaxf(rmax, sMax[g * 128 + r]);
@@ -416,31 +449,29 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
         }
         dgtc::tmem_st_wait();
         dgtc::fence_before_sync();
-        // the next tile's element data have landed once every thread's copies are done
-        dgtc::cp_async_wait_all();
         __syncthreads();
 
-        // 4. tensor-core contraction: 13 slice pairs x KSTEPS, issued by thread
-        //    0 while warps 1.. start gathering the next tile's neighbour traces
+        // 4. tensor-core contraction: 13 slice pairs x KSTEPS, issued by thread 0
+        //    K-step by K-step, so that consecutive MMAs (different pairs) mostly
+        //    accumulate into different accumulators
         if (tid == 0) {
             dgtc::fence_after_sync();
-            unsigned started = 0;  // bit per accumulator slot
+            unsigned started = 0;  // bit per accumulator
 #pragma unroll 1
-            for (int pi = 0; pi < 13; ++pi) {
-                const int ia = kPairA[pi], jb = kPairB[pi];
-                const int slot = (ia + jb) < 2 ? (ia + jb) : 2;
-                const uint32_t d = tbase + MS::ACC + slot * NPAD;
-#pragma unroll 1
-                for (int t = 0; t < KSTEPS; ++t) {
+            for (int t = 0; t < KSTEPS; ++t) {
+#pragma unroll
+                for (int pi = 0; pi < 13; ++pi) {
+                    const int ia = kPairA[pi], jb = kPairB[pi];
+                    const int slot = pi == 0 ? 0 : pi < 3 ? 1 : 2 + (pi - 3) % NX;
                     const uint64_t bd = dgtc::desc_kmajor(sB + (jb * KSTEPS + t) * MS::BTILE, 128, 256);
-                    dgtc::mma_bf16_ts(d, tbase + ia * ACOLS + t * 8, bd, idesc, (started >> slot) & 1u);
+                    dgtc::mma_bf16_ts(tbase + MS::ACC + slot * NPAD, tbase + ia * ACOLS + t * 8, bd, idesc,
+                                      (started >> slot) & 1u);
                     started |= 1u << slot;
                 }
             }
             dgtc::mma_commit(bar);
         }
         __syncwarp();
-        if (warp > 0 && next < ntiles) issue_neighbour_copies<DIM, P>(a, smem, nebase, nmoff, tid - 32, NT - 32);
 
         // 5. epilogue: accumulators -> stage increment, RK4 stage update;
         //    warp group g takes output nodes [g*NPP, (g+1)*NPP)
@@ -451,14 +482,33 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             alive = false;
         } else {
             dgtc::fence_after_sync();
-            uint32_t v0[8 * NCH], v1[8 * NCH], v2[8 * NCH];
+            uint32_t v0[8 * NCH], v1[8 * NCH];
+            float v2[8 * NCH];  // sum of the accumulators of the pairs with i+j >= 2
 #pragma unroll
             for (int c = 0; c < NCH; ++c) {
                 dgtc::tmem_ld8(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 0 * NPAD + i0 + 8 * c), v0 + 8 * c);
                 dgtc::tmem_ld8(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 1 * NPAD + i0 + 8 * c), v1 + 8 * c);
-                dgtc::tmem_ld8(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 2 * NPAD + i0 + 8 * c), v2 + 8 * c);
             }
-            dgtc::tmem_ld_wait();
+#pragma unroll
+            for (int k = 0; k < 8 * NCH; ++k) v2[k] = 0.0f;
+            // the extra accumulators, four at a time
+#pragma unroll
+            for (int x0 = 0; x0 < NX; x0 += 4) {
+                uint32_t vx[4][8 * NCH];
+#pragma unroll
+                for (int x = 0; x < 4; ++x)
+                    if (x0 + x < NX)
+#pragma unroll
+                        for (int c = 0; c < NCH; ++c)
+                            dgtc::tmem_ld8(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + (2 + x0 + x) * NPAD + i0 + 8 * c),
+                                           vx[x] + 8 * c);
+                dgtc::tmem_ld_wait();
+#pragma unroll
+                for (int x = 0; x < 4; ++x)
+                    if (x0 + x < NX)
+#pragma unroll
+                        for (int k = 0; k < 8 * NCH; ++k) v2[k] += __uint_as_float(vx[x][k]);
+            }
             if (row_ok) {
                 const float sdt = live ? a.dt * exp2i(ea - 16) : 0.0f;
 #pragma unroll
@@ -467,7 +517,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
                     if (i >= NP) break;
                     float hi, lo;
                     two_sum(__uint_as_float(v0[t]), __uint_as_float(v1[t]), hi, lo);
-                    lo += __uint_as_float(v2[t]);
+                    lo += v2[t];
                     const float scl = sdt * exp2i(sEb[i]);
                     const float rr = fmaf(scl, hi, scl * lo);
                     const long long idx = rbase + i;

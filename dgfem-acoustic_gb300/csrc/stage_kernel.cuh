@@ -110,17 +110,20 @@ __device__ __forceinline__ void stage_tile(const StageArgs<Real> &a, long long b
     const Real *sL = sOps + DIM * NP * NP;
     const uint8_t *sFmask = sTab;
     const uint8_t *sPerm = sTab + NF * NFP;
-    const int le = tid / NP;
-    const int i = tid - le * NP;
+    // threads past EPB*NP (a CTA larger than the tile) work on element 0,
+    // node 0 but never write shared or global memory
+    const bool active = tid < NT;
+    const int le = active ? tid / NP : 0;
+    const int i = active ? tid - le * NP : 0;
     const Real *win = a.win + boff;
     const int e = tile * EPB + le;
-    const bool valid = (tid < NT) && (e < a.K);
+    const bool valid = active && (e < a.K);
     const long long base = (long long)e * NP + i;
     Real q[NQ];
 #pragma unroll
     for (int f = 0; f < NQ; ++f) {
         q[f] = valid ? win[f * a.fstride + base] : Real(0);
-        sQ[(le * NP + i) * 4 + f] = q[f];
+        if (active) sQ[(le * NP + i) * 4 + f] = q[f];
     }
     __syncthreads();
 
@@ -177,7 +180,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<Real> &a, long long b
     }
 
     // Face values at the element's face nodes.
-    for (int s = i; s < NSLOT; s += NP) {
+    for (int s = active ? i : NSLOT; s < NSLOT; s += NP) {
         const int lf = s / NFP;
         const int k = s - lf * NFP;
         const int vi = sFmask[lf * NFP + k];

@@ -158,6 +158,21 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src, uint32_t 
 }
 // Waits for all cp.async copies of the calling thread.
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// Closes the calling thread's current group of cp.async copies.
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Waits until at most N of the calling thread's committed groups are pending.
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// A global load kept at its place in the program (the compiler does not sink
+// it towards its first use), so that its latency overlaps the work after it.
+__device__ __forceinline__ float ld_early(const float *p) {
+    float v;
+    asm volatile("ld.global.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
 
 // Two BF16 values (exactly representable) packed low = first, high = second.
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
