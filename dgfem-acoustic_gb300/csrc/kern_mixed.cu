@@ -18,7 +18,7 @@ namespace {
 template <int DIM, int P>
 void b_image(const double *ops, std::vector<uint8_t> &img, std::vector<int> &eb) {
     using MS = MixedShape<DIM, P>;
-    constexpr int NP = MS::NP, KTOT = MS::KTOT, KSTEPS = MS::KSTEPS, NPAD = MS::NPAD;
+    constexpr int NP = MS::NP, KTOT = MS::KTOT, NPAD = MS::NPAD;
     const double *D = ops;                      // [u][j][i]
     const double *L = ops + DIM * NP * NP;      // [slot][i]
     img.assign(MS::BBYTES, 0);
@@ -49,7 +49,9 @@ void b_image(const double *ops, std::vector<uint8_t> &img, std::vector<int> &eb)
                 uint32_t bits;
                 std::memcpy(&bits, &val, 4);
                 uint16_t h = (uint16_t)(bits >> 16);
-                size_t off = (size_t)(sl * KSTEPS + k / 16) * MS::BTILE + (i / 8) * 256 + ((k % 16) / 8) * 128 +
+                // per K-step the four slices follow one another along N, so
+                // that one MMA can take several slices as one wider operand
+                size_t off = (size_t)((k / 16) * 4 + sl) * MS::BTILE + (i / 8) * 256 + ((k % 16) / 8) * 128 +
                              (i % 8) * 16 + (k % 8) * 2;
                 std::memcpy(&img[off], &h, 2);
             }

@@ -54,13 +54,19 @@ struct MixedShape {
     static constexpr int ACC = 4 * ACOLS;           // first accumulator column
     static constexpr int TMEM_COLS = 512;
     static constexpr bool FITS = ACC + 3 * NPAD <= TMEM_COLS;
-    // accumulators: 0 for the slice pairs with i+j = 0, 1 for i+j = 1 (both
-    // exact), NX more for the ten pairs with i+j >= 2 (spread so that the
-    // MMAs of consecutive pairs do not wait on one another)
+    // Level scheme (where it fits): one accumulator per level L = i+j of the
+    // slice pairs (0..4).  The B slices of a K-step lie side by side along N,
+    // so A slice i meets B slices 0..min(3, 4-i) in one MMA of N = that many
+    // x NPAD, accumulating into levels i..: four MMAs per K-step.
+    static constexpr bool LEVELS = ACC + 5 * NPAD <= TMEM_COLS && 4 * NPAD <= 256;
+    // Pair scheme (otherwise): one MMA per slice pair; accumulator 0 for
+    // i+j = 0, 1 for i+j = 1 (both exact), NX more for the ten pairs with
+    // i+j >= 2 (spread so that the MMAs of consecutive pairs do not wait on
+    // one another)
     static constexpr int NACC_FIT = (TMEM_COLS - ACC) / NPAD;
-    static constexpr int NACC = NACC_FIT < 9 ? NACC_FIT : 9;
+    static constexpr int NACC = LEVELS ? 5 : NACC_FIT < 9 ? NACC_FIT : 9;
     static constexpr int NX = NACC - 2;
-    static constexpr int BTILE = NPAD * 32;         // bytes of one (slice, K-step) B tile
+    static constexpr int BTILE = NPAD * 32;         // bytes of one (K-step, slice) B tile; image [K-step][slice]
     static constexpr int BBYTES = 4 * KSTEPS * BTILE;
     static constexpr int QS = NP + 1;               // padded element stride in the state tile
     static constexpr int KSTR = KPAD + 1;           // padded row stride of the staged A rows (odd)
@@ -447,6 +453,14 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             for (int sl = 0; sl < 4; ++sl)
                 dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, sl * ACOLS + c * 8), w[sl]);
         }
+        if constexpr (MS::LEVELS) {
+            // level 4 only receives accumulating MMAs: clear this part's columns
+            uint32_t z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            __syncwarp();
+#pragma unroll
+            for (int c = 0; c < NCH; ++c)
+                dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 4 * NPAD + i0 + 8 * c), z);
+        }
         dgtc::tmem_st_wait();
         dgtc::fence_before_sync();
         __syncthreads();
@@ -456,17 +470,32 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
         //    accumulate into different accumulators
         if (tid == 0) {
             dgtc::fence_after_sync();
-            unsigned started = 0;  // bit per accumulator
+            if constexpr (MS::LEVELS) {
+                // level 4 was zeroed while slicing; A slice 0 at K-step 0
+                // starts levels 0..3
 #pragma unroll 1
-            for (int t = 0; t < KSTEPS; ++t) {
+                for (int t = 0; t < KSTEPS; ++t) {
+                    const uint64_t bd = dgtc::desc_kmajor(sB + t * 4 * MS::BTILE, 128, 256);
 #pragma unroll
-                for (int pi = 0; pi < 13; ++pi) {
-                    const int ia = kPairA[pi], jb = kPairB[pi];
-                    const int slot = pi == 0 ? 0 : pi < 3 ? 1 : 2 + (pi - 3) % NX;
-                    const uint64_t bd = dgtc::desc_kmajor(sB + (jb * KSTEPS + t) * MS::BTILE, 128, 256);
-                    dgtc::mma_bf16_ts(tbase + MS::ACC + slot * NPAD, tbase + ia * ACOLS + t * 8, bd, idesc,
-                                      (started >> slot) & 1u);
-                    started |= 1u << slot;
+                    for (int ia = 0; ia < 4; ++ia) {
+                        const int nj = ia < 2 ? 4 : 5 - ia;
+                        dgtc::mma_bf16_ts(tbase + MS::ACC + ia * NPAD, tbase + ia * ACOLS + t * 8, bd,
+                                          dgtc::idesc_bf16_f32(128, nj * NPAD), (t > 0 || ia > 0) ? 1u : 0u);
+                    }
+                }
+            } else {
+                unsigned started = 0;  // bit per accumulator
+#pragma unroll 1
+                for (int t = 0; t < KSTEPS; ++t) {
+#pragma unroll
+                    for (int pi = 0; pi < 13; ++pi) {
+                        const int ia = kPairA[pi], jb = kPairB[pi];
+                        const int slot = pi == 0 ? 0 : pi < 3 ? 1 : 2 + (pi - 3) % NX;
+                        const uint64_t bd = dgtc::desc_kmajor(sB + (t * 4 + jb) * MS::BTILE, 128, 256);
+                        dgtc::mma_bf16_ts(tbase + MS::ACC + slot * NPAD, tbase + ia * ACOLS + t * 8, bd, idesc,
+                                          (started >> slot) & 1u);
+                        started |= 1u << slot;
+                    }
                 }
             }
             dgtc::mma_commit(bar);
