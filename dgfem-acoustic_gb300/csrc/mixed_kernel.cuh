@@ -68,7 +68,7 @@ struct MixedShape {
     static constexpr int NX = NACC - 2;
     static constexpr int BTILE = NPAD * 32;         // bytes of one (K-step, slice) B tile; image [K-step][slice]
     static constexpr int BBYTES = 4 * KSTEPS * BTILE;
-    static constexpr int QS = NP + 1;               // padded element stride in the state tile
+    static constexpr int QS = NP;                   // element stride in the state tile
     static constexpr int KSTR = KPAD + 1;           // padded row stride of the staged A rows (odd)
     static constexpr int MAX_WG = 4;                // warp groups per CTA (4 warps each), at most
     // shared memory layout (bytes)
@@ -86,6 +86,8 @@ struct MixedShape {
     static constexpr int OFF_EB = r16(OFF_TAB + S::NTAB);
     static constexpr int OFF_BAR = OFF_EB + NPAD * 4;
     static constexpr int SMEM = OFF_BAR + 16;
+    // the epilogue stages the tile's two output arrays in the A-row region
+    static_assert(2 * NQ * ELEMS * NP <= 128 * KSTR, "output staging fits in the A-row region");
     static_assert(SMEM <= 227 * 1024, "tile does not fit in shared memory");
     // at least half of the SM's shared memory, so one CTA (the tensor-memory
     // owner) runs per SM
@@ -154,18 +156,27 @@ __device__ __forceinline__ void issue_conn_copies(const MixedArgs &a, unsigned c
 // Jacobians and face geometry (zero-filled past K).
 template <int DIM, int P, int NT>
 __device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned char *smem, long long ebase,
-                                                  long long moff, int tid) {
+                                                  long long moff, bool vec, int tid) {
     using MS = MixedShape<DIM, P>;
     constexpr int NP = MS::NP, NF = MS::NF, NQ = MS::NQ, ELEMS = MS::ELEMS, QS = MS::QS;
+    static_assert(QS == NP, "the state tile is stored unpadded, as in global memory");
     float *sQ = reinterpret_cast<float *>(smem + MS::OFF_Q);
     double *sGeo = reinterpret_cast<double *>(smem + MS::OFF_GEO);
     float4 *sFgeo = reinterpret_cast<float4 *>(smem + MS::OFF_FGEO);
-    for (int idx = tid; idx < NQ * ELEMS * NP; idx += NT) {
-        const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
-        const int le = rem / NP, j = rem - le * NP;
-        const bool ok = ebase + le < a.K;
-        const float *src = ok ? &a.win[moff + f * a.fstride + ebase * NP + rem] : a.win;
-        dgtc::cp_async4(&sQ[(f * ELEMS + le) * QS + j], src, ok ? 4u : 0u);
+    if (vec && ebase + ELEMS <= a.K) {
+        // a whole tile of 16-byte aligned fields: 16-byte copies
+        constexpr int W = ELEMS * NP / 4;
+        for (int idx = tid; idx < NQ * W; idx += NT) {
+            const int f = idx / W, w = idx - f * W;
+            dgtc::cp_async16(&sQ[f * ELEMS * NP + 4 * w], &a.win[moff + f * a.fstride + ebase * NP + 4 * w], 16u);
+        }
+    } else {
+        for (int idx = tid; idx < NQ * ELEMS * NP; idx += NT) {
+            const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
+            const bool ok = ebase + rem / NP < a.K;
+            const float *src = ok ? &a.win[moff + f * a.fstride + ebase * NP + rem] : a.win;
+            dgtc::cp_async4(&sQ[f * ELEMS * NP + rem], src, ok ? 4u : 0u);
+        }
     }
     for (int idx = tid; idx < ELEMS * DIM * DIM; idx += NT) {
         const bool ok = ebase + idx / (DIM * DIM) < a.K;
@@ -260,6 +271,10 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     // (K-steps when slicing, output nodes in the epilogue) its warp group takes
     const int r = (warp & 3) * 32 + lane;
     const int part = warp >> 2;
+    // whole tiles move as 16-byte vectors when every field starts on 16 bytes
+    float *const out_lo = STAGE <= 3 ? a.acc : STAGE == kStageEuler ? a.wlo : a.ulo;
+    const bool vec = (a.fstride % 4 == 0) && (a.bstride % 4 == 0) && ((ELEMS * NP) % 4 == 0) &&
+                     (((uintptr_t)a.win | (uintptr_t)a.wout | (uintptr_t)out_lo) % 16 == 0);
     const int rf = r / ELEMS, rle = r - rf * ELEMS;
     bool alive = true;
     uint32_t phase = 0;
@@ -280,7 +295,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
         long long eb, mo;
         tile_base(blockIdx.x, eb, mo);
         issue_conn_copies<DIM, P, NT>(a, smem, eb, 0, tid);
-        issue_tile_copies<DIM, P, NT>(a, smem, eb, mo, tid);
+        issue_tile_copies<DIM, P, NT>(a, smem, eb, mo, vec, tid);
         dgtc::cp_async_wait_all();
         __syncthreads();
         issue_neighbour_copies<DIM, P>(a, smem, eb, mo, 0, tid, NT);
@@ -390,7 +405,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
         }
         __syncthreads();
         // the tile's element data are consumed: start copying the next tile's
-        if (next < ntiles) issue_tile_copies<DIM, P, NT>(a, smem, nebase, nmoff, tid);
+        if (next < ntiles) issue_tile_copies<DIM, P, NT>(a, smem, nebase, nmoff, vec, tid);
         dgtc::cp_async_commit();
         // this thread's connectivity copies of the next tile are complete (only
         // the group just committed may still be pending); the barrier after
@@ -538,6 +553,10 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
 #pragma unroll
                         for (int k = 0; k < 8 * NCH; ++k) v2[k] += __uint_as_float(vx[x][k]);
             }
+            // outputs go through shared memory (the A-row region, free since
+            // the slicing) so that the global stores are whole-tile vectors
+            float *sO0 = sA;                      // acc, or the new low part
+            float *sO1 = sA + NQ * ELEMS * NP;    // next stage input / new state
             if (row_ok) {
                 const float sdt = live ? a.dt * exp2i(ea - 16) : 0.0f;
 #pragma unroll
@@ -549,32 +568,43 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
                     lo += v2[t];
                     const float scl = sdt * exp2i(sEb[i]);
                     const float rr = fmaf(scl, hi, scl * lo);
-                    const long long idx = rbase + i;
+                    const int o = r * NP + i;  // row r = (field, element) of the tile
                     if (STAGE == 1) {
-                        a.acc[idx] = rr;
-                        a.wout[idx] = pu[t] + (pl[t] + 0.5f * rr);
+                        sO0[o] = rr;
+                        sO1[o] = pu[t] + (pl[t] + 0.5f * rr);
                     } else if (STAGE == 2) {
-                        a.acc[idx] = fmaf(2.0f, rr, pa[t]);
-                        a.wout[idx] = pu[t] + (pl[t] + 0.5f * rr);
+                        sO0[o] = fmaf(2.0f, rr, pa[t]);
+                        sO1[o] = pu[t] + (pl[t] + 0.5f * rr);
                     } else if (STAGE == 3) {
-                        a.acc[idx] = fmaf(2.0f, rr, pa[t]);
-                        a.wout[idx] = pu[t] + (pl[t] + rr);
-                    } else if (STAGE == kStageEuler) {
-                        float s, e;
-                        two_sum(pu[t], rr, s, e);
-                        e += pl[t];
-                        const float nh = s + e;
-                        a.wout[idx] = nh;
-                        a.wlo[idx] = e - (nh - s);
+                        sO0[o] = fmaf(2.0f, rr, pa[t]);
+                        sO1[o] = pu[t] + (pl[t] + rr);
                     } else {
-                        const float dlt = (pa[t] + rr) * (1.0f / 6.0f);
+                        const float dlt = STAGE == kStageEuler ? rr : (pa[t] + rr) * (1.0f / 6.0f);
                         float s, e;
                         two_sum(pu[t], dlt, s, e);
                         e += pl[t];
                         const float nh = s + e;
-                        a.wout[idx] = nh;
-                        a.ulo[idx] = e - (nh - s);
+                        sO1[o] = nh;
+                        sO0[o] = e - (nh - s);
                     }
+                }
+            }
+            __syncthreads();
+            if (vec && ebase + ELEMS <= a.K) {
+                constexpr int W = ELEMS * NP / 4;
+                for (int idx = tid; idx < NQ * W; idx += NT) {
+                    const int f = idx / W, w = idx - f * W;
+                    const long long g = moff + f * a.fstride + ebase * NP + 4 * w;
+                    *reinterpret_cast<float4 *>(&out_lo[g]) = *reinterpret_cast<const float4 *>(&sO0[f * ELEMS * NP + 4 * w]);
+                    *reinterpret_cast<float4 *>(&a.wout[g]) = *reinterpret_cast<const float4 *>(&sO1[f * ELEMS * NP + 4 * w]);
+                }
+            } else {
+                for (int idx = tid; idx < NQ * ELEMS * NP; idx += NT) {
+                    const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
+                    if (ebase + rem / NP >= a.K) continue;
+                    const long long g = moff + f * a.fstride + ebase * NP + rem;
+                    out_lo[g] = sO0[idx];
+                    a.wout[g] = sO1[idx];
                 }
             }
         }
