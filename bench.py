@@ -201,16 +201,17 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ byte model
-def stage_bytes(pre, real_bytes: int, pair_state: bool = False) -> list[float]:
+def stage_bytes(pre, real_bytes: int, pair_state: bool = False, geo_bytes: int = 8) -> list[float]:
     """Algorithmic HBM bytes of each fused stage launch (unique bytes: state
     reads/writes, geometry once; neighbour traces are L2 re-reads).
     Stage 1 reads u, writes acc and w; stages 2-3 read w, u, acc and write
     acc, w; stage 4 reads w, u, acc and writes u.  With the state kept as an
     FP32 pair (mixed form) every read of u also reads its low part and stage 4
-    writes both."""
+    writes both.  geo_bytes: size of an inverse-Jacobian entry (FP64, or FP32
+    in the mixed form)."""
     nq = pre.dim + 1
     n = pre.ndof * nq
-    geo = pre.num_el * (pre.dim * pre.dim * 8 + pre.nf * 4 * real_bytes + pre.nf * 8)
+    geo = pre.num_el * (pre.dim * pre.dim * geo_bytes + pre.nf * 4 * real_bytes + pre.nf * 8)
     words = (4, 6, 6, 6) if pair_state else (3, 5, 5, 4)
     return [n * real_bytes * k + geo for k in words]
 
@@ -297,7 +298,7 @@ FORMS = {
 def roofline_for(sol, pre, form, t, dt, nprof):
     _, prof = sol.profile_steps(t, dt, nprof)
     real = 8 if form == "fp64" else 4
-    sb = stage_bytes(pre, real, pair_state=(form == "mixed"))
+    sb = stage_bytes(pre, real, pair_state=(form == "mixed"), geo_bytes=4 if form == "mixed" else 8)
     avg_ms = [prof["stage_ms"][s] / max(prof["stage_launches"][s], 1) for s in range(4)]
     achieved = sum(sb) / (sum(avg_ms) * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()

@@ -57,7 +57,7 @@ struct MixedArgs {
     long long fstride;
     long long bstride;     // distance between batch members
     int nbatch;            // batch members (sources) on the mesh
-    const double *geo;     // [K][DIM*DIM]
+    const float *geo;      // [K][DIM*DIM] inverse Jacobians rounded to FP32
     const float *fgeo;     // [K][NF][4]
     const int2 *conn;      // [K][NF]
     const uint8_t *bimg;   // B slices, shared-memory image

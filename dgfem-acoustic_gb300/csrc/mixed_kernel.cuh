@@ -77,8 +77,8 @@ struct MixedShape {
     static constexpr int OFF_Q = OFF_B + BBYTES;                      // state tile [f][le][QS]
     static constexpr int OFF_A = r16(OFF_Q + NQ * ELEMS * QS * 4);    // FP32 A rows [128][KSTR]
     static constexpr int OFF_NBR = r16(OFF_A + 128 * KSTR * 4);       // neighbour traces [task][4]
-    static constexpr int OFF_GEO = OFF_NBR + ELEMS * NSLOT * 16;      // [le][DIM*DIM] doubles
-    static constexpr int OFF_CONN = r16(OFF_GEO + ELEMS * DIM * DIM * 8);  // 2 x [le][NF] int2
+    static constexpr int OFF_GEO = OFF_NBR + ELEMS * NSLOT * 16;      // [le][DIM*DIM] floats
+    static constexpr int OFF_CONN = r16(OFF_GEO + ELEMS * DIM * DIM * 4);  // 2 x [le][NF] int2
     static constexpr int CONN_BYTES = r16(ELEMS * NF * 8);
     static constexpr int OFF_FGEO = OFF_CONN + 2 * CONN_BYTES;         // [le][NF] float4
     static constexpr int OFF_MAX = OFF_FGEO + ELEMS * NF * 16;
@@ -118,25 +118,27 @@ __device__ __forceinline__ int row_exponent(float amax) {
 // 2^k as a float for -126 <= k <= 127.
 __device__ __forceinline__ float exp2i(int k) { return __uint_as_float((unsigned)(k + 127) << 23); }
 
-// Four BF16 fixed-point slices of x*scale (|x*scale| < 256): m0 + m1 2^-8 +
-// m2 2^-16 + m3 2^-24, each m an integer of at most 8 significant bits.
+// Four BF16 fixed-point slices of y = x*scale (|y| < 256): s0 + s1 + s2 + s3
+// with s_k a multiple of 2^-8k and |s_k| <= 256 * 2^-8k (at most 8
+// significant bits, so exact in BF16).  Rounding to a multiple of 2^-8k is
+// done by adding and subtracting 1.5 * 2^(23-8k) (round to nearest even, as
+// rintf of the scaled value; full-rate additions instead of conversions);
+// each remainder y - s_k is exact.
 __device__ __forceinline__ void slice4(float x, float scale, float (&m)[4]) {
-    float y = x * scale;
-    m[0] = rintf(y);
-    y = (y - m[0]) * 256.0f;
-    m[1] = rintf(y);
-    y = (y - m[1]) * 256.0f;
-    m[2] = rintf(y);
-    y = (y - m[2]) * 256.0f;
-    m[3] = rintf(y);
-    m[1] *= 0.00390625f;
-    m[2] *= 1.52587890625e-05f;
-    m[3] *= 5.9604644775390625e-08f;
+    const float y = x * scale;
+    m[0] = __fsub_rn(__fadd_rn(y, 12582912.0f), 12582912.0f);  // 1.5 * 2^23
+    const float r1 = __fsub_rn(y, m[0]);
+    m[1] = __fsub_rn(__fadd_rn(r1, 49152.0f), 49152.0f);  // 1.5 * 2^15
+    const float r2 = __fsub_rn(r1, m[1]);
+    m[2] = __fsub_rn(__fadd_rn(r2, 192.0f), 192.0f);  // 1.5 * 2^7
+    const float r3 = __fsub_rn(r2, m[2]);
+    m[3] = __fsub_rn(__fadd_rn(r3, 0.75f), 0.75f);  // 1.5 * 2^-1
 }
 
+// Two values exactly representable in BF16, packed low = first, high =
+// second: their upper halves (a byte permute, no rounding needed).
 __device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
-    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<uint32_t *>(&v);
+    return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
 }
 
 // Issues the cp.async copies of a tile's connectivity words into buffer cb.
@@ -161,7 +163,7 @@ __device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned c
     constexpr int NP = MS::NP, NF = MS::NF, NQ = MS::NQ, ELEMS = MS::ELEMS, QS = MS::QS;
     static_assert(QS == NP, "the state tile is stored unpadded, as in global memory");
     float *sQ = reinterpret_cast<float *>(smem + MS::OFF_Q);
-    double *sGeo = reinterpret_cast<double *>(smem + MS::OFF_GEO);
+    float *sGeo = reinterpret_cast<float *>(smem + MS::OFF_GEO);
     float4 *sFgeo = reinterpret_cast<float4 *>(smem + MS::OFF_FGEO);
     if (vec && ebase + ELEMS <= a.K) {
         // a whole tile of 16-byte aligned fields: 16-byte copies
@@ -180,7 +182,7 @@ __device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned c
     }
     for (int idx = tid; idx < ELEMS * DIM * DIM; idx += NT) {
         const bool ok = ebase + idx / (DIM * DIM) < a.K;
-        dgtc::cp_async8(&sGeo[idx], ok ? &a.geo[ebase * DIM * DIM + idx] : a.geo, ok ? 8u : 0u);
+        dgtc::cp_async4(&sGeo[idx], ok ? &a.geo[ebase * DIM * DIM + idx] : a.geo, ok ? 4u : 0u);
     }
     for (int idx = tid; idx < ELEMS * NF; idx += NT) {
         const bool ok = ebase + idx / NF < a.K;
@@ -233,7 +235,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     const float *sQ = reinterpret_cast<const float *>(smem + MS::OFF_Q);
     float *sA = reinterpret_cast<float *>(smem + MS::OFF_A);
     const float4 *sNbr = reinterpret_cast<const float4 *>(smem + MS::OFF_NBR);
-    const double *sGeo = reinterpret_cast<const double *>(smem + MS::OFF_GEO);
+    const float *sGeo = reinterpret_cast<const float *>(smem + MS::OFF_GEO);
     const float4 *sFgeo = reinterpret_cast<const float4 *>(smem + MS::OFF_FGEO);
     float *sMax = reinterpret_cast<float *>(smem + MS::OFF_MAX);
     uint8_t *sTab = smem + MS::OFF_TAB;
@@ -320,7 +322,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
 #pragma unroll
             for (int x = 0; x < DIM; ++x)
 #pragma unroll
-                for (int u = 0; u < DIM; ++u) Bg[x][u] = (float)sGeo[le * DIM * DIM + x * DIM + u];
+                for (int u = 0; u < DIM; ++u) Bg[x][u] = sGeo[le * DIM * DIM + x * DIM + u];
             float q[NQ];
 #pragma unroll
             for (int f = 0; f < NQ; ++f) q[f] = sQ[(f * ELEMS + le) * QS + j];

@@ -137,6 +137,7 @@ struct dg_ctx {
     bool mixed = false;
     dgk::MixedKernelSet mks;
     float *d_ulo = nullptr;      // low part of the state pair
+    float *d_geo32 = nullptr;    // inverse Jacobians rounded to FP32 (what the kernels use)
     uint8_t *d_bimg = nullptr;   // sliced operator image
     int *d_beb = nullptr;        // operator row exponents
     int *d_err = nullptr;        // device-side error flag (wait timeouts)
@@ -168,7 +169,8 @@ void free_ctx(dg_ctx *c) {
     void *ptrs[] = {c->d_state, c->d_geo,     c->d_fgeo,    c->d_conn,    c->d_ops,     c->d_tabs,
                     c->d_t0,    c->d_stage64, c->d_mass,    c->d_detj,    c->d_mon,     c->d_bad,
                     c->d_src_at, c->d_src_off, c->d_src_list, c->d_src_w, c->d_src_params, c->d_ulo,
-                    c->d_bimg,  c->d_beb,     c->d_err,     c->d_rec_dof, c->d_trace,   c->d_step0};
+                    c->d_bimg,  c->d_beb,     c->d_err,     c->d_rec_dof, c->d_trace,   c->d_step0,
+                    c->d_geo32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -218,7 +220,7 @@ cudaError_t launch_stage(dg_ctx *c, int stage, double dt) {
         a.fstride = s.fstride;
         a.bstride = c->bstride;
         a.nbatch = c->nbatch;
-        a.geo = s.geo;
+        a.geo = c->d_geo32;
         a.fgeo = s.fgeo;
         a.conn = s.conn;
         a.bimg = c->d_bimg;
@@ -430,6 +432,12 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
         c->grid = std::max(1, std::min(ntiles, (resident + nbatch - 1) / nbatch));
         if (c->mixed) {
             if (!fin(cudaMalloc(&c->d_ulo, state_bytes), "cudaMalloc(ulo)")) break;
+            {
+                std::vector<float> g32(lay.geo.begin(), lay.geo.end());
+                if (!fin(cudaMalloc(&c->d_geo32, g32.size() * 4), "cudaMalloc(geo32)")) break;
+                if (!fin(cudaMemcpy(c->d_geo32, g32.data(), g32.size() * 4, cudaMemcpyHostToDevice), "copy geo32"))
+                    break;
+            }
             if (!fin(cudaMemsetAsync(c->d_ulo, 0, state_bytes, c->stream), "cudaMemset")) break;
             std::vector<uint8_t> img;
             std::vector<int> eb;

@@ -17,3 +17,4 @@ def test_tcgen05_bf16_gemm_is_exact():
     code = D.lib().dg_tc_selftest(0, ctypes.byref(err))
     assert code == 0, D.lib().dg_last_error().decode()
     assert err.value == 0.0
+
