@@ -11,11 +11,13 @@
 // FP32 accumulators, both operands are cut into four fixed-point slices with
 // one exponent per row: a = 2^(ea-8) sum_s m_s 2^(-8s), |m_s| <= 256 integer,
 // stored in BF16 exactly; B is sliced on the host the same way per output
-// node.  Slice products are integers (times 2^-8(i+j)); the pairs with
-// i+j = 0 and i+j = 1 sum exactly in two FP32 tensor-memory accumulators
-// (|sum| < 2^24 units), pairs with 2 <= i+j <= 4 go to a third one.  The
-// epilogue adds the three in double-FP32, scales by 2^(ea+eb-16) dt and
-// applies the RK4 stage update with the state u kept as an FP32 pair.
+// node.  Slice products are integers (times 2^-8(i+j)); the ten pairs with
+// i+j <= 3 are formed (the pairs with i+j = 4 lie 2^-32 below the row scales,
+// under the FP32 resolution of the result).  Pairs with i+j = 0 and i+j = 1
+// sum exactly in FP32 tensor-memory accumulators (|sum| < 2^24 units), the
+// others in further accumulators.  The epilogue adds them in double-FP32,
+// scales by 2^(ea+eb-16) dt and applies the RK4 stage update with the state u
+// kept as an FP32 pair.
 //
 // Roles (128*NWG threads, one CTA per SM, persistent over tiles): cp.async copies
 // bring a tile's state, geometry, connectivity and neighbour traces into
@@ -25,7 +27,7 @@
 // Row r is then sliced by lane r%32 of warps r/32 + 4g of every warp group g
 // (warp w may only touch tensor-memory lanes 32(w%4)..32(w%4)+31), each
 // group taking a share of the K-steps, and stored with tcgen05.st.  One
-// thread issues the 13 x KSTEPS tcgen05.mma and commits them to an mbarrier;
+// thread issues the tcgen05.mma and commits them to an mbarrier;
 // the warp groups then read the accumulators of their row with tcgen05.ld,
 // split by output node, for the epilogue.  Every wait is bounded; on timeout the kernel records an error,
 // waits once more for the MMAs in flight, frees tensor memory and stops.
@@ -55,16 +57,16 @@ struct MixedShape {
     static constexpr int TMEM_COLS = 512;
     static constexpr bool FITS = ACC + 3 * NPAD <= TMEM_COLS;
     // Level scheme (where it fits): one accumulator per level L = i+j of the
-    // slice pairs (0..4).  The B slices of a K-step lie side by side along N,
-    // so A slice i meets B slices 0..min(3, 4-i) in one MMA of N = that many
-    // x NPAD, accumulating into levels i..: four MMAs per K-step.
-    static constexpr bool LEVELS = ACC + 5 * NPAD <= TMEM_COLS && 4 * NPAD <= 256;
+    // slice pairs (0..3).  The B slices of a K-step lie side by side along N,
+    // so A slice i meets B slices 0..3-i in one MMA of N = (4-i) x NPAD,
+    // accumulating into levels i..3: four MMAs per K-step.
+    static constexpr bool LEVELS = ACC + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256;
     // Pair scheme (otherwise): one MMA per slice pair; accumulator 0 for
-    // i+j = 0, 1 for i+j = 1 (both exact), NX more for the ten pairs with
-    // i+j >= 2 (spread so that the MMAs of consecutive pairs do not wait on
+    // i+j = 0, 1 for i+j = 1 (both exact), NX more for the seven pairs with
+    // i+j = 2, 3 (spread so that the MMAs of consecutive pairs do not wait on
     // one another)
     static constexpr int NACC_FIT = (TMEM_COLS - ACC) / NPAD;
-    static constexpr int NACC = LEVELS ? 5 : NACC_FIT < 9 ? NACC_FIT : 9;
+    static constexpr int NACC = LEVELS ? 4 : NACC_FIT < 9 ? NACC_FIT : 9;
     static constexpr int NX = NACC - 2;
     static constexpr int BTILE = NPAD * 32;         // bytes of one (K-step, slice) B tile; image [K-step][slice]
     static constexpr int BBYTES = 4 * KSTEPS * BTILE;
@@ -94,7 +96,8 @@ struct MixedShape {
     static constexpr int SMEM_LAUNCH = SMEM < 118 * 1024 ? 118 * 1024 : SMEM;
 };
 
-// Pair list of the slice products: (A slice, B slice), i + j <= 4.
+// Pair list of the slice products (A slice, B slice) by level i + j; the
+// first ten (i + j <= 3) are formed.
 __device__ __constant__ const int8_t kPairA[13] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 1, 2, 3};
 __device__ __constant__ const int8_t kPairB[13] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0, 3, 2, 1};
 
@@ -470,42 +473,29 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             for (int sl = 0; sl < 4; ++sl)
                 dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, sl * ACOLS + c * 8), w[sl]);
         }
-        if constexpr (MS::LEVELS) {
-            // level 4 only receives accumulating MMAs: clear this part's columns
-            uint32_t z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            __syncwarp();
-#pragma unroll
-            for (int c = 0; c < NCH; ++c)
-                dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 4 * NPAD + i0 + 8 * c), z);
-        }
         dgtc::tmem_st_wait();
         dgtc::fence_before_sync();
         __syncthreads();
 
-        // 4. tensor-core contraction: 13 slice pairs x KSTEPS, issued by thread 0
-        //    K-step by K-step, so that consecutive MMAs (different pairs) mostly
-        //    accumulate into different accumulators
+        // 4. tensor-core contraction, issued by thread 0 K-step by K-step
         if (tid == 0) {
             dgtc::fence_after_sync();
             if constexpr (MS::LEVELS) {
-                // level 4 was zeroed while slicing; A slice 0 at K-step 0
-                // starts levels 0..3
+                // A slice 0 at K-step 0 starts all four levels
 #pragma unroll 1
                 for (int t = 0; t < KSTEPS; ++t) {
                     const uint64_t bd = dgtc::desc_kmajor(sB + t * 4 * MS::BTILE, 128, 256);
 #pragma unroll
-                    for (int ia = 0; ia < 4; ++ia) {
-                        const int nj = ia < 2 ? 4 : 5 - ia;
+                    for (int ia = 0; ia < 4; ++ia)
                         dgtc::mma_bf16_ts(tbase + MS::ACC + ia * NPAD, tbase + ia * ACOLS + t * 8, bd,
-                                          dgtc::idesc_bf16_f32(128, nj * NPAD), (t > 0 || ia > 0) ? 1u : 0u);
-                    }
+                                          dgtc::idesc_bf16_f32(128, (4 - ia) * NPAD), (t > 0 || ia > 0) ? 1u : 0u);
                 }
             } else {
                 unsigned started = 0;  // bit per accumulator
 #pragma unroll 1
                 for (int t = 0; t < KSTEPS; ++t) {
 #pragma unroll
-                    for (int pi = 0; pi < 13; ++pi) {
+                    for (int pi = 0; pi < 10; ++pi) {
                         const int ia = kPairA[pi], jb = kPairB[pi];
                         const int slot = pi == 0 ? 0 : pi < 3 ? 1 : 2 + (pi - 3) % NX;
                         const uint64_t bd = dgtc::desc_kmajor(sB + (t * 4 + jb) * MS::BTILE, 128, 256);
