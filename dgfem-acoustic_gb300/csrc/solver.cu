@@ -15,6 +15,7 @@
 #include "host/capi_common.h"
 #include "host/layout.h"
 #include "host/refel.h"
+#include "ctx.h"
 #include "kernels.h"
 #include "stage_kernel.cuh"
 
@@ -99,56 +100,6 @@ __global__ void monitor_kernel(const Real *u, long long fstride, int K, int np, 
 
 }  // namespace
 
-struct dg_ctx {
-    int dim = 0, order = 0, np = 0, nf = 0, nfp = 0, nq = 0, K = 0;
-    long long ndof = 0;  // K * np
-    int nbatch = 1;       // independent states (sources) on the mesh
-    long long bstride = 0;  // values per batch member: nq * ndof
-    int prec = 0, flux_sign = 0, device = 0, use_graph = 1;
-    size_t rsize = 8;
-    double c0 = 1, rho0 = 1, v0[3] = {0, 0, 0};
-    cudaStream_t stream = nullptr;
-    char *d_state = nullptr;  // u, acc, wa, wb
-    void *d_u = nullptr, *d_acc = nullptr, *d_wa = nullptr, *d_wb = nullptr;
-    double *d_geo = nullptr;
-    void *d_fgeo = nullptr;
-    int2 *d_conn = nullptr;
-    void *d_ops = nullptr;
-    uint8_t *d_tabs = nullptr;
-    double *d_t0 = nullptr;
-    double *d_stage64 = nullptr;  // FP64 staging (FP32 contexts)
-    double *d_mass = nullptr, *d_detj = nullptr, *d_mon = nullptr;
-    unsigned long long *d_bad = nullptr;
-    // sources: node j is the field-0 value at d_src_at[j] (member folded in)
-    int src_nodes = 0;
-    long long *d_src_at = nullptr;
-    int *d_src_off = nullptr, *d_src_list = nullptr;
-    double *d_src_w = nullptr, *d_src_params = nullptr;
-    std::vector<double> src_duration;
-    // receivers
-    int rec_n = 0, rec_max = 0;
-    long long rec_done = 0;  // steps recorded so far
-    int *d_rec_dof = nullptr;
-    double *d_trace = nullptr;
-    long long *d_step0 = nullptr;
-    dgk::KernelSet ks;
-    int grid = 0;
-    // mixed form
-    bool mixed = false;
-    dgk::MixedKernelSet mks;
-    float *d_ulo = nullptr;      // low part of the state pair
-    float *d_geo32 = nullptr;    // inverse Jacobians rounded to FP32 (what the kernels use)
-    uint8_t *d_bimg = nullptr;   // sliced operator image
-    int *d_beb = nullptr;        // operator row exponents
-    int *d_err = nullptr;        // device-side error flag (wait timeouts)
-    // graph cache
-    cudaGraphExec_t gexec = nullptr;
-    double graph_dt = 0;
-    int graph_src = -1;
-    int graph_method = -1;
-    // events for profiling
-    std::vector<cudaEvent_t> events;
-};
 
 namespace {
 

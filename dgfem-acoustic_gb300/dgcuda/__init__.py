@@ -58,6 +58,7 @@ def _check(code: int) -> None:
 
 
 P_d, P_i, P_u8 = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_ubyte)
+P_f = C.POINTER(C.c_float)
 
 
 class MeshDesc(C.Structure):
@@ -145,6 +146,25 @@ def _declare(L: C.CDLL) -> None:
         "dg_multi_set_config": (C.c_int, [vp, C.c_int]),
         "dg_multi_autotune": (C.c_int, [vp, P_d, C.c_int, P_i, P_d]),
         "dg_multi_info": (C.c_int, [vp, C.POINTER(C.c_longlong), P_i, P_i, P_i]),
+        "dg_mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint, C.c_int, C.POINTER(vp)]),
+        "dg_mlp_destroy": (None, [vp]),
+        "dg_mlp_num_params": (C.c_longlong, [vp]),
+        "dg_mlp_get_params": (C.c_int, [vp, P_f]),
+        "dg_mlp_set_params": (C.c_int, [vp, P_f]),
+        "dg_mlp_forward": (C.c_int, [vp, P_f, C.c_int, P_f]),
+        "dg_mlp_loss_grad": (C.c_int, [vp, P_f, P_f, C.c_int, P_d, P_f]),
+        "dg_mlp_train_step": (C.c_int, [vp, P_f, P_f, C.c_int, C.c_double, P_d]),
+        "dg_learned_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(PhysDesc), C.c_int, C.c_int, C.c_int,
+                                        C.c_int, C.c_double, C.c_uint, C.c_int, C.POINTER(vp)]),
+        "dg_learned_destroy": (None, [vp]),
+        "dg_learned_info": (C.c_int, [vp, P_i, P_i, C.POINTER(vp)]),
+        "dg_learned_collect": (C.c_int, [vp, C.POINTER(P_d), C.c_int, C.c_int]),
+        "dg_learned_num_samples": (C.c_longlong, [vp]),
+        "dg_learned_train": (C.c_int, [vp, C.c_int, C.c_int, C.c_double, C.c_uint, P_d]),
+        "dg_learned_apply": (C.c_int, [vp, C.POINTER(P_d), C.c_int]),
+        "dg_learned_step_stats": (C.c_int, [vp, C.POINTER(C.c_longlong), P_d, P_d]),
+        "dg_parareal": (C.c_int, [vp, C.POINTER(MeshDesc), C.POINTER(PhysDesc), C.c_int, C.POINTER(P_d), C.c_int,
+                                  C.c_int, C.c_double, C.c_double, C.c_int, C.POINTER(P_d), P_i, P_d]),
         "dg_create_batch": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(PhysDesc), C.POINTER(Opts), C.c_int,
                                       C.POINTER(vp)]),
         "dg_set_state_member": (C.c_int, [vp, C.c_int, C.POINTER(P_d)]),
@@ -652,3 +672,126 @@ class MultiSolver:
         _check(lib().dg_multi_info(self._h, C.byref(dofs), C.byref(ncfg), C.byref(cfg), bt))
         return {"dofs_per_field": dofs.value, "ncfg": ncfg.value, "cfg": cfg.value,
                 "block_threads": list(bt)[:ncfg.value]}
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(P_f)
+
+
+class MLP:
+    """dg_mlp: FP32 MLP nin -> width (GELU) x hidden_layers -> nout, trained
+    on the GPU by the library's own kernels."""
+
+    def __init__(self, nin: int, width: int, nout: int, hidden_layers: int, seed: int = 0, device: int = 0):
+        h = C.c_void_p()
+        _check(lib().dg_mlp_create(nin, width, nout, hidden_layers, seed, device, C.byref(h)))
+        self._h = h
+        self.nin, self.width, self.nout, self.hidden = nin, width, nout, hidden_layers
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.dg_mlp_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def num_params(self) -> int:
+        return int(lib().dg_mlp_num_params(self._h))
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.num_params(), dtype=np.float32)
+        _check(lib().dg_mlp_get_params(self._h, _fptr(p)))
+        return p
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(lib().dg_mlp_set_params(self._h, _fptr(p)))
+
+    def forward(self, X: np.ndarray) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((X.shape[0], self.nout), dtype=np.float32)
+        _check(lib().dg_mlp_forward(self._h, _fptr(X), X.shape[0], _fptr(Y)))
+        return Y
+
+    def loss_grad(self, X: np.ndarray, T: np.ndarray) -> tuple[float, np.ndarray]:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        g = np.zeros(self.num_params(), dtype=np.float32)
+        loss = C.c_double()
+        _check(lib().dg_mlp_loss_grad(self._h, _fptr(X), _fptr(T), X.shape[0], C.byref(loss), _fptr(g)))
+        return loss.value, g
+
+    def train_step(self, X: np.ndarray, T: np.ndarray, lr: float) -> float:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        loss = C.c_double()
+        _check(lib().dg_mlp_train_step(self._h, _fptr(X), _fptr(T), X.shape[0], lr, C.byref(loss)))
+        return loss.value
+
+
+class Learned:
+    """dg_learned: element-local network as coarse propagator of coarse_steps
+    fine RK4 steps on one mesh."""
+
+    def __init__(self, pre: Precomp, c0: float, rho0: float, v0=(0.0, 0.0, 0.0), flux: str = "upwind",
+                 width: int = 256, hidden_layers: int = 3, coarse_steps: int = 10, dt: float = 1e-6, seed: int = 0,
+                 device: int = 0):
+        self._desc = pre.desc()
+        self._phys = PhysDesc(c0, rho0, (C.c_double * 3)(*v0))
+        self.flux = {"reference": FLUX_REFERENCE, "upwind": FLUX_UPWIND}[flux]
+        h = C.c_void_p()
+        _check(lib().dg_learned_create(C.byref(self._desc), C.byref(self._phys), self.flux, width, hidden_layers,
+                                       coarse_steps, dt, seed, device, C.byref(h)))
+        self._h = h
+        self.pre = pre
+        self.coarse_steps = coarse_steps
+        self.dt = dt
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.dg_learned_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def collect(self, u0: np.ndarray, nsnap: int, max_rows: int = 1 << 20) -> None:
+        u0 = np.ascontiguousarray(u0, dtype=np.float64)
+        ptrs = (P_d * 4)(*[_dptr(u0[q]) for q in range(4)])
+        _check(lib().dg_learned_collect(self._h, ptrs, nsnap, max_rows))
+
+    def num_samples(self) -> int:
+        return int(lib().dg_learned_num_samples(self._h))
+
+    def train(self, epochs: int, batch: int = 4096, lr: float = 1e-3, seed: int = 0) -> float:
+        loss = C.c_double()
+        _check(lib().dg_learned_train(self._h, epochs, batch, lr, seed, C.byref(loss)))
+        return loss.value
+
+    def step_stats(self) -> dict:
+        n, am, amin = C.c_longlong(), C.c_double(), C.c_double()
+        _check(lib().dg_learned_step_stats(self._h, C.byref(n), C.byref(am), C.byref(amin)))
+        return {"applications": n.value, "alpha_mean": am.value, "alpha_min": amin.value}
+
+    def apply(self, u: np.ndarray, napps: int) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float64).copy()
+        ptrs = (P_d * 4)(*[_dptr(u[q]) for q in range(4)])
+        _check(lib().dg_learned_apply(self._h, ptrs, napps))
+        return u
+
+
+def parareal(pre: Precomp, c0: float, rho0: float, u0: np.ndarray, nslices: int, slice_steps: int, dt: float,
+             tol: float, max_iter: int, learned: "Learned | None" = None, v0=(0.0, 0.0, 0.0),
+             flux: str = "upwind") -> tuple[np.ndarray, int, list]:
+    """dg_parareal: returns (end state of the last slice, iterations, change per iteration)."""
+    desc = pre.desc()
+    phys = PhysDesc(c0, rho0, (C.c_double * 3)(*v0))
+    u0 = np.ascontiguousarray(u0, dtype=np.float64)
+    uin = (P_d * 4)(*[_dptr(u0[q]) for q in range(4)])
+    out = np.zeros_like(u0)
+    uout = (P_d * 4)(*[_dptr(out[q]) for q in range(4)])
+    it = C.c_int()
+    hist = np.zeros(max(max_iter, 1))
+    _check(lib().dg_parareal(learned._h if learned else None, C.byref(desc), C.byref(phys),
+                             {"reference": FLUX_REFERENCE, "upwind": FLUX_UPWIND}[flux], uin, nslices, slice_steps, dt,
+                             tol, max_iter, uout, C.byref(it), _dptr(hist)))
+    return out, it.value, hist[:it.value].tolist()

@@ -251,6 +251,58 @@ int dg_multi_set_config(dg_multi *ctx, int cfg);
 int dg_multi_autotune(dg_multi *ctx, const double *dt, int trial_steps, int *chosen, double *ms_per_step);
 int dg_multi_info(dg_multi *ctx, long long *dofs_per_field, int *ncfg, int *cfg, int *block_threads);
 
+/* Learned coarse propagator and parareal (no counterpart in the reference).
+ *
+ * dg_mlp: a fully connected network nin -> width (GELU) x hidden_layers ->
+ * nout in FP32, trained on the GPU by its own forward, backward (mean
+ * squared error) and Adam kernels.  Parameters are packed per layer as the
+ * weights [out][in] row-major followed by the biases [out]. */
+typedef struct dg_mlp dg_mlp;
+int dg_mlp_create(int nin, int width, int nout, int hidden_layers, unsigned seed, int device, dg_mlp **out);
+void dg_mlp_destroy(dg_mlp *net);
+long long dg_mlp_num_params(const dg_mlp *net);
+int dg_mlp_get_params(dg_mlp *net, float *params);
+int dg_mlp_set_params(dg_mlp *net, const float *params);
+/* X [rows][nin] -> Y [rows][nout] (host arrays). */
+int dg_mlp_forward(dg_mlp *net, const float *X, int rows, float *Y);
+/* Mean squared error over rows x nout against T and its gradient (packed
+ * like the parameters; grad may be NULL). */
+int dg_mlp_loss_grad(dg_mlp *net, const float *X, const float *T, int rows, double *loss, float *grad);
+int dg_mlp_train_step(dg_mlp *net, const float *X, const float *T, int rows, double lr, double *loss);
+
+/* dg_learned: an element-local network (inputs: the element's DOFs, its face
+ * neighbours' traces at its face nodes, its boundary-face kinds and inverse
+ * Jacobian; outputs: the element's DOF increments over coarse_steps fine RK4
+ * steps of size dt) trained on FP64 DG trajectories of the mesh. */
+typedef struct dg_learned dg_learned;
+int dg_learned_create(const dg_mesh_desc *mesh, const dg_phys_desc *phys, int flux_sign, int width,
+                      int hidden_layers, int coarse_steps, double dt, unsigned seed, int device, dg_learned **out);
+void dg_learned_destroy(dg_learned *learned);
+int dg_learned_info(dg_learned *learned, int *nin, int *nout, dg_mlp **net);
+/* Runs the FP64 DG from u0 for nsnap x coarse_steps steps and keeps the
+ * (features, increments) pairs of active elements, at most max_rows per
+ * snapshot. */
+int dg_learned_collect(dg_learned *learned, const double *const u0[4], int nsnap, int max_rows);
+long long dg_learned_num_samples(dg_learned *learned);
+int dg_learned_train(dg_learned *learned, int epochs, int batch, double lr, unsigned seed, double *loss);
+/* Each coarse application adds alpha x the predicted increment, alpha <= 1
+ * the largest factor that does not raise the discrete energy (lumped mass);
+ * the number of applications so far and their mean and least alpha. */
+int dg_learned_step_stats(dg_learned *learned, long long *applications, double *alpha_mean, double *alpha_min);
+/* napps coarse applications on a host state, in place. */
+int dg_learned_apply(dg_learned *learned, double *const u[4], int napps);
+
+/* Parareal over nslices time slices of slice_steps FP64 RK4 steps each from
+ * u0: the fine propagator is the FP64 DG run for all slices as one batch,
+ * the coarse one the learned network (slice_steps / coarse_steps
+ * applications) or, with learned = NULL, the identity.  Stops when the
+ * largest relative change of a slice end state is at most tol, or after
+ * max_iter iterations (max_iter = nslices reproduces the serial DG).  uout
+ * gets the end state of the last slice, hist[k] the change at iteration k. */
+int dg_parareal(dg_learned *learned, const dg_mesh_desc *mesh, const dg_phys_desc *phys, int flux_sign,
+                const double *const u0[4], int nslices, int slice_steps, double dt, double tol, int max_iter,
+                double *const uout[4], int *iters, double *hist);
+
 /* Self-test of the tensor-core primitives of the mixed form (no counterpart
  * in the reference): a 128x32x112 BF16 GEMM with A in tensor memory and B in
  * shared memory on the given device; *max_abs_err = 0 when the FP32 result

@@ -1,0 +1,108 @@
+"""The learned part: the GPU MLP kernels against the float64 NumPy oracle
+(forward, loss and gradients), training, and parareal with the identity and
+with the learned coarse propagator, judged by the serial FP64 DG."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import dgcuda as D
+import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+C0, RHO0 = 340.0, 1.225
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("nin,width,nout,hidden,rows", [(40, 64, 12, 3, 300), (37, 70, 13, 2, 301),
+                                                         (261, 256, 80, 3, 517)])
+def test_mlp_forward_loss_and_gradients_match_oracle(nin, width, nout, hidden, rows):
+    rng = np.random.default_rng(nin)
+    net = D.MLP(nin, width, nout, hidden, seed=3)
+    p = net.params()
+    assert p.size == sum(o * i + o for (o, i) in M.shapes(nin, width, nout, hidden))
+    p = (rng.standard_normal(p.size) * 0.2).astype(np.float32)
+    net.set_params(p)
+    X = rng.standard_normal((rows, nin)).astype(np.float32)
+    T = rng.standard_normal((rows, nout)).astype(np.float32)
+    Y = net.forward(X)
+    Yo, _, _ = M.forward(p, X, nin, width, nout, hidden)
+    assert rel(Y, Yo) <= 1e-5
+    loss, g = net.loss_grad(X, T)
+    lo, go = M.loss_grad(p, X, T, nin, width, nout, hidden)
+    assert abs(loss - lo) <= 1e-5 * lo
+    assert rel(g, go) <= 1e-4
+    net.close()
+
+
+def test_mlp_training_reduces_the_loss():
+    rng = np.random.default_rng(0)
+    X = rng.uniform(-1, 1, (2048, 6)).astype(np.float32)
+    T = np.stack([np.sin(2 * X[:, 0]) * X[:, 1], X[:, 2] ** 2 - X[:, 3] * X[:, 4]], axis=1).astype(np.float32)
+    net = D.MLP(6, 64, 2, 3, seed=1)
+    first = net.loss_grad(X, T)[0]
+    for _ in range(300):
+        net.train_step(X, T, 3e-3)
+    assert net.loss_grad(X, T)[0] < 0.05 * first
+
+
+def room(nx=6, ny=5, nz=4, order=3):
+    mesh = D.Mesh.box_tet(nx, ny, nz, (0.0, 0.0, 0.0), (1.2, 1.0, 0.8), order=order,
+                          side_names=("Reflecting", "Absorbing", "Reflecting", "Reflecting", "Absorbing",
+                                      "Reflecting"))
+    return mesh, D.Precomp(mesh)
+
+
+def test_identity_parareal_reaches_the_serial_dg_in_n_iterations():
+    mesh, pre = room(4, 3, 3, order=2)
+    dt = D.cfl_dt(pre, C0)
+    u0 = pre.initial_state([(0, 0.5, 0.4, 0.4, 0.01, 1.0)])
+    nslices, steps = 4, 5
+    s = D.Solver(pre, C0, RHO0, flux="upwind")
+    s.set_state(u0)
+    s.rk4_steps(0.0, dt, nslices * steps)
+    ref = s.get_state()
+    out, iters, hist = D.parareal(pre, C0, RHO0, u0, nslices, steps, dt, tol=0.0, max_iter=nslices)
+    assert iters == nslices and len(hist) == nslices
+    for q in range(4):
+        assert rel(out[q], ref[q]) <= 1e-12
+    # fewer iterations than slices leave the last slice inexact
+    out2, _, _ = D.parareal(pre, C0, RHO0, u0, nslices, steps, dt, tol=0.0, max_iter=2)
+    assert rel(out2[0], ref[0]) > 1e-3
+
+
+def test_learned_coarse_propagator_beats_the_identity():
+    """Trained on FP64 DG trajectories of four pulse positions, the network
+    (3 hidden GELU layers of 128, one fine step per application, energy
+    clipped) propagates a pulse at a fifth position; parareal with it is
+    closer to the serial DG after two iterations than parareal without it
+    (identity coarse propagator), and converged parareal is the DG answer."""
+    mesh, pre = room()
+    dt = D.cfl_dt(pre, C0)
+    L = D.Learned(pre, C0, RHO0, width=128, hidden_layers=3, coarse_steps=1, dt=dt, seed=7)
+    for pos in [(0.3, 0.3, 0.3), (0.9, 0.7, 0.5), (0.5, 0.2, 0.6), (0.8, 0.5, 0.2)]:
+        L.collect(pre.initial_state([(0, *pos, 0.02, 1.0)]), nsnap=60)
+    assert L.num_samples() > 1000
+    loss = L.train(epochs=40, batch=1024, lr=1e-3)
+    assert np.isfinite(loss)
+    u0 = pre.initial_state([(0, 0.6, 0.45, 0.4, 0.02, 1.0)])
+    nslices, steps = 8, 16
+    s = D.Solver(pre, C0, RHO0, flux="upwind")
+    s.set_state(u0)
+    s.rk4_steps(0.0, dt, nslices * steps)
+    ref = s.get_state()
+    err = {}
+    for name, lrn in (("learned", L), ("identity", None)):
+        out, it, _ = D.parareal(pre, C0, RHO0, u0, nslices, steps, dt, tol=0.0, max_iter=2, learned=lrn)
+        err[name] = rel(out[0], ref[0])
+    assert err["learned"] < 0.5 * err["identity"], err
+    st = L.step_stats()
+    assert st["applications"] > 0 and 0.0 < st["alpha_mean"] <= 1.0
+    # converged parareal with the network is the DG answer
+    out, it, hist = D.parareal(pre, C0, RHO0, u0, nslices, steps, dt, tol=1e-5, max_iter=nslices, learned=L)
+    assert rel(out[0], ref[0]) <= 1e-4
+    assert it <= nslices
