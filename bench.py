@@ -425,6 +425,8 @@ def ours_arm(args, world, rank, local, pg):
         line["batched"] = batched_section(D, args, local)
     if world == 1 and not args.no_uneven:
         line["uneven_batch"] = uneven_section(D, args, local)
+    if world == 1 and not args.no_parareal:
+        line["learned_parareal"] = parareal_section(D, args, local)
     print(json.dumps(line), flush=True)
 
 
@@ -525,6 +527,55 @@ def uneven_section(D, args, local):
             "clocks": clk.summary()}
 
 
+def parareal_section(D, args, local):
+    """Learned parareal on a room with seeded box obstacles (order 3): an
+    element-local MLP (3 hidden GELU layers of 256) trained on the GPU on FP64
+    DG trajectories of 8 pulse positions, used as coarse propagator of
+    parareal (one fine step per application) for a pulse at another
+    position; fine propagator = the FP64 DG over all slices as one batch.
+    Compared with parareal without the network (identity coarse propagator)
+    and with the serial FP64 DG, which judges the error."""
+    from dgcuda import workloads as W
+
+    t0 = time.time()
+    cells = tuple(args.parareal_cells)
+    mesh, pre, dt, ic, train = W.room(cells=cells, order=3, seed=SEED)
+    nsl, sst = args.parareal_slices, args.parareal_slice_steps
+    L = D.Learned(pre, C0, RHO0, flux=FLUX, width=256, hidden_layers=3, coarse_steps=1, dt=dt, seed=SEED,
+                  device=local)
+    for tic in train:
+        L.collect(pre.initial_state([tic]), nsnap=args.parareal_train_steps, max_rows=2000)
+    t_collect = time.time() - t0
+    t1 = time.time()
+    loss = L.train(epochs=args.parareal_epochs, batch=4096, lr=1e-3, seed=SEED)
+    t_train = time.time() - t1
+    u0 = pre.initial_state([ic])
+    s = D.Solver(pre, C0, RHO0, flux=FLUX, device=local)
+    s.set_state(u0)
+    _, ms_serial = s.rk4_steps_timed(0.0, dt, nsl * sst)
+    ref = s.get_state()
+    s.close()
+    out = {"workload": f"room 20 x 12 x 8 as {cells[0]}x{cells[1]}x{cells[2]} hexes x 6 tets minus 12 seeded box "
+                       f"obstacles ({pre.num_el} tets), order 3, reflecting walls, Gaussian pulse (sigma one cell) at "
+                       f"a seeded point; {nsl} slices x {sst} RK4 steps; network trained on 8 other pulse positions",
+           "tets": pre.num_el, "slices": nsl, "slice_steps": sst, "tol": args.parareal_tol,
+           "training": {"pairs": L.num_samples(), "epochs": args.parareal_epochs, "final_loss": loss,
+                        "collect_s": t_collect, "train_s": t_train},
+           "serial_fp64_ms": ms_serial}
+    for name, lrn in (("learned", L), ("identity", None)):
+        w0 = time.perf_counter()
+        u, it, hist = D.parareal(pre, C0, RHO0, u0, nsl, sst, dt, tol=args.parareal_tol, max_iter=nsl, learned=lrn,
+                                 flux=FLUX)
+        wall = time.perf_counter() - w0
+        err = max(float(np.linalg.norm(u[q] - ref[q]) / np.linalg.norm(ref[q])) for q in range(4))
+        out[name] = {"iterations": it, "wall_ms": wall * 1e3, "rel_l2_vs_serial_fp64": err,
+                     "change_per_iteration": hist}
+    out["coarse_step_alpha"] = L.step_stats()
+    out["serial_equivalent_fine_work_dof_stages"] = pre.ndof * 4 * 4 * nsl * sst
+    L.close()
+    return out
+
+
 def accuracy_all(D, pre, u0, dt, v0, args, local, nq):
     """Every form after the configuration's steps, relative L2 per field
     against the FP64 form (which the parity tests tie to the CPU oracle)."""
@@ -569,6 +620,13 @@ def main():
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven multi-mesh section")
     ap.add_argument("--uneven-meshes", type=int, default=32)
     ap.add_argument("--uneven-steps", type=int, default=500)
+    ap.add_argument("--no-parareal", action="store_true", help="skip the learned parareal section")
+    ap.add_argument("--parareal-cells", type=int, nargs=3, default=[20, 12, 8])
+    ap.add_argument("--parareal-slices", type=int, default=16)
+    ap.add_argument("--parareal-slice-steps", type=int, default=50)
+    ap.add_argument("--parareal-train-steps", type=int, default=100)
+    ap.add_argument("--parareal-epochs", type=int, default=10)
+    ap.add_argument("--parareal-tol", type=float, default=1e-5)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least three untimed warm-up steps
     world, rank, local, pg = dist_init()

@@ -275,10 +275,13 @@ __global__ void apply_increment_kernel(double *u, long long ndof, int K, int np,
 
 // Energy products of the state u and the increment d (lumped: element
 // Jacobian determinant times the nodal energy density p^2/(rho c^2) +
-// rho |v|^2): out[0] += <u, d>, out[1] += <d, d>, out[2] += <u, u>.
+// rho |v|^2): block b writes its partial <u, d>, <d, d>, <u, u> to
+// part[3b..3b+2]; sum_parts adds them in a fixed order, so that a coarse
+// application is bit-reproducible (parareal's cancellation G(U) - G(U) needs
+// that).
 __global__ void energy_products_kernel(const double *u, long long ndof, int K, int np, int nq, const float *Y,
                                        const float *escale, double s0, double s1, double s2, double s3,
-                                       const double *detj, double wp, double wv, double *out) {
+                                       const double *detj, double wp, double wv, double *part) {
     const double sc[4] = {s0, s1, s2, s3};
     const long long n = (long long)K * np * nq;
     double ud = 0.0, dd = 0.0, uu = 0.0;
@@ -306,10 +309,27 @@ __global__ void energy_products_kernel(const double *u, long long ndof, int K, i
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        atomicAdd(&out[0], r0[0]);
-        atomicAdd(&out[1], r1[0]);
-        atomicAdd(&out[2], r2[0]);
+        part[3 * blockIdx.x] = r0[0];
+        part[3 * blockIdx.x + 1] = r1[0];
+        part[3 * blockIdx.x + 2] = r2[0];
     }
+}
+
+// out[k] = sum over the nparts partial triples (one block, fixed order).
+__global__ void sum_parts_kernel(const double *part, int nparts, double *out) {
+    __shared__ double r[3][256];
+    double a[3] = {0, 0, 0};
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x)
+        for (int k = 0; k < 3; ++k) a[k] += part[3 * b + k];
+    for (int k = 0; k < 3; ++k) r[k][threadIdx.x] = a[k];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int k = 0; k < 3; ++k) r[k][threadIdx.x] += r[k][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 3; ++k) out[k] = r[k][0];
 }
 
 // Training targets: (u1 - u0) per element in output order, divided by the
@@ -624,6 +644,7 @@ struct dg_learned {
     float *d_escale = nullptr;  // [K] input scale of each element
     double *d_detj = nullptr;   // [K] element Jacobian determinants
     double *d_prod = nullptr;   // energy products of a coarse application
+    double *d_parts = nullptr;  // their per-block partial sums
     double alpha_sum = 0, alpha_min = 1;  // step factors of the applications so far
     long long applications = 0;
     std::vector<float *> samples_x, samples_t;  // device blocks of training rows
@@ -668,12 +689,13 @@ int coarse_apply(dg_learned *L, double *u, cudaStream_t s) {
     // energy-stable step: u + d, scaled back to E(u) if it has more energy
     // (the upwind DG propagator with these walls never gains energy)
     const long long nv = (long long)c->K * c->np * c->nq;
-    CK(cudaMemsetAsync(L->d_prod, 0, 24, n->stream));
     double os[4];
     for (int f = 0; f < 4; ++f) os[f] = (double)L->out_scale[f] * L->tscale[f];
-    energy_products_kernel<<<grid_for(nv), 256, 0, n->stream>>>(
-        u, c->ndof, c->K, c->np, c->nq, n->d_Y, L->d_escale, os[0], os[1], os[2], os[3], L->d_detj,
-        1.0 / (c->rho0 * c->c0 * c->c0), c->rho0, L->d_prod);
+    const int nb = grid_for(nv);
+    energy_products_kernel<<<nb, 256, 0, n->stream>>>(u, c->ndof, c->K, c->np, c->nq, n->d_Y, L->d_escale, os[0],
+                                                       os[1], os[2], os[3], L->d_detj,
+                                                       1.0 / (c->rho0 * c->c0 * c->c0), c->rho0, L->d_parts);
+    sum_parts_kernel<<<1, 256, 0, n->stream>>>(L->d_parts, nb, L->d_prod);
     double pr[3];
     CK(cudaMemcpyAsync(pr, L->d_prod, 24, cudaMemcpyDeviceToHost, n->stream));
     CK(cudaStreamSynchronize(n->stream));
@@ -744,6 +766,7 @@ int dg_learned_create(const dg_mesh_desc *mesh, const dg_phys_desc *phys, int fl
     if (e == cudaSuccess) e = cudaMalloc(&L->d_feat, (size_t)c->K * L->nin * 4);
     if (e == cudaSuccess) e = cudaMalloc(&L->d_escale, (size_t)c->K * 4);
     if (e == cudaSuccess) e = cudaMalloc(&L->d_prod, 24);
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_parts, (size_t)3 * 4096 * 8);
     if (e == cudaSuccess) e = cudaMalloc(&L->d_detj, (size_t)c->K * 8);
     if (e == cudaSuccess) e = cudaMemcpy(L->d_detj, mesh->el_jacobian_dets, (size_t)c->K * 8, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&L->d_u0, (size_t)c->ndof * c->nq * 8);
@@ -761,7 +784,7 @@ void dg_learned_destroy(dg_learned *L) {
     for (float *p : L->samples_x) cudaFree(p);
     for (float *p : L->samples_t) cudaFree(p);
     for (void *p : {(void *)L->d_conn, (void *)L->d_tabs, (void *)L->d_geo, (void *)L->d_feat, (void *)L->d_escale,
-                    (void *)L->d_prod, (void *)L->d_detj, (void *)L->d_u0, (void *)L->d_u1})
+                    (void *)L->d_prod, (void *)L->d_parts, (void *)L->d_detj, (void *)L->d_u0, (void *)L->d_u1})
         if (p) cudaFree(p);
     if (L->net) dg_mlp_destroy(L->net);
     if (L->fine) dg_destroy(L->fine);

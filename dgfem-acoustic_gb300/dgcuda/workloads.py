@@ -73,3 +73,35 @@ def uneven(nmesh: int = 32, seed: int = 2026, h: float = 0.025, min_tets: int = 
         dofs, w = pre.gaussian_source(*pos, sigma)
         srcs.append((i, dofs, w, 1.0, float(rng.uniform(2.0, 8.0)), 0.0, 1e30))
     return meshes, pres, phys, np.array(dts), srcs
+
+
+def room(cells=(20, 12, 8), size=(20.0, 12.0, 8.0), order: int = 3, nobst: int = 12, seed: int = 2026,
+         ntrain: int = 8):
+    """Room of the given size as a hex grid split into tets, with nobst seeded
+    box obstacles (1-3 cells per side, cells removed, reflecting), reflecting
+    walls.  Returns (mesh, pre, dt, ic, train_ics): ic is a Gaussian pressure
+    pulse (sigma = one cell) at a seeded free point, train_ics ntrain more."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = cells
+    h = np.array(size) / np.array(cells)
+    gone = np.zeros(cells[::-1], dtype=bool)  # [k][j][i]
+    for _ in range(nobst):
+        ext = rng.integers(1, 4, 3)
+        at = [int(rng.integers(0, c - e + 1)) for c, e in zip(cells, ext)]
+        gone[at[2]:at[2] + ext[2], at[1]:at[1] + ext[1], at[0]:at[0] + ext[0]] = True
+    removed = [int(i + nx * (j + ny * k)) for k, j, i in zip(*np.nonzero(gone))]
+    mesh = Mesh.box_tet(nx, ny, nz, (0.0, 0.0, 0.0), tuple(size), order=order, side_names=("Reflecting",) * 6,
+                        removed=removed, obstacle_name="Reflecting")
+    pre = Precomp(mesh)
+    dt = cfl_dt(pre, C0)
+    sigma = float(h.max())
+
+    def free_point():
+        while True:
+            c = rng.integers(1, np.array(cells) - 1)
+            if not gone[c[2], c[1], c[0]]:
+                return tuple((c + 0.5) * h)
+
+    ic = (0, *free_point(), 2 * sigma ** 2, 1.0)
+    train = [(0, *free_point(), 2 * sigma ** 2, 1.0) for _ in range(ntrain)]
+    return mesh, pre, dt, ic, train

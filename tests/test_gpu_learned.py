@@ -106,3 +106,21 @@ def test_learned_coarse_propagator_beats_the_identity():
     out, it, hist = D.parareal(pre, C0, RHO0, u0, nslices, steps, dt, tol=1e-5, max_iter=nslices, learned=L)
     assert rel(out[0], ref[0]) <= 1e-4
     assert it <= nslices
+    # and after as many iterations as slices it is the serial DG to rounding
+    # (needs a bit-reproducible coarse step: G(U) - G(U) cancels exactly)
+    out, it, _ = D.parareal(pre, C0, RHO0, u0, nslices, steps, dt, tol=0.0, max_iter=nslices, learned=L)
+    assert it == nslices
+    for q in range(4):
+        assert rel(out[q], ref[q]) <= 1e-11
+
+
+def test_learned_coarse_step_is_bit_reproducible():
+    mesh, pre = room(4, 3, 3)
+    dt = D.cfl_dt(pre, C0)
+    L = D.Learned(pre, C0, RHO0, width=64, hidden_layers=2, coarse_steps=1, dt=dt, seed=1)
+    u0 = pre.initial_state([(0, 0.5, 0.5, 0.4, 0.02, 1.0)])
+    L.collect(u0, nsnap=10)
+    L.train(epochs=2, batch=512)
+    a = L.apply(u0, 5)
+    b = L.apply(u0, 5)
+    assert np.array_equal(a, b)
