@@ -86,7 +86,13 @@ struct MixedShape {
     static constexpr int OFF_MAX = OFF_FGEO + ELEMS * NF * 16;
     static constexpr int OFF_TAB = OFF_MAX + MAX_WG * 128 * 4;
     static constexpr int OFF_EB = r16(OFF_TAB + S::NTAB);
-    static constexpr int OFF_BAR = OFF_EB + NPAD * 4;
+    // Overlap (where shared memory allows): the epilogue stages its outputs
+    // in their own region, so that the next tile's A rows can be built while
+    // this tile's MMAs run.
+    static constexpr int OUT_FLOATS = 2 * NQ * ELEMS * NP;
+    static constexpr int OFF_OUT = r16(OFF_EB + NPAD * 4);
+    static constexpr bool OVERLAP = OFF_OUT + OUT_FLOATS * 4 + 16 <= 227 * 1024;
+    static constexpr int OFF_BAR = OVERLAP ? r16(OFF_OUT + OUT_FLOATS * 4) : OFF_EB + NPAD * 4;
     static constexpr int SMEM = OFF_BAR + 16;
     // the epilogue stages the tile's two output arrays in the A-row region
     static_assert(2 * NQ * ELEMS * NP <= 128 * KSTR, "output staging fits in the A-row region");
@@ -144,14 +150,15 @@ __device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
     return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
 }
 
-// Issues the cp.async copies of a tile's connectivity words into buffer cb.
-template <int DIM, int P, int NT>
+// Issues the cp.async copies of a tile's connectivity words into buffer cb;
+// the calling threads take words first, first + stride, ...
+template <int DIM, int P>
 __device__ __forceinline__ void issue_conn_copies(const MixedArgs &a, unsigned char *smem, long long ebase, int cb,
-                                                  int tid) {
+                                                  int first, int stride) {
     using MS = MixedShape<DIM, P>;
     constexpr int NF = MS::NF, ELEMS = MS::ELEMS;
     int2 *sConn = reinterpret_cast<int2 *>(smem + MS::OFF_CONN + cb * MS::CONN_BYTES);
-    for (int idx = tid; idx < ELEMS * NF; idx += NT) {
+    for (int idx = first; idx < ELEMS * NF; idx += stride) {
         const bool ok = ebase + idx / NF < a.K;
         dgtc::cp_async8(&sConn[idx], ok ? &a.conn[ebase * NF + idx] : a.conn, ok ? 8u : 0u);
     }
@@ -159,9 +166,9 @@ __device__ __forceinline__ void issue_conn_copies(const MixedArgs &a, unsigned c
 
 // Issues the cp.async copies of a tile's element data: state, inverse
 // Jacobians and face geometry (zero-filled past K).
-template <int DIM, int P, int NT>
+template <int DIM, int P>
 __device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned char *smem, long long ebase,
-                                                  long long moff, bool vec, int tid) {
+                                                  long long moff, bool vec, int first, int stride) {
     using MS = MixedShape<DIM, P>;
     constexpr int NP = MS::NP, NF = MS::NF, NQ = MS::NQ, ELEMS = MS::ELEMS, QS = MS::QS;
     static_assert(QS == NP, "the state tile is stored unpadded, as in global memory");
@@ -171,23 +178,23 @@ __device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned c
     if (vec && ebase + ELEMS <= a.K) {
         // a whole tile of 16-byte aligned fields: 16-byte copies
         constexpr int W = ELEMS * NP / 4;
-        for (int idx = tid; idx < NQ * W; idx += NT) {
+        for (int idx = first; idx < NQ * W; idx += stride) {
             const int f = idx / W, w = idx - f * W;
             dgtc::cp_async16(&sQ[f * ELEMS * NP + 4 * w], &a.win[moff + f * a.fstride + ebase * NP + 4 * w], 16u);
         }
     } else {
-        for (int idx = tid; idx < NQ * ELEMS * NP; idx += NT) {
+        for (int idx = first; idx < NQ * ELEMS * NP; idx += stride) {
             const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
             const bool ok = ebase + rem / NP < a.K;
             const float *src = ok ? &a.win[moff + f * a.fstride + ebase * NP + rem] : a.win;
             dgtc::cp_async4(&sQ[f * ELEMS * NP + rem], src, ok ? 4u : 0u);
         }
     }
-    for (int idx = tid; idx < ELEMS * DIM * DIM; idx += NT) {
+    for (int idx = first; idx < ELEMS * DIM * DIM; idx += stride) {
         const bool ok = ebase + idx / (DIM * DIM) < a.K;
         dgtc::cp_async4(&sGeo[idx], ok ? &a.geo[ebase * DIM * DIM + idx] : a.geo, ok ? 4u : 0u);
     }
-    for (int idx = tid; idx < ELEMS * NF; idx += NT) {
+    for (int idx = first; idx < ELEMS * NF; idx += stride) {
         const bool ok = ebase + idx / NF < a.K;
         dgtc::cp_async16(&sFgeo[idx], ok ? &a.fgeo[(ebase * NF + idx) * 4] : a.fgeo, ok ? 16u : 0u);
     }
@@ -218,11 +225,120 @@ __device__ __forceinline__ void issue_neighbour_copies(const MixedArgs &a, unsig
     }
 }
 
+// Phase 2: the tile's A rows in shared memory (FP32): contravariant volume
+// fluxes (one task per element node) and the face values negated and scaled
+// by detJf/detJe (one task per face slot), from the tile's state, geometry,
+// connectivity words (buffer cb) and neighbour traces.
+template <int DIM, int P>
+__device__ __forceinline__ void build_rows(const MixedArgs &a, unsigned char *smem, long long ebase, int cb, int first,
+                                           int stride) {
+    using MS = MixedShape<DIM, P>;
+    constexpr int NP = MS::NP, NF = MS::NF, NFP = MS::NFP, NQ = MS::NQ, NSLOT = MS::NSLOT;
+    constexpr int ELEMS = MS::ELEMS, QS = MS::QS, KSTR = MS::KSTR;
+    const float *sQ = reinterpret_cast<const float *>(smem + MS::OFF_Q);
+    float *sA = reinterpret_cast<float *>(smem + MS::OFF_A);
+    const float4 *sNbr = reinterpret_cast<const float4 *>(smem + MS::OFF_NBR);
+    const float *sGeo = reinterpret_cast<const float *>(smem + MS::OFF_GEO);
+    const int2 *sConn = reinterpret_cast<const int2 *>(smem + MS::OFF_CONN + cb * MS::CONN_BYTES);
+    const float4 *sFgeo = reinterpret_cast<const float4 *>(smem + MS::OFF_FGEO);
+    const uint8_t *sFmask = smem + MS::OFF_TAB;
+    // 2a. contravariant fluxes, one task per element node
+    for (int task = first; task < ELEMS * NP; task += stride) {
+        const int le = task / NP, j = task - le * NP;
+        float Bg[DIM][DIM];
+#pragma unroll
+        for (int x = 0; x < DIM; ++x)
+#pragma unroll
+            for (int u = 0; u < DIM; ++u) Bg[x][u] = sGeo[le * DIM * DIM + x * DIM + u];
+        float q[NQ];
+#pragma unroll
+        for (int f = 0; f < NQ; ++f) q[f] = sQ[(f * ELEMS + le) * QS + j];
+#pragma unroll
+        for (int u = 0; u < DIM; ++u) {
+            float au = 0.0f, w = 0.0f;
+#pragma unroll
+            for (int x = 0; x < DIM; ++x) {
+                au = fmaf(Bg[x][u], a.v0[x], au);
+                w = fmaf(Bg[x][u], q[1 + x], w);
+            }
+            sA[(0 * ELEMS + le) * KSTR + u * NP + j] = fmaf(au, q[0], a.rc2 * w);
+            const float pr = a.inv_rho * q[0];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d)
+                sA[((1 + d) * ELEMS + le) * KSTR + u * NP + j] = fmaf(au, q[1 + d], pr * Bg[d][u]);
+        }
+    }
+    // 2b. face values, negated and scaled: -(detJf/detJe) Fn
+    for (int task = first; task < ELEMS * NSLOT; task += stride) {
+        const int le = task / NSLOT, s = task - le * NSLOT;
+        const int lf = s / NFP, k = s - lf * NFP;
+        float Fn[NQ];
+#pragma unroll
+        for (int f = 0; f < NQ; ++f) Fn[f] = 0.0f;
+        float scale = 0.0f;
+        if (ebase + le < a.K) {
+            const int vi = sFmask[lf * NFP + k];
+            float own[NQ];
+#pragma unroll
+            for (int f = 0; f < NQ; ++f) own[f] = sQ[(f * ELEMS + le) * QS + vi];
+            const int2 cn = sConn[le * NF + lf];
+            const float4 g4 = sFgeo[le * NF + lf];
+            const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
+            float n[DIM];
+#pragma unroll
+            for (int x = 0; x < DIM; ++x) n[x] = gg[x];
+            scale = gg[DIM];
+            float vn0 = 0.0f;
+#pragma unroll
+            for (int x = 0; x < DIM; ++x) vn0 = fmaf(a.v0[x], n[x], vn0);
+            const int kind = (cn.y >> 5) & 3;
+            if (kind == kKindInterior) {
+                const float4 o4 = sNbr[task];
+                const float o[4] = {o4.x, o4.y, o4.z, o4.w};
+                const float tau = (cn.y & 128) ? -1.0f : 1.0f;
+                const float sp = own[0] + o[0];
+                float svn = 0.0f;
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) svn = fmaf(own[1 + x] + o[1 + x], n[x], svn);
+                const float hj = a.half_c0 * tau;
+                Fn[0] = fmaf(hj, own[0] - o[0], 0.5f * fmaf(vn0, sp, a.rc2 * svn));
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    Fn[1 + d] = fmaf(hj, own[1 + d] - o[1 + d],
+                                     0.5f * fmaf(vn0, own[1 + d] + o[1 + d], a.inv_rho * sp * n[d]));
+            } else if (kind == kKindReflecting) {
+                float vn = 0.0f;
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
+                float vw[DIM], vwn = 0.0f;
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) {
+                    vw[x] = own[1 + x] - vn * n[x];
+                    vwn = fmaf(vw[x], n[x], vwn);
+                }
+                Fn[0] = fmaf(vn0, own[0], a.rc2 * vwn);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) Fn[1 + d] = fmaf(vn0, vw[d], a.inv_rho * own[0] * n[d]);
+            } else {
+                float vn = 0.0f;
+#pragma unroll
+                for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
+                const float q0 = 0.25f * a.c0;
+                Fn[0] = fmaf(q0, own[0], 0.25f * a.c0 * a.c0 * a.rho * vn);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) Fn[1 + d] = fmaf(0.25f * n[d] * a.inv_rho, own[0], q0 * n[d] * vn);
+            }
+        }
+#pragma unroll
+        for (int f = 0; f < NQ; ++f) sA[(f * ELEMS + le) * KSTR + DIM * NP + s] = -scale * Fn[f];
+    }
+}
+
 template <int DIM, int P, int STAGE, int NWG>
 __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedArgs a) {
     using MS = MixedShape<DIM, P>;
-    constexpr int NP = MS::NP, NF = MS::NF, NFP = MS::NFP, NQ = MS::NQ, NSLOT = MS::NSLOT;
-    constexpr int ELEMS = MS::ELEMS, QS = MS::QS, KTOT = MS::KTOT, KSTEPS = MS::KSTEPS, KSTR = MS::KSTR;
+    constexpr int NP = MS::NP, NQ = MS::NQ;
+    constexpr int ELEMS = MS::ELEMS, KTOT = MS::KTOT, KSTEPS = MS::KSTEPS, KSTR = MS::KSTR;
     constexpr int NPAD = MS::NPAD, ACOLS = MS::ACOLS;
     constexpr int NT = 128 * NWG;                       // threads
     constexpr int KSP = (KSTEPS + NWG - 1) / NWG;       // K-steps sliced per warp group
@@ -231,22 +347,18 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     static_assert(MS::FITS, "tile does not fit in tensor memory");
     static_assert(NWG >= 1 && NWG <= MS::MAX_WG, "warp groups");
     constexpr int NX = MS::NX;
+    constexpr bool OVERLAP = MS::OVERLAP;
     static_assert(NX >= 1, "at least three accumulators");
     static_assert(MS::ACC + (MS::NACC - 1) * NPAD + (NWG - 1) * NPP + 8 * NCH <= MS::TMEM_COLS,
                   "epilogue loads stay inside the allocation");
     extern __shared__ __align__(1024) unsigned char smem[];
-    const float *sQ = reinterpret_cast<const float *>(smem + MS::OFF_Q);
     float *sA = reinterpret_cast<float *>(smem + MS::OFF_A);
-    const float4 *sNbr = reinterpret_cast<const float4 *>(smem + MS::OFF_NBR);
-    const float *sGeo = reinterpret_cast<const float *>(smem + MS::OFF_GEO);
-    const float4 *sFgeo = reinterpret_cast<const float4 *>(smem + MS::OFF_FGEO);
     float *sMax = reinterpret_cast<float *>(smem + MS::OFF_MAX);
     uint8_t *sTab = smem + MS::OFF_TAB;
     int *sEb = reinterpret_cast<int *>(smem + MS::OFF_EB);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + MS::OFF_BAR);
     uint32_t *sTmem = reinterpret_cast<uint32_t *>(smem + MS::OFF_BAR + 8);
     int *sFail = reinterpret_cast<int *>(smem + MS::OFF_BAR + 12);
-    const uint8_t *sFmask = sTab;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0) {
@@ -299,12 +411,27 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     if ((long long)blockIdx.x < ntiles) {
         long long eb, mo;
         tile_base(blockIdx.x, eb, mo);
-        issue_conn_copies<DIM, P, NT>(a, smem, eb, 0, tid);
-        issue_tile_copies<DIM, P, NT>(a, smem, eb, mo, vec, tid);
+        issue_conn_copies<DIM, P>(a, smem, eb, 0, tid, NT);
+        issue_tile_copies<DIM, P>(a, smem, eb, mo, vec, tid, NT);
         dgtc::cp_async_wait_all();
         __syncthreads();
         issue_neighbour_copies<DIM, P>(a, smem, eb, mo, 0, tid, NT);
         dgtc::cp_async_commit();
+        if constexpr (OVERLAP) {
+            // the first tile's rows now; every later tile's while its
+            // predecessor's MMAs run
+            dgtc::cp_async_wait_all();
+            __syncthreads();
+            const long long T1 = (long long)blockIdx.x + gridDim.x;
+            if (T1 < ntiles) {
+                long long e1, m1;
+                tile_base(T1, e1, m1);
+                issue_conn_copies<DIM, P>(a, smem, e1, 1, tid, NT);
+            }
+            dgtc::cp_async_commit();
+            build_rows<DIM, P>(a, smem, eb, 0, tid, NT);
+            __syncthreads();
+        }
     }
     int cb = 0;  // connectivity buffer of the current tile
     for (long long tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x, cb ^= 1) {
@@ -313,104 +440,19 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
         const long long next = tile + gridDim.x;
         long long nebase = 0, nmoff = 0;
         if (next < ntiles) tile_base(next, nebase, nmoff);
-        const int2 *sConn = reinterpret_cast<const int2 *>(smem + MS::OFF_CONN + cb * MS::CONN_BYTES);
-        dgtc::cp_async_wait_all();
-        __syncthreads();
-        if (next < ntiles) issue_conn_copies<DIM, P, NT>(a, smem, nebase, cb ^ 1, tid);
-        dgtc::cp_async_commit();
-        // 2a. contravariant fluxes, one task per element node
-        for (int task = tid; task < ELEMS * NP; task += NT) {
-            const int le = task / NP, j = task - le * NP;
-            float Bg[DIM][DIM];
-#pragma unroll
-            for (int x = 0; x < DIM; ++x)
-#pragma unroll
-                for (int u = 0; u < DIM; ++u) Bg[x][u] = sGeo[le * DIM * DIM + x * DIM + u];
-            float q[NQ];
-#pragma unroll
-            for (int f = 0; f < NQ; ++f) q[f] = sQ[(f * ELEMS + le) * QS + j];
-#pragma unroll
-            for (int u = 0; u < DIM; ++u) {
-                float au = 0.0f, w = 0.0f;
-#pragma unroll
-                for (int x = 0; x < DIM; ++x) {
-                    au = fmaf(Bg[x][u], a.v0[x], au);
-                    w = fmaf(Bg[x][u], q[1 + x], w);
-                }
-                sA[(0 * ELEMS + le) * KSTR + u * NP + j] = fmaf(au, q[0], a.rc2 * w);
-                const float pr = a.inv_rho * q[0];
-#pragma unroll
-                for (int d = 0; d < DIM; ++d)
-                    sA[((1 + d) * ELEMS + le) * KSTR + u * NP + j] = fmaf(au, q[1 + d], pr * Bg[d][u]);
-            }
+        if constexpr (!OVERLAP) {
+            dgtc::cp_async_wait_all();
+            __syncthreads();
+            if (next < ntiles) issue_conn_copies<DIM, P>(a, smem, nebase, cb ^ 1, tid, NT);
+            dgtc::cp_async_commit();
+            build_rows<DIM, P>(a, smem, ebase, cb, tid, NT);
+            __syncthreads();
         }
-        // 2b. face values, negated and scaled: -(detJf/detJe) Fn
-        for (int task = tid; task < ELEMS * NSLOT; task += NT) {
-            const int le = task / NSLOT, s = task - le * NSLOT;
-            const int lf = s / NFP, k = s - lf * NFP;
-            float Fn[NQ];
-#pragma unroll
-            for (int f = 0; f < NQ; ++f) Fn[f] = 0.0f;
-            float scale = 0.0f;
-            if (ebase + le < a.K) {
-                const int vi = sFmask[lf * NFP + k];
-                float own[NQ];
-#pragma unroll
-                for (int f = 0; f < NQ; ++f) own[f] = sQ[(f * ELEMS + le) * QS + vi];
-                const int2 cn = sConn[le * NF + lf];
-                const float4 g4 = sFgeo[le * NF + lf];
-                const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
-                float n[DIM];
-#pragma unroll
-                for (int x = 0; x < DIM; ++x) n[x] = gg[x];
-                scale = gg[DIM];
-                float vn0 = 0.0f;
-#pragma unroll
-                for (int x = 0; x < DIM; ++x) vn0 = fmaf(a.v0[x], n[x], vn0);
-                const int kind = (cn.y >> 5) & 3;
-                if (kind == kKindInterior) {
-                    const float4 o4 = sNbr[task];
-                    const float o[4] = {o4.x, o4.y, o4.z, o4.w};
-                    const float tau = (cn.y & 128) ? -1.0f : 1.0f;
-                    const float sp = own[0] + o[0];
-                    float svn = 0.0f;
-#pragma unroll
-                    for (int x = 0; x < DIM; ++x) svn = fmaf(own[1 + x] + o[1 + x], n[x], svn);
-                    const float hj = a.half_c0 * tau;
-                    Fn[0] = fmaf(hj, own[0] - o[0], 0.5f * fmaf(vn0, sp, a.rc2 * svn));
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d)
-                        Fn[1 + d] = fmaf(hj, own[1 + d] - o[1 + d],
-                                         0.5f * fmaf(vn0, own[1 + d] + o[1 + d], a.inv_rho * sp * n[d]));
-                } else if (kind == kKindReflecting) {
-                    float vn = 0.0f;
-#pragma unroll
-                    for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
-                    float vw[DIM], vwn = 0.0f;
-#pragma unroll
-                    for (int x = 0; x < DIM; ++x) {
-                        vw[x] = own[1 + x] - vn * n[x];
-                        vwn = fmaf(vw[x], n[x], vwn);
-                    }
-                    Fn[0] = fmaf(vn0, own[0], a.rc2 * vwn);
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d) Fn[1 + d] = fmaf(vn0, vw[d], a.inv_rho * own[0] * n[d]);
-                } else {
-                    float vn = 0.0f;
-#pragma unroll
-                    for (int x = 0; x < DIM; ++x) vn = fmaf(own[1 + x], n[x], vn);
-                    const float q0 = 0.25f * a.c0;
-                    Fn[0] = fmaf(q0, own[0], 0.25f * a.c0 * a.c0 * a.rho * vn);
-#pragma unroll
-                    for (int d = 0; d < DIM; ++d) Fn[1 + d] = fmaf(0.25f * n[d] * a.inv_rho, own[0], q0 * n[d] * vn);
-                }
-            }
-#pragma unroll
-            for (int f = 0; f < NQ; ++f) sA[(f * ELEMS + le) * KSTR + DIM * NP + s] = -scale * Fn[f];
-        }
-        __syncthreads();
         // the tile's element data are consumed: start copying the next tile's
-        if (next < ntiles) issue_tile_copies<DIM, P, NT>(a, smem, nebase, nmoff, vec, tid);
+        // (with the overlap, warp 0 copies nothing for the next tile: it only
+        // issues the MMAs while the other warps consume these copies)
+        if (next < ntiles && (!OVERLAP || warp > 0))
+            issue_tile_copies<DIM, P>(a, smem, nebase, nmoff, vec, OVERLAP ? tid - 32 : tid, OVERLAP ? NT - 32 : NT);
         dgtc::cp_async_commit();
         // this thread's connectivity copies of the next tile are complete (only
         // the group just committed may still be pending); the barrier after
@@ -444,7 +486,9 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             sMax[part * 128 + r] = m;
         }
         __syncthreads();
-        if (next < ntiles) issue_neighbour_copies<DIM, P>(a, smem, nebase, nmoff, cb ^ 1, tid, NT);
+        if (next < ntiles && (!OVERLAP || warp > 0))
+            issue_neighbour_copies<DIM, P>(a, smem, nebase, nmoff, cb ^ 1, OVERLAP ? tid - 32 : tid,
+                                           OVERLAP ? NT - 32 : NT);
         dgtc::cp_async_commit();
         float rmax = sMax[r];
 #pragma unroll
@@ -508,6 +552,22 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             dgtc::mma_commit(bar);
         }
         __syncwarp();
+        if constexpr (OVERLAP) {
+            // while warp 0 issues the MMAs and they run, warps 1.. build the
+            // next tile's rows (barrier 1 spans those warps only)
+            if (next < ntiles && warp > 0) {
+                dgtc::cp_async_wait_all();
+                asm volatile("bar.sync 1, %0;" ::"r"(NT - 32) : "memory");
+                const long long next2 = next + gridDim.x;
+                if (next2 < ntiles) {
+                    long long e2, m2;
+                    tile_base(next2, e2, m2);
+                    issue_conn_copies<DIM, P>(a, smem, e2, cb, tid - 32, NT - 32);
+                }
+                build_rows<DIM, P>(a, smem, nebase, cb ^ 1, tid - 32, NT - 32);
+            }
+            dgtc::cp_async_commit();
+        }
 
         // 5. epilogue: accumulators -> stage increment, RK4 stage update;
         //    warp group g takes output nodes [g*NPP, (g+1)*NPP)
@@ -547,8 +607,8 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             }
             // outputs go through shared memory (the A-row region, free since
             // the slicing) so that the global stores are whole-tile vectors
-            float *sO0 = sA;                      // acc, or the new low part
-            float *sO1 = sA + NQ * ELEMS * NP;    // next stage input / new state
+            float *sO0 = OVERLAP ? reinterpret_cast<float *>(smem + MS::OFF_OUT) : sA;  // acc, or the new low part
+            float *sO1 = sO0 + NQ * ELEMS * NP;   // next stage input / new state
             if (row_ok) {
                 const float sdt = live ? a.dt * exp2i(ea - 16) : 0.0f;
 #pragma unroll
