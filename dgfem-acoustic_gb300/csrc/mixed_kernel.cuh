@@ -402,11 +402,15 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     // written back.  Tile T covers element block T / nbatch of batch member
     // T % nbatch (members of one block are adjacent, so the block's geometry
     // is reused from L2).
+    // (tile counts stay below 2^31, checked on the host: 32-bit division,
+    // none at all for a single member)
     const long long ntiles = (long long)((a.K + ELEMS - 1) / ELEMS) * a.nbatch;
+    const unsigned nbu = (unsigned)a.nbatch;
     auto tile_base = [&](long long T, long long &eb, long long &mo) {
-        const long long et = T / a.nbatch;
-        eb = et * ELEMS;
-        mo = (T - et * a.nbatch) * a.bstride;
+        const unsigned t32 = (unsigned)T;
+        const unsigned et = nbu == 1u ? t32 : t32 / nbu;
+        eb = (long long)et * ELEMS;
+        mo = (long long)(t32 - et * nbu) * a.bstride;
     };
     if ((long long)blockIdx.x < ntiles) {
         long long eb, mo;

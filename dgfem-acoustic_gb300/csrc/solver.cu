@@ -408,6 +408,10 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
             if (rc != DG_OK) break;
             // one CTA per SM: each owns the SM's tensor memory
             long long mtiles = (long long)((K + c->mks.elems_per_tile - 1) / c->mks.elems_per_tile) * nbatch;
+            if (mtiles >= (1LL << 31)) {
+                rc = fail(DG_ERR_UNSUPPORTED, "mesh x batch too large for the mixed form's tile index");
+                break;
+            }
             c->grid = (int)std::max(1LL, std::min(mtiles, (long long)nsm));
         }
         if (!fin(cudaStreamSynchronize(c->stream), "sync")) break;
