@@ -51,6 +51,16 @@ struct dg_ctx {
     uint8_t *d_bimg = nullptr;   // sliced operator image
     int *d_beb = nullptr;        // operator row exponents
     int *d_err = nullptr;        // device-side error flag (wait timeouts)
+    // curved elements (per-point form)
+    int curved = 0, cng = 0, cngf = 0;
+    const void *curved_fn = nullptr;
+    size_t curved_smem = 0;
+    int curved_grid = 0;
+    int *d_cel = nullptr, *d_cslot = nullptr;
+    double *d_cminv = nullptr, *d_cwm = nullptr, *d_cwdet = nullptr, *d_cfw = nullptr;
+    double *d_cphi = nullptr, *d_cdphi = nullptr, *d_cfphi = nullptr;
+    int2 *d_cfconn = nullptr;
+    uint8_t *d_cfmap = nullptr;
     // graph cache
     cudaGraphExec_t gexec = nullptr;
     double graph_dt = 0;

@@ -1,4 +1,5 @@
 // C ABI of the host mesh layer (include/dgmesh.h).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -115,6 +116,14 @@ int dgm_get_raw(const dgm_mesh *h, dgm_raw *o) {
     return DG_OK;
 }
 
+int dgm_set_nodes(dgm_mesh *h, const double *xyz) {
+    if (!h || !xyz) return fail(DG_ERR_ARG, "null argument");
+    for (size_t i = 0; i < h->m.xyz.size(); ++i)
+        if (!std::isfinite(xyz[i])) return fail(DG_ERR_ARG, "non-finite node coordinate");
+    std::copy(xyz, xyz + h->m.xyz.size(), h->m.xyz.begin());
+    return DG_OK;
+}
+
 void dgm_free_mesh(dgm_mesh *m) { delete m; }
 
 int dgm_precompute(const dgm_mesh *m, int nbc, const int *tags, const int *refl, dgm_precomp **out) {
@@ -143,6 +152,25 @@ int dgm_get_desc(const dgm_precomp *h, dg_mesh_desc *d) {
     d->el_f_ids = p.el_f_ids.data(); d->el_f_orientation = p.el_f_orient.data();
     d->f_nbr_el_ids = p.f_nbr.data(); d->f_n_to_el_n_ids = p.f_n_to_el_n.data();
     d->f_bc = p.f_bc.data(); d->f_is_boundary = p.f_is_bnd.data();
+    const bool qp = p.ncurved > 0;
+    d->el_num_int_pts = qp ? p.ng : 0;
+    d->el_int_param_coords = qp ? p.el_qp.data() : nullptr;
+    d->el_basis_fcts = qp ? p.el_phi.data() : nullptr;
+    d->el_ugrad_basis_fcts = qp ? p.el_dphi.data() : nullptr;
+    d->el_jacobians_qp = qp ? p.el_jac_qp.data() : nullptr;
+    d->el_jacobian_dets_qp = qp ? p.el_detj_qp.data() : nullptr;
+    d->f_num_int_pts = qp ? p.ngf : 0;
+    d->f_int_param_coords = qp ? p.f_qp.data() : nullptr;
+    d->f_basis_fcts = qp ? p.f_phi.data() : nullptr;
+    d->f_normals_qp = qp ? p.f_normal_qp.data() : nullptr;
+    d->f_jacobian_dets_qp = qp ? p.f_detj_qp.data() : nullptr;
+    return DG_OK;
+}
+
+int dgm_get_curved(const dgm_precomp *h, int *ncurved, const unsigned char **flags) {
+    if (!h || !ncurved) return fail(DG_ERR_ARG, "null argument");
+    *ncurved = h->p.ncurved;
+    if (flags) *flags = h->p.el_curved.data();
     return DG_OK;
 }
 

@@ -1,10 +1,12 @@
-// Reference-semantics mesh precompute for affine simplices.
+// Reference-semantics mesh precompute (affine and curved simplices).
 #include "precompute.h"
 
 #include <algorithm>
 #include <cmath>
 #include <numeric>
 #include <unordered_map>
+
+#include "rules.h"
 
 namespace dg {
 
@@ -52,6 +54,133 @@ struct VecHash {
     }
 };
 
+// Per-point element data (Mesh.cpp:31-38 and the gradient solve at 58-71):
+// at every point g of the Gauss(2p) rule, J = sum_k x_k dphi_k/du (gmsh
+// storage [u*3+x], completed for 2D elements) and its determinant.  The
+// first-point arrays are replaced by the values at point 0.
+template <typename NodeFn>
+std::string element_points(const RawMesh &m, const RefElement &re, NodeFn X, Precomp &P) {
+    const int dim = P.dim, np = P.np, K = P.K;
+    QuadRule r = quad_rule(dim, 2 * P.order);
+    if (r.n == 0) return "no element quadrature rule for this order";
+    const int ng = r.n;
+    P.ng = ng;
+    P.el_qp = r.uvwq;
+    P.el_phi.assign((size_t)ng * np, 0.0);
+    P.el_dphi.assign((size_t)ng * np * 3, 0.0);
+    for (int g = 0; g < ng; ++g)
+        lagrange_eval(dim, P.order, &r.uvwq[g * 4], &P.el_phi[(size_t)g * np], &P.el_dphi[(size_t)g * np * 3]);
+    P.el_jac_qp.assign((size_t)K * ng * 9, 0.0);
+    P.el_detj_qp.assign((size_t)K * ng, 0.0);
+    for (int e = 0; e < K; ++e) {
+        const int *en = &m.el_nodes[(size_t)e * np];
+        for (int g = 0; g < ng; ++g) {
+            double jac[3][3] = {};
+            for (int k = 0; k < np; ++k) {
+                const double *xk = X(en[k]);
+                const double *dk = &P.el_dphi[((size_t)g * np + k) * 3];
+                for (int u = 0; u < dim; ++u)
+                    for (int x = 0; x < 3; ++x) jac[u][x] += xk[x] * dk[u];
+            }
+            double det;
+            if (dim == 2) {
+                double c[3];
+                cross3(jac[0], jac[1], c);
+                det = norm3(c);
+                complete_jacobian(2, jac);
+            } else {
+                double c[3];
+                cross3(jac[1], jac[2], c);
+                det = jac[0][0] * c[0] + jac[0][1] * c[1] + jac[0][2] * c[2];
+            }
+            if (!(det > 0)) return "inverted or degenerate curved element " + std::to_string(e);
+            double *J = &P.el_jac_qp[((size_t)e * ng + g) * 9];
+            for (int u = 0; u < 3; ++u)
+                for (int x = 0; x < 3; ++x) J[u * 3 + x] = jac[u][x];
+            P.el_detj_qp[(size_t)e * ng + g] = det;
+        }
+        for (int k = 0; k < 9; ++k) P.el_jac[(size_t)e * 9 + k] = P.el_jac_qp[(size_t)e * ng * 9 + k];
+        P.el_detj[e] = P.el_detj_qp[(size_t)e * ng];
+    }
+    (void)re;
+    return "";
+}
+
+// Per-point face data (Mesh.cpp:135-194): face Jacobian from all face nodes
+// (completed), determinant, gradients of face basis functions 0 and 1 by the
+// transposed-Jacobian solve, normal = grad0 x grad1 (3D) or grad0 x (0,0,-1)
+// (2D), sign aligned with point 0 as the reference does (3D: the normal at
+// point 0; 2D: grad0 at point 0), normalised.  The first-point face arrays
+// are replaced by the values at point 0.
+template <typename NodeFn>
+std::string face_points(const RefElement &re, NodeFn X, Precomp &P) {
+    const int dim = P.dim, nfp = P.nfp, F = P.F, fdim = dim - 1;
+    QuadRule r = quad_rule(fdim, 2 * P.order);
+    if (r.n == 0) return "no face quadrature rule for this order";
+    const int ngf = r.n;
+    P.ngf = ngf;
+    P.f_qp = r.uvwq;
+    P.f_phi.assign((size_t)ngf * nfp, 0.0);
+    std::vector<double> fd((size_t)ngf * nfp * 3, 0.0);
+    for (int g = 0; g < ngf; ++g)
+        lagrange_eval(fdim, P.order, &r.uvwq[g * 4], &P.f_phi[(size_t)g * nfp], &fd[(size_t)g * nfp * 3]);
+    P.f_normal_qp.assign((size_t)F * ngf * 3, 0.0);
+    P.f_detj_qp.assign((size_t)F * ngf, 0.0);
+    for (int f = 0; f < F; ++f) {
+        const int *fn = &P.f_node_tags[(size_t)f * nfp];
+        double grad0_first[3] = {0, 0, 0};
+        for (int g = 0; g < ngf; ++g) {
+            double jac[3][3] = {};
+            for (int k = 0; k < nfp; ++k) {
+                const double *xk = X(fn[k]);
+                const double *dk = &fd[((size_t)g * nfp + k) * 3];
+                for (int u = 0; u < fdim; ++u)
+                    for (int x = 0; x < 3; ++x) jac[u][x] += xk[x] * dk[u];
+            }
+            double det;
+            if (fdim == 1) {
+                det = norm3(jac[0]);
+            } else {
+                double c[3];
+                cross3(jac[0], jac[1], c);
+                det = norm3(c);
+            }
+            complete_jacobian(fdim, jac);
+            double A[9];
+            for (int rr = 0; rr < dim; ++rr)
+                for (int cc = 0; cc < dim; ++cc) A[rr * dim + cc] = jac[rr][cc];
+            const double *d0 = &fd[((size_t)g * nfp + 0) * 3];
+            const double *d1 = &fd[((size_t)g * nfp + 1) * 3];
+            double g0[3] = {d0[0], fdim == 2 ? d0[1] : 0.0, 0.0};
+            double g1[3] = {d1[0], fdim == 2 ? d1[1] : 0.0, 0.0};
+            if (!lu_solve(A, g0, dim) || !lu_solve(A, g1, dim)) return "singular face Jacobian";
+            double n[3];
+            double *nq = &P.f_normal_qp[((size_t)f * ngf + g) * 3];
+            if (dim == 2) {
+                double z[3] = {0, 0, -1};
+                cross3(g0, z, n);
+                if (g == 0)
+                    for (int x = 0; x < 3; ++x) grad0_first[x] = g0[x];
+                if (g0[0] * grad0_first[0] + g0[1] * grad0_first[1] + g0[2] * grad0_first[2] < 0)
+                    for (int x = 0; x < 3; ++x) n[x] = -n[x];
+            } else {
+                cross3(g0, g1, n);
+                const double *n0 = &P.f_normal_qp[(size_t)f * ngf * 3];
+                if (g != 0 && n0[0] * n[0] + n0[1] * n[1] + n0[2] * n[2] < 0)
+                    for (int x = 0; x < 3; ++x) n[x] = -n[x];
+            }
+            double nn = norm3(n);
+            if (!(nn > 0)) return "degenerate face normal at a quadrature point of face " + std::to_string(f);
+            for (int x = 0; x < 3; ++x) nq[x] = n[x] / nn;
+            P.f_detj_qp[(size_t)f * ngf + g] = det;
+        }
+        for (int x = 0; x < 3; ++x) P.f_normal[(size_t)f * 3 + x] = P.f_normal_qp[(size_t)f * ngf * 3 + x];
+        P.f_detj[f] = P.f_detj_qp[(size_t)f * ngf];
+    }
+    (void)re;
+    return "";
+}
+
 }  // namespace
 
 std::string precompute(const RawMesh &m, const std::vector<std::pair<int, bool>> &physical_bcs, Precomp &P) {
@@ -81,6 +210,7 @@ std::string precompute(const RawMesh &m, const std::vector<std::pair<int, bool>>
     P.el_jac.assign((size_t)K * 9, 0.0);
     P.el_detj.assign(K, 0.0);
     P.dof_xyz.assign((size_t)K * np * 3, 0.0);
+    P.el_curved.assign(K, 0);
     for (int e = 0; e < K; ++e) {
         const int *en = &m.el_nodes[(size_t)e * np];
         const double *x0 = X(en[0]);
@@ -104,17 +234,26 @@ std::string precompute(const RawMesh &m, const std::vector<std::pair<int, bool>>
         if (!(P.el_detj[e] > 0)) return "degenerate or inverted element " + std::to_string(e);
         for (int u = 0; u < 3; ++u)
             for (int k = 0; k < 3; ++k) P.el_jac[(size_t)e * 9 + u * 3 + k] = jac[u][k];
+        // curved: some node is off the affine image of the reference lattice
+        // by more than 1e-11 of the element size
+        double dev = 0;
         for (int i = 0; i < np; ++i) {
             const double *xi = X(en[i]);
-            double dev = 0;
             for (int k = 0; k < 3; ++k) {
                 double a = x0[k];
                 for (int u = 0; u < dim; ++u) a += jac[u][k] * re.r[i * 3 + u];
                 dev = std::max(dev, std::fabs(a - xi[k]));
                 P.dof_xyz[((size_t)e * np + i) * 3 + k] = xi[k];
             }
-            if (dev > 1e-9 * h) return "curved (non-affine) element " + std::to_string(e) + " is not supported";
         }
+        if (dev > 1e-11 * h) {
+            P.el_curved[e] = 1;
+            ++P.ncurved;
+        }
+    }
+    if (P.ncurved > 0) {
+        std::string err = element_points(m, re, X, P);
+        if (!err.empty()) return err;
     }
 
     // Unique faces in first-occurrence order
@@ -210,6 +349,11 @@ std::string precompute(const RawMesh &m, const std::vector<std::pair<int, bool>>
         for (int k = 0; k < 3; ++k) P.f_normal[(size_t)f * 3 + k] = n[k] / nn;
     }
 
+    if (P.ncurved > 0) {
+        std::string err = face_points(re, X, P);
+        if (!err.empty()) return err;
+    }
+
     // Orientation of each element face relative to the face normal
     P.el_f_orient.assign((size_t)K * nf, 1);
     for (int e = 0; e < K; ++e) {
@@ -249,6 +393,8 @@ std::string precompute(const RawMesh &m, const std::vector<std::pair<int, bool>>
             if (P.el_f_ids[(size_t)e0 * nf + lf] != f) continue;
             int o = P.el_f_orient[(size_t)e0 * nf + lf];
             for (int k = 0; k < 3; ++k) P.f_normal[(size_t)f * 3 + k] *= o;
+            for (size_t k = 0; k < (size_t)P.ngf * 3 && P.ncurved > 0; ++k)
+                P.f_normal_qp[(size_t)f * P.ngf * 3 + k] *= o;
             P.el_f_orient[(size_t)e0 * nf + lf] = 1;
         }
     }

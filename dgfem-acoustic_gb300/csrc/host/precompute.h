@@ -1,7 +1,13 @@
 // Reference-semantics mesh precompute: the arrays the reference's Mesh
-// constructor builds (Mesh.cpp:20-435) that its RK4 right-hand side reads,
-// restricted to straight-sided (affine) simplices, where every per-quadrature-
-// point quantity is constant over an element or face and is stored once.
+// constructor builds (Mesh.cpp:20-435) that its RK4 right-hand side reads.
+// On straight-sided (affine) simplices every per-quadrature-point quantity is
+// constant over an element or face and is stored once (at the first point).
+// Elements whose nodes are not the affine image of the reference lattice
+// (curved, isoparametric elements) are counted; when there is at least one,
+// the per-point arrays of the reference (Jacobians and determinants of every
+// element at every point of its Gauss(2p) rule, face normals and determinants
+// at every face point, basis values and gradients) are filled as well, for
+// all elements and faces, in the reference's layouts (Mesh.h:31-108).
 //
 // Semantics kept from the reference:
 //  * unique faces = first occurrence in (element, local face) order, face node
@@ -45,6 +51,19 @@ struct Precomp {
     std::vector<int> f_node_tags;     // [F][nfp]
     std::vector<double> dof_xyz;      // [K*np][3]
     std::vector<int> el_node_tags;    // [K][np]
+    // curved elements
+    int ncurved = 0;
+    std::vector<unsigned char> el_curved;  // [K] node lattice not affine
+    int ng = 0, ngf = 0;                // points of the element / face rules
+    std::vector<double> el_qp;          // [ng][4] u, v, w, weight
+    std::vector<double> el_phi;         // [ng][np]
+    std::vector<double> el_dphi;        // [ng][np][3] d/du, d/dv, d/dw
+    std::vector<double> el_jac_qp;      // [K][ng][9] dx_x/du_u at [u*3+x]
+    std::vector<double> el_detj_qp;     // [K][ng]
+    std::vector<double> f_qp;           // [ngf][4]
+    std::vector<double> f_phi;          // [ngf][nfp]
+    std::vector<double> f_normal_qp;    // [F][ngf][3] after the boundary flip
+    std::vector<double> f_detj_qp;      // [F][ngf]
 };
 
 // physical_bcs: (physical tag, reflecting?) for the boundary groups the

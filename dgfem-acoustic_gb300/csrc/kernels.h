@@ -27,6 +27,9 @@ bool kernels_f64_3d(int order, KernelSet *out);
 bool kernels_f32_2d(int order, KernelSet *out);
 bool kernels_f32_3d(int order, KernelSet *out);
 
+// Per-point stage kernel of curved elements (curved_kernel.cuh); prec as above.
+bool get_curved_kernel(int prec, int dim, const void **fn);
+
 }  // namespace dgk
 
 namespace dgk {

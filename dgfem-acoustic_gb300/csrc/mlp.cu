@@ -744,10 +744,11 @@ int dg_learned_create(const dg_mesh_desc *mesh, const dg_phys_desc *phys, int fl
     L->nout = c->nq * c->np;
     dg::Layout lay;
     std::string err = dg::build_layout(*mesh, flux_sign, lay);
+    if (err.empty() && lay.curved.C > 0) err = "the learned coarse propagator's features assume straight-sided elements";
     if (!err.empty()) {
         dg_destroy(L->fine);
         delete L;
-        return fail(DG_ERR_MESH, err);
+        return fail(lay.curved.C > 0 ? DG_ERR_UNSUPPORTED : DG_ERR_MESH, err);
     }
     double gmax = 0;
     for (double g : lay.geo) gmax = std::max(gmax, std::fabs(g));

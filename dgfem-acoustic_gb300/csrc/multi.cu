@@ -458,6 +458,11 @@ int dg_multi_create(int nmesh, const dg_mesh_desc *meshes, const dg_phys_desc *p
                 rc = fail(DG_ERR_MESH, "mesh " + std::to_string(i) + ": " + err);
                 break;
             }
+            if (lay.curved.C > 0) {
+                rc = fail(DG_ERR_UNSUPPORTED, "mesh " + std::to_string(i) +
+                                                  ": curved elements run in single-mesh contexts (dg_create)");
+                break;
+            }
             dg_multi::Mesh g;
             g.order = meshes[i].order;
             g.np = lay.np;

@@ -16,6 +16,7 @@
 #include "host/layout.h"
 #include "host/refel.h"
 #include "ctx.h"
+#include "curved_kernel.cuh"
 #include "kernels.h"
 #include "stage_kernel.cuh"
 
@@ -61,21 +62,35 @@ __global__ void join_kernel(const float *hi, const float *lo, double *dst, long 
 }
 
 // FP64 monitors: thread per element, u^T M u per field, non-finite count.
+// Curved elements (cslot[e] >= 0) use their own mass matrix, applied as the
+// rule it was summed on: u^T M u = sum_g w detJ(g) u(g)^2.
 template <typename Real>
 __global__ void monitor_kernel(const Real *u, long long fstride, int K, int np, int nq, const double *mass,
                                const double *detj, double rho, double c0, double *out /*[2+nq]*/,
-                               unsigned long long *bad) {
+                               unsigned long long *bad, const int *cslot, const double *cwdet, const double *cphi,
+                               int cng) {
     __shared__ double red[256][5];
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     double loc[5] = {0, 0, 0, 0, 0};
     unsigned long long nbad = 0;
     if (e < K) {
+        const int cs = cslot ? cslot[e] : -1;
         for (int f = 0; f < nq; ++f) {
             const Real *q = u + f * fstride + (long long)e * np;
             double s = 0;
+            for (int i = 0; i < np; ++i)
+                if (!isfinite(double(q[i]))) ++nbad;
+            if (cs >= 0) {
+                for (int g = 0; g < cng; ++g) {
+                    double v = 0;
+                    for (int j = 0; j < np; ++j) v += cphi[g * np + j] * double(q[j]);
+                    s += cwdet[(long long)cs * cng + g] * v * v;
+                }
+                loc[1 + f] = s;
+                continue;
+            }
             for (int i = 0; i < np; ++i) {
                 double qi = double(q[i]);
-                if (!isfinite(qi)) ++nbad;
                 double t = 0;
                 for (int j = 0; j < np; ++j) t += mass[i * np + j] * double(q[j]);
                 s += qi * t;
@@ -121,7 +136,8 @@ void free_ctx(dg_ctx *c) {
                     c->d_t0,    c->d_stage64, c->d_mass,    c->d_detj,    c->d_mon,     c->d_bad,
                     c->d_src_at, c->d_src_off, c->d_src_list, c->d_src_w, c->d_src_params, c->d_ulo,
                     c->d_bimg,  c->d_beb,     c->d_err,     c->d_rec_dof, c->d_trace,   c->d_step0,
-                    c->d_geo32};
+                    c->d_geo32, c->d_cel,     c->d_cslot,   c->d_cminv,   c->d_cwm,     c->d_cwdet,
+                    c->d_cfw,   c->d_cphi,    c->d_cdphi,   c->d_cfphi,   c->d_cfconn,  c->d_cfmap};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -157,7 +173,53 @@ void fill_args(dg_ctx *c, dgk::StageArgs<Real> &a, int stage, double dt) {
     }
 }
 
+cudaError_t launch_affine_stage(dg_ctx *c, int stage, double dt);
+
+template <typename Real>
+cudaError_t launch_curved(dg_ctx *c, int stage, double dt) {
+    dgk::StageArgs<Real> s;
+    fill_args<Real>(c, s, stage, dt);
+    dgk::CurvedArgs<Real> a;
+    a.win = s.win;
+    a.u = s.u;
+    a.acc = s.acc;
+    a.wout = s.wout;
+    a.fstride = c->ndof;
+    a.bstride = c->bstride;
+    a.el = c->d_cel;
+    a.minv = c->d_cminv;
+    a.wm = c->d_cwm;
+    a.fw = c->d_cfw;
+    a.fconn = c->d_cfconn;
+    a.fmap = c->d_cfmap;
+    a.phi = c->d_cphi;
+    a.dphi = c->d_cdphi;
+    a.fphi = c->d_cfphi;
+    a.C = c->curved;
+    a.np = c->np;
+    a.ng = c->cng;
+    a.ngf = c->cngf;
+    a.nfp = c->nfp;
+    a.stage = stage == kEulerStage ? 4 : stage;
+    a.dt = dt;
+    a.rc2 = c->rho0 * c->c0 * c->c0;
+    a.inv_rho = 1.0 / c->rho0;
+    a.half_c0 = 0.5 * c->c0;
+    a.c0 = c->c0;
+    a.rho = c->rho0;
+    for (int k = 0; k < 3; ++k) a.v0[k] = c->v0[k];
+    void *args[] = {&a};
+    return cudaLaunchKernel(c->curved_fn, dim3(c->curved_grid, c->nbatch, 1), dim3(128, 1, 1), args,
+                            c->curved_smem, c->stream);
+}
+
 cudaError_t launch_stage(dg_ctx *c, int stage, double dt) {
+    cudaError_t e = launch_affine_stage(c, stage, dt);
+    if (e != cudaSuccess || c->curved == 0) return e;
+    return c->prec == DG_PREC_FP64 ? launch_curved<double>(c, stage, dt) : launch_curved<float>(c, stage, dt);
+}
+
+cudaError_t launch_affine_stage(dg_ctx *c, int stage, double dt) {
     if (c->mixed) {
         dgk::MixedArgs a;
         dgk::StageArgs<float> s;
@@ -310,6 +372,10 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
     c->c0 = ph->c0; c->rho0 = ph->rho0;
     for (int k = 0; k < 3; ++k) c->v0[k] = ph->v0[k];
     c->mixed = c->prec == DG_PREC_MIXED;
+    if (c->mixed && lay.curved.C > 0) {
+        free_ctx(c);
+        return fail(DG_ERR_UNSUPPORTED, "curved elements run in the fp64 and fp32 forms, not the mixed form");
+    }
     // the mixed form keeps FP32 stage data and uses the FP32 helper kernels
     if (!dgk::get_kernels(c->mixed ? DG_PREC_FP32 : c->prec, dim, m->order, &c->ks)) {
         free_ctx(c);
@@ -413,6 +479,42 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
                 break;
             }
             c->grid = (int)std::max(1LL, std::min(mtiles, (long long)nsm));
+        }
+        if (lay.curved.C > 0) {
+            const dg::CurvedLayout &cv = lay.curved;
+            c->curved = cv.C;
+            c->cng = cv.ng;
+            c->cngf = cv.ngf;
+            if (!dgk::get_curved_kernel(c->prec == DG_PREC_FP64 ? 0 : 1, dim, &c->curved_fn)) {
+                rc = fail(DG_ERR_UNSUPPORTED, "no curved-element kernel for this precision");
+                break;
+            }
+            c->curved_smem = dgk::curved_smem_bytes(dim, np, cv.ng, cv.ngf);
+            if (!fin(cudaFuncSetAttribute(c->curved_fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)c->curved_smem),
+                     "cudaFuncSetAttribute(curved)"))
+                break;
+            auto up = [&](const void *src, size_t bytes, void **dst) -> bool {
+                if (!fin(cudaMalloc(dst, std::max<size_t>(bytes, 16)), "cudaMalloc(curved)")) return false;
+                return fin(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice), "copy curved");
+            };
+            if (!up(cv.el.data(), cv.el.size() * 4, (void **)&c->d_cel)) break;
+            if (!up(cv.slot.data(), cv.slot.size() * 4, (void **)&c->d_cslot)) break;
+            if (!up(cv.minv.data(), cv.minv.size() * 8, (void **)&c->d_cminv)) break;
+            if (!up(cv.wm.data(), cv.wm.size() * 8, (void **)&c->d_cwm)) break;
+            if (!up(cv.wdet.data(), cv.wdet.size() * 8, (void **)&c->d_cwdet)) break;
+            if (!up(cv.fw.data(), cv.fw.size() * 8, (void **)&c->d_cfw)) break;
+            if (!up(cv.phi.data(), cv.phi.size() * 8, (void **)&c->d_cphi)) break;
+            if (!up(cv.dphi.data(), cv.dphi.size() * 8, (void **)&c->d_cdphi)) break;
+            if (!up(cv.fphi.data(), cv.fphi.size() * 8, (void **)&c->d_cfphi)) break;
+            if (!up(cv.fconn.data(), cv.fconn.size() * 4, (void **)&c->d_cfconn)) break;
+            if (!up(cv.fmap.data(), cv.fmap.size(), (void **)&c->d_cfmap)) break;
+            int cper = 0;
+            if (!fin(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cper, c->curved_fn, 128, c->curved_smem),
+                     "occupancy(curved)"))
+                break;
+            const int cres = std::max(cper, 1) * nsm;
+            c->curved_grid = std::max(1, std::min(cv.C, (cres + nbatch - 1) / nbatch));
         }
         if (!fin(cudaStreamSynchronize(c->stream), "sync")) break;
     } while (0);
@@ -810,11 +912,11 @@ int dg_monitors(dg_ctx *c, double *energy, double *l2, long long *status) {
     if (c->prec == DG_PREC_FP64)
         monitor_kernel<double><<<blocks, 256, 0, c->stream>>>((const double *)c->d_u, c->ndof, c->K, c->np, c->nq,
                                                               c->d_mass, c->d_detj, c->rho0, c->c0, c->d_mon,
-                                                              c->d_bad);
+                                                              c->d_bad, c->d_cslot, c->d_cwdet, c->d_cphi, c->cng);
     else
         monitor_kernel<float><<<blocks, 256, 0, c->stream>>>((const float *)c->d_u, c->ndof, c->K, c->np, c->nq,
                                                              c->d_mass, c->d_detj, c->rho0, c->c0, c->d_mon,
-                                                             c->d_bad);
+                                                             c->d_bad, c->d_cslot, c->d_cwdet, c->d_cphi, c->cng);
     CK(cudaGetLastError());
     double h[8];
     unsigned long long bad = 0;
@@ -840,6 +942,14 @@ int dg_info(dg_ctx *c, long long *dofs, int *fields, long long *state_bytes) {
     if (dofs) *dofs = c->ndof;
     if (fields) *fields = c->nq;
     if (state_bytes) *state_bytes = c->bstride * c->nbatch * (long long)c->rsize * 4;
+    return DG_OK;
+}
+
+int dg_curved_info(dg_ctx *c, int *ncurved, int *points, int *face_points) {
+    if (!c) return fail(DG_ERR_ARG, "null context");
+    if (ncurved) *ncurved = c->curved;
+    if (points) *points = c->cng;
+    if (face_points) *face_points = c->cngf;
     return DG_OK;
 }
 

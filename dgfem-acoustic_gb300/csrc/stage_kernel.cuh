@@ -45,7 +45,8 @@ struct Shape {
 
 // Connectivity word of an element face: bits 0-1 neighbour's local face,
 // 2-4 face permutation, 5-6 kind (0 interior, 1 reflecting, 2 absorbing),
-// 7 negative jump sign.
+// 7 negative jump sign, 8 curved element (its update comes from the per-point
+// kernel; the affine kernels skip it).
 enum : int { kKindInterior = 0, kKindReflecting = 1, kKindAbsorbing = 2 };
 enum : int { kStageEuler = 5 };
 
@@ -263,7 +264,8 @@ __device__ __forceinline__ void stage_tile(const StageArgs<Real> &a, long long b
 #pragma unroll
         for (int f = 0; f < NQ; ++f) L[f] = fma(l, fn[f], L[f]);
     }
-    if (valid) {
+    // curved elements (connectivity bit 8) belong to the per-point kernel
+    if (valid && !(__ldg(&a.conn[(long long)e * NF].y) & 256)) {
         Real *acc = a.acc + boff;
         Real *wout = a.wout + boff;
         const Real *uu = a.u + boff;

@@ -66,7 +66,11 @@ class MeshDesc(C.Structure):
                 ("f_num", C.c_int), ("f_num_per_el", C.c_int), ("f_num_nodes", C.c_int), ("fc", C.c_int),
                 ("el_jacobians", P_d), ("el_jacobian_dets", P_d), ("f_normals", P_d), ("f_jacobian_dets", P_d),
                 ("el_f_ids", P_i), ("el_f_orientation", P_i), ("f_nbr_el_ids", P_i), ("f_n_to_el_n_ids", P_i),
-                ("f_bc", P_i), ("f_is_boundary", P_u8)]
+                ("f_bc", P_i), ("f_is_boundary", P_u8),
+                ("el_num_int_pts", C.c_int), ("el_int_param_coords", P_d), ("el_basis_fcts", P_d),
+                ("el_ugrad_basis_fcts", P_d), ("el_jacobians_qp", P_d), ("el_jacobian_dets_qp", P_d),
+                ("f_num_int_pts", C.c_int), ("f_int_param_coords", P_d), ("f_basis_fcts", P_d),
+                ("f_normals_qp", P_d), ("f_jacobian_dets_qp", P_d)]
 
 
 class PhysDesc(C.Structure):
@@ -129,6 +133,9 @@ def _declare(L: C.CDLL) -> None:
         "dg_monitors": (C.c_int, [vp, P_d, P_d, C.POINTER(C.c_longlong)]),
         "dg_synchronize": (C.c_int, [vp]),
         "dg_info": (C.c_int, [vp, C.POINTER(C.c_longlong), P_i, C.POINTER(C.c_longlong)]),
+        "dg_curved_info": (C.c_int, [vp, P_i, P_i, P_i]),
+        "dgm_set_nodes": (C.c_int, [vp, P_d]),
+        "dgm_get_curved": (C.c_int, [vp, P_i, C.POINTER(P_u8)]),
         "dg_host_alloc": (vp, [C.c_ulonglong]),
         "dg_host_free": (None, [vp]),
         "dg_layout_build": (C.c_int, [C.POINTER(MeshDesc), C.c_int, C.POINTER(vp)]),
@@ -253,6 +260,19 @@ class Mesh:
     def write_msh(self, path: str | os.PathLike) -> None:
         _check(lib().dgm_write_msh(self._h, str(path).encode()))
 
+    def set_nodes(self, xyz: np.ndarray) -> None:
+        """Replace every node's coordinates (rows in node_tags order)."""
+        a = np.ascontiguousarray(xyz, dtype=np.float64)
+        if a.shape != (self.raw()["node_tags"].size, 3):
+            raise ValueError("xyz must be [num_nodes][3]")
+        _check(lib().dgm_set_nodes(self._h, _dptr(a)))
+
+    def warp(self, fn) -> "Mesh":
+        """Move every node by fn(xyz) -> xyz' (rows of [num_nodes][3]); a
+        smooth nonlinear fn curves the elements.  Returns self."""
+        self.set_nodes(fn(self.raw()["xyz"].copy()))
+        return self
+
     def raw(self) -> dict:
         v = RawView()
         _check(lib().dgm_get_raw(self._h, C.byref(v)))
@@ -340,6 +360,9 @@ class Precomp:
         self.dim, self.order, self.num_el, self.np = d.dim, d.order, d.num_el, d.el_num_nodes
         self.f_num, self.nf, self.nfp, self.fc = d.f_num, d.f_num_per_el, d.f_num_nodes, d.fc
         self.ndof = self.num_el * self.np
+        n = C.c_int()
+        _check(lib().dgm_get_curved(self._h, C.byref(n), None))
+        self.num_curved = n.value
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
@@ -369,6 +392,28 @@ class Precomp:
             "f_bc": _arr(d.f_bc, F, np.int32),
             "f_is_boundary": _arr(d.f_is_boundary, F, np.uint8),
             "f_node_tags": _arr(tags, F * nfp, np.int32).reshape(F, nfp),
+        }
+
+    def curved_arrays(self) -> dict:
+        """Per-point arrays of a mesh with curved elements (empty otherwise)."""
+        d = self.desc()
+        if d.el_num_int_pts <= 0:
+            return {}
+        K, F, np_, nfp, ng, ngf = d.num_el, d.f_num, d.el_num_nodes, d.f_num_nodes, d.el_num_int_pts, d.f_num_int_pts
+        flags = P_u8()
+        n = C.c_int()
+        _check(lib().dgm_get_curved(self._h, C.byref(n), C.byref(flags)))
+        return {
+            "curved": _arr(flags, K, np.uint8).astype(bool),
+            "el_qp": _arr(d.el_int_param_coords, 4 * ng, np.float64).reshape(ng, 4),
+            "el_phi": _arr(d.el_basis_fcts, ng * np_, np.float64).reshape(ng, np_),
+            "el_dphi": _arr(d.el_ugrad_basis_fcts, ng * np_ * 3, np.float64).reshape(ng, np_, 3),
+            "el_jac": _arr(d.el_jacobians_qp, K * ng * 9, np.float64).reshape(K, ng, 9),
+            "el_detj": _arr(d.el_jacobian_dets_qp, K * ng, np.float64).reshape(K, ng),
+            "f_qp": _arr(d.f_int_param_coords, 4 * ngf, np.float64).reshape(ngf, 4),
+            "f_phi": _arr(d.f_basis_fcts, ngf * nfp, np.float64).reshape(ngf, nfp),
+            "f_normal": _arr(d.f_normals_qp, F * ngf * 3, np.float64).reshape(F, ngf, 3),
+            "f_detj": _arr(d.f_jacobian_dets_qp, F * ngf, np.float64).reshape(F, ngf),
         }
 
     def layout(self, flux: str = "reference") -> dict:
@@ -556,7 +601,10 @@ class Solver:
     def info(self) -> dict:
         d, f, b = C.c_longlong(), C.c_int(), C.c_longlong()
         _check(lib().dg_info(self._h, C.byref(d), C.byref(f), C.byref(b)))
-        return {"dofs_per_field": d.value, "fields": f.value, "state_bytes": b.value}
+        nc, ng, ngf = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().dg_curved_info(self._h, C.byref(nc), C.byref(ng), C.byref(ngf)))
+        return {"dofs_per_field": d.value, "fields": f.value, "state_bytes": b.value, "curved": nc.value,
+                "curved_points": ng.value, "curved_face_points": ngf.value}
 
 
 def min_inradius(pre: Precomp) -> float:

@@ -23,8 +23,9 @@
  * Conventions: 0 = success, negative = error (DG_ERR_*); no exceptions cross
  * the ABI.  A context is not thread-safe; use one per host thread.  The host
  * keeps ownership of every array passed in; dg_create copies what it needs.
- * All element data are for straight-sided (affine) simplices: per-quadrature-
- * point arrays of the reference are passed at their first point only.
+ * Element and face data are passed at the first quadrature point; meshes
+ * with curved (non-affine, isoparametric) elements also pass the reference's
+ * per-quadrature-point arrays (the el_num_int_pts block of dg_mesh_desc).
  */
 #ifndef DGCUDA_H
 #define DGCUDA_H
@@ -74,6 +75,22 @@ typedef struct dg_mesh_desc {
     const int *f_n_to_el_n_ids;      /* [f_num][f_num_nodes][2], -1 for a missing side (Mesh.h:97-99) */
     const int *f_bc;                 /* [f_num]: 1 reflecting, otherwise absorbing (Mesh.h:218) */
     const unsigned char *f_is_boundary; /* [f_num] (Mesh.h:217) */
+    /* Curved elements: the per-point arrays of the reference Mesh on its
+     * Gauss(2p) rules (Mesh.cpp:31-38, 135-194).  Zero / NULL for meshes of
+     * straight-sided elements.  An element whose Jacobian differs between its
+     * points (relative 1e-11) runs the per-point (curved) form; every other
+     * element runs the affine form on its first-point data. */
+    int el_num_int_pts;                  /* m_elNumIntPts */
+    const double *el_int_param_coords;   /* [Ng][4] u, v, w, weight (m_elIntParamCoords) */
+    const double *el_basis_fcts;         /* [Ng][Np] (m_elBasisFcts, Mesh.h:46-48) */
+    const double *el_ugrad_basis_fcts;   /* [Ng][Np][3] (m_elUGradBasisFcts) */
+    const double *el_jacobians_qp;       /* [num_el][Ng][9] dx_x/du_u at [u*3+x] (m_elJacobians, Mesh.h:37-39) */
+    const double *el_jacobian_dets_qp;   /* [num_el][Ng] (m_elJacobianDets) */
+    int f_num_int_pts;                   /* m_fNumIntPts */
+    const double *f_int_param_coords;    /* [Ngf][4] (m_fIntParamCoords) */
+    const double *f_basis_fcts;          /* [Ngf][Nfp] (m_fBasisFcts, Mesh.h:85-87) */
+    const double *f_normals_qp;          /* [f_num][Ngf][3] after the boundary flip (m_fNormals, Mesh.h:88-90) */
+    const double *f_jacobian_dets_qp;    /* [f_num][Ngf] (m_fJacobianDets) */
 } dg_mesh_desc;
 
 /* Mean flow and medium (include/configParser.h:26-28). */
@@ -166,6 +183,10 @@ int dg_synchronize(dg_ctx *ctx);
 /* Sizes and the device data the context holds (for callers that time or
  * inspect it): number of DOFs per field, fields evolved, bytes of state. */
 int dg_info(dg_ctx *ctx, long long *dofs_per_field, int *fields, long long *state_bytes);
+
+/* Curved elements of the context (run by the per-point kernel) and the
+ * points of the element and face rules they use. */
+int dg_curved_info(dg_ctx *ctx, int *ncurved, int *points, int *face_points);
 
 /* Pinned host buffers for fast dg_set_state / dg_get_state. */
 void *dg_host_alloc(unsigned long long bytes);

@@ -56,6 +56,10 @@ int dgm_box_tet(int nx, int ny, int nz, const double lo[3], const double hi[3], 
                 const char *const side_names[6], const int *removed, int nremoved,
                 const char *obstacle_name, dgm_mesh **out);
 int dgm_get_raw(const dgm_mesh *m, dgm_raw *out);
+/* Replace the coordinates of every node (xyz[num_nodes][3], in the order of
+ * dgm_raw.node_tags), e.g. to curve a generated mesh; no counterpart in the
+ * reference, which reads node positions from gmsh. */
+int dgm_set_nodes(dgm_mesh *m, const double *xyz);
 void dgm_free_mesh(dgm_mesh *m);
 
 /* Boundary conditions: physical tags (dimension dim-1) in ascending order,
@@ -63,6 +67,8 @@ void dgm_free_mesh(dgm_mesh *m);
 int dgm_precompute(const dgm_mesh *m, int nbc, const int *bc_phys_tags, const int *bc_reflecting,
                    dgm_precomp **out);
 int dgm_get_desc(const dgm_precomp *p, dg_mesh_desc *out);
+/* Number of curved (non-affine) elements and a per-element flag [num_el]. */
+int dgm_get_curved(const dgm_precomp *p, int *ncurved, const unsigned char **flags);
 int dgm_get_dof_coords(const dgm_precomp *p, const double **xyz); /* [num_el*np][3] */
 int dgm_get_face_node_tags(const dgm_precomp *p, const int **tags); /* [f_num][f_num_nodes] */
 double dgm_min_edge(const dgm_precomp *p);
