@@ -427,6 +427,8 @@ def ours_arm(args, world, rank, local, pg):
         line["uneven_batch"] = uneven_section(D, args, local)
     if world == 1 and not args.no_parareal:
         line["learned_parareal"] = parareal_section(D, args, local)
+    if world == 1 and not args.no_curved:
+        line["curved"] = curved_section(D, args, local)
     print(json.dumps(line), flush=True)
 
 
@@ -525,6 +527,80 @@ def uneven_section(D, args, local):
             "separate_contexts_ms_per_step": sep_ms,
             "one_launch_over_separate": sep_ms / (ms / args.uneven_steps),
             "clocks": clk.summary()}
+
+
+def curved_flops(pre, info) -> float:
+    """Algorithmic flops of one curved element in one stage launch: flux at
+    the element points (interpolation, flux, w detJ J^-T), stiffness
+    contraction, traces of both sides at the face points, face flux,
+    projection on the face basis, inverse mass."""
+    d, np_, nq, nf, nfp = pre.dim, pre.np, pre.dim + 1, pre.nf, pre.nfp
+    ng, ngf = info["curved_points"], info["curved_face_points"]
+    fma = (ng * np_ * nq + ng * (d * nq + d * d * nq) + d * ng * np_ * nq + 2 * nf * ngf * nfp * nq + nf * ngf * 20
+           + nf * nfp * ngf * nq + np_ * np_ * nq)
+    return 2.0 * fma
+
+
+def curved_section(D, args, local):
+    """Curved (isoparametric) elements: unit cube n^3 x 6 tets, order 3, its
+    nodes moved by a smooth map that curves every element ("full") or the
+    elements with x > 1/2 ("half"), against the straight cube; FP64 and FP32
+    contexts; RK4.  Per variant the whole-step rate, and the per-point
+    kernel's device time per launch (CUDA events) with its FP64/FP32
+    arithmetic rate and HBM bytes rate.  CPU baseline: the oracle (per-point
+    form for every element, as the reference) on a smaller fully curved cube."""
+    from dgcuda import workloads as W
+
+    n, steps = args.curved_cells, args.curved_steps
+    out = {"workload": f"unit cube {n}^3 x 6 tets, order 3, absorbing walls, nodes moved by a smooth map "
+                       "(amplitude 0.02) curving all ('full') or half ('half') of the elements; RK4",
+           "unit": UNIT, "variants": []}
+    for kind in ("none", "half", "full"):
+        mesh, pre = W.curved_cube(n, 3, kind)
+        dt = D.cfl_dt(pre, C0)
+        u0 = pre.initial_state([(0, 0.5, 0.5, 0.5, 2 * SIGMA ** 2, 1.0)])
+        units = pre.ndof * 4 * 4
+        for prec in ("fp64", "fp32"):
+            s = D.Solver(pre, C0, RHO0, precision=prec, flux=FLUX, device=local)
+            s.set_state(u0)
+            t = s.rk4_steps(0.0, dt, args.warmup)
+            t, ms = s.rk4_steps_timed(t, dt, steps)
+            _, kt = s.profile_steps(t, dt, 2)
+            info = s.info()
+            v = {"kind": kind, "form": prec, "tets": pre.num_el, "curved": info["curved"],
+                 "value": units * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+                 "affine_kernel_ms_per_launch": sum(kt["stage_ms"]) / max(sum(kt["stage_launches"]), 1)}
+            if kt["curved_launches"]:
+                cms = kt["curved_ms"] / kt["curved_launches"]
+                rb = 8 if prec == "fp64" else 4
+                C, ng, ngf = info["curved"], info["curved_points"], info["curved_face_points"]
+                # per curved element: inverse mass, metric, face data (context precision), state
+                # (stage input, u, acc read; acc, next input written: about 5 values per DOF)
+                nbytes = C * (rb * (pre.np ** 2 + ng * 9 + pre.nf * ngf * 4) + 5 * rb * pre.np * 4)
+                fl = C * curved_flops(pre, info)
+                v.update({"curved_kernel_ms_per_launch": cms,
+                          "curved_kernel_tflops": fl / (cms * 1e-3) / 1e12,
+                          "curved_kernel_gbs": nbytes / (cms * 1e-3) / 1e9,
+                          "curved_kernel_dof_stage_per_s": C * pre.np * 4 / (cms * 1e-3)})
+            out["variants"].append(v)
+            s.close()
+        log(f"[bench] curved {kind}: {pre.num_curved}/{pre.num_el} curved, "
+            + ", ".join(f"{x['form']} {x['value'] / 1e9:.2f} G" for x in out["variants"][-2:]))
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle_py as O
+
+        nc = args.curved_cpu_cells
+        mesh, pre = W.curved_cube(nc, 3, "full")
+        dt = D.cfl_dt(pre, C0)
+        threads = os.cpu_count() or 1
+        orc = O.Oracle(mesh.raw(), dt, C0, RHO0, bcs=mesh.bcs(), upwind=(FLUX == "upwind"), num_threads=threads)
+        orc.set_state(pre.initial_state([(0, 0.5, 0.5, 0.5, 2 * SIGMA ** 2, 1.0)]))
+        _, sec = orc.run(0.0, 2)
+        out["cpu_baseline"] = {"value": pre.ndof * 4 * 4 * 2 / sec, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"fully curved cube {nc}^3 x 6 = {pre.num_el} tets, order 3, 2 RK4 steps, "
+                                         f"{sec:.1f} s"}
+    return out
 
 
 def parareal_section(D, args, local):
@@ -627,10 +703,22 @@ def main():
     ap.add_argument("--parareal-train-steps", type=int, default=100)
     ap.add_argument("--parareal-epochs", type=int, default=10)
     ap.add_argument("--parareal-tol", type=float, default=1e-5)
+    ap.add_argument("--no-curved", action="store_true", help="skip the curved-element section")
+    ap.add_argument("--curved-cells", type=int, default=24)
+    ap.add_argument("--curved-steps", type=int, default=50)
+    ap.add_argument("--curved-cpu-cells", type=int, default=6)
+    ap.add_argument("--curved-only", action="store_true",
+                    help="run the curved-element section alone (profiling case) and print it as one JSON line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least three untimed warm-up steps
     world, rank, local, pg = dist_init()
-    if args.impl == "reference":
+    if args.curved_only:
+        import dgcuda as D
+
+        ensure_built()
+        if rank == 0:
+            print(json.dumps({"curved": curved_section(D, args, local)}), flush=True)
+    elif args.impl == "reference":
         reference_arm(args, world, rank, pg)
     else:
         ours_arm(args, world, rank, local, pg)

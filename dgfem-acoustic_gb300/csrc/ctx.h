@@ -56,9 +56,12 @@ struct dg_ctx {
     const void *curved_fn = nullptr;
     size_t curved_smem = 0;
     int curved_grid = 0;
+    int naff = 0;                 // elements the affine kernels run (all when no element is curved)
+    int *d_aff = nullptr;         // their ids when some element is curved
     int *d_cel = nullptr, *d_cslot = nullptr;
-    double *d_cminv = nullptr, *d_cwm = nullptr, *d_cwdet = nullptr, *d_cfw = nullptr;
-    double *d_cphi = nullptr, *d_cdphi = nullptr, *d_cfphi = nullptr;
+    void *d_cminv = nullptr, *d_cwm = nullptr, *d_cfw = nullptr;   // context precision
+    void *d_cphi = nullptr, *d_cdphi = nullptr, *d_cfphi = nullptr;
+    double *d_cwdet = nullptr, *d_cphi64 = nullptr;                // FP64, for the monitors
     int2 *d_cfconn = nullptr;
     uint8_t *d_cfmap = nullptr;
     // graph cache

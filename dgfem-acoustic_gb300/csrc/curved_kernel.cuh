@@ -1,7 +1,7 @@
 // Stage kernel of curved (non-affine, isoparametric) elements: the per-point
 // form of the reference's right-hand side, with geometry that varies inside
-// an element.  One CTA per curved element (grid-stride), FP64 arithmetic,
-// stage data of the context's precision.  Per element:
+// an element.  One CTA per curved element (grid-stride), arithmetic and
+// element data in the context's precision (FP64 or FP32).  Per element:
 //
 //   volume  U(g) = sum_j phi_j(g) q_j at the points g of the element rule,
 //           Fc_u(g) = sum_x [w detJ J^-T]_(x,u)(g) Flux_x(U(g)),
@@ -20,7 +20,7 @@
 //           called at solver.cpp:46-48), then the RK4 / forward-Euler stage
 //           combination of the affine kernels.
 //
-// The affine stage kernels skip these elements (connectivity bit 8), and both
+// The affine stage kernels run over the list of the other elements, and both
 // kernels read only stage inputs and write only their own elements, so the two
 // launches of a stage are independent.
 #pragma once
@@ -39,68 +39,68 @@ struct CurvedArgs {
     Real *wout;
     long long fstride, bstride;
     const int *el;         // [C] element ids
-    const double *minv;    // [C][np*np] row-major inverse mass (applied as its transpose, as linEq)
-    const double *wm;      // [C][ng][DIM*DIM] w detJ J^-T at x*DIM+u
-    const double *fw;      // [C][NF][ngf][4] outward normal, w detJf
+    const Real *minv;      // [C][np*np] row-major inverse mass (applied as its transpose, as linEq)
+    const Real *wm;        // [C][ng][DIM*DIM] w detJ J^-T at x*DIM+u
+    const Real *fw;        // [C][NF][ngf][4] outward normal, w detJf
     const int2 *fconn;     // [C][NF] neighbour (-1), word: kind bits 5-6, jump sign bit 7
     const uint8_t *fmap;   // [C][NF][2][nfp] own / neighbour element node of face node k
-    const double *phi;     // [ng][np]
-    const double *dphi;    // [DIM][ng][np]
-    const double *fphi;    // [ngf][nfp]
+    const Real *phi;       // [ng][np]
+    const Real *dphi;      // [DIM][ng][np]
+    const Real *fphi;      // [ngf][nfp]
     int C, np, ng, ngf, nfp;
     int stage;             // 0-3 RK4 stages, 4 forward Euler
-    double dt, rc2, inv_rho, half_c0, c0, rho, v0[3];
+    Real dt, rc2, inv_rho, half_c0, c0, rho, v0[3];
 };
 
-// Shared memory (doubles unless noted) for an element of np nodes.
-__host__ __device__ inline size_t curved_smem_bytes(int dim, int np, int ng, int ngf) {
+// Shared memory for an element of np nodes (rsize = bytes of the arithmetic type).
+__host__ __device__ inline size_t curved_smem_bytes(int dim, int np, int ng, int ngf, int rsize) {
     const int nq = dim + 1, nf = dim + 1;
     size_t d = (size_t)nq * np        // state
                + (size_t)ng * dim * nq  // contravariant flux at the points
                + (size_t)nf * ngf * nq  // weighted numerical flux at the face points
                + (size_t)nq * np;       // S - F
-    return d * sizeof(double) + (size_t)nf * np * sizeof(int);
+    return d * rsize + (size_t)nf * np * sizeof(int);
 }
 
 // Physical flux of the linearised Euler equations with uniform mean flow
 // (Mesh.cpp:577-592): F[x][0] = v0_x p + rho c0^2 v_x, F[x][1+d] = v0_x v_d +
 // delta_xd p / rho.
-template <int DIM>
-__device__ __forceinline__ void lee_flux(const double *q, const double *v0, double rc2, double inv_rho,
-                                         double (&F)[DIM][DIM + 1]) {
+template <int DIM, typename Real>
+__device__ __forceinline__ void lee_flux(const Real *q, const Real *v0, Real rc2, Real inv_rho,
+                                         Real (&F)[DIM][DIM + 1]) {
 #pragma unroll
     for (int x = 0; x < DIM; ++x) {
         F[x][0] = fma(v0[x], q[0], rc2 * q[1 + x]);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) F[x][1 + d] = v0[x] * q[1 + d] + (x == d ? q[0] * inv_rho : 0.0);
+        for (int d = 0; d < DIM; ++d) F[x][1 + d] = v0[x] * q[1 + d] + (x == d ? q[0] * inv_rho : Real(0));
     }
 }
 
 // Normal numerical flux at one face point seen from the element (outward
 // normal n): interior Lax-Friedrichs with jump sign tau, reflecting wall
 // (normal velocity removed, flux projected), absorbing (R K R^-1 q).
-template <int DIM>
-__device__ __forceinline__ void face_flux(int kind, double tau, const double *own, const double *o, const double *n,
-                                          double rc2, double inv_rho, double half_c0, double c0, double rho,
-                                          const double *v0, double (&Fn)[DIM + 1]) {
-    double vn0 = 0;
+template <int DIM, typename Real>
+__device__ __forceinline__ void face_flux(int kind, Real tau, const Real *own, const Real *o, const Real *n,
+                                          Real rc2, Real inv_rho, Real half_c0, Real c0, Real rho,
+                                          const Real *v0, Real (&Fn)[DIM + 1]) {
+    Real vn0 = Real(0);
 #pragma unroll
     for (int x = 0; x < DIM; ++x) vn0 = fma(v0[x], n[x], vn0);
     if (kind == kKindInterior) {
-        const double sp = own[0] + o[0];
-        double svn = 0;
+        const Real sp = own[0] + o[0];
+        Real svn = Real(0);
 #pragma unroll
         for (int x = 0; x < DIM; ++x) svn = fma(own[1 + x] + o[1 + x], n[x], svn);
-        const double hj = half_c0 * tau;
-        Fn[0] = fma(hj, own[0] - o[0], 0.5 * fma(vn0, sp, rc2 * svn));
+        const Real hj = half_c0 * tau;
+        Fn[0] = fma(hj, own[0] - o[0], Real(0.5) * fma(vn0, sp, rc2 * svn));
 #pragma unroll
         for (int d = 0; d < DIM; ++d)
-            Fn[1 + d] = fma(hj, own[1 + d] - o[1 + d], 0.5 * fma(vn0, own[1 + d] + o[1 + d], inv_rho * sp * n[d]));
+            Fn[1 + d] = fma(hj, own[1 + d] - o[1 + d], Real(0.5) * fma(vn0, own[1 + d] + o[1 + d], inv_rho * sp * n[d]));
     } else if (kind == kKindReflecting) {
-        double vn = 0;
+        Real vn = Real(0);
 #pragma unroll
         for (int x = 0; x < DIM; ++x) vn = fma(own[1 + x], n[x], vn);
-        double vw[DIM], vwn = 0;
+        Real vw[DIM], vwn = Real(0);
 #pragma unroll
         for (int x = 0; x < DIM; ++x) {
             vw[x] = own[1 + x] - vn * n[x];
@@ -110,13 +110,13 @@ __device__ __forceinline__ void face_flux(int kind, double tau, const double *ow
 #pragma unroll
         for (int d = 0; d < DIM; ++d) Fn[1 + d] = fma(vn0, vw[d], inv_rho * own[0] * n[d]);
     } else {
-        double vn = 0;
+        Real vn = Real(0);
 #pragma unroll
         for (int x = 0; x < DIM; ++x) vn = fma(own[1 + x], n[x], vn);
-        const double q0 = 0.25 * c0;
-        Fn[0] = fma(q0, own[0], 0.25 * c0 * c0 * rho * vn);
+        const Real q0 = Real(0.25) * c0;
+        Fn[0] = fma(q0, own[0], Real(0.25) * c0 * c0 * rho * vn);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) Fn[1 + d] = fma(0.25 * n[d] * inv_rho, own[0], q0 * n[d] * vn);
+        for (int d = 0; d < DIM; ++d) Fn[1 + d] = fma(Real(0.25) * n[d] * inv_rho, own[0], q0 * n[d] * vn);
     }
 }
 
@@ -125,21 +125,21 @@ __global__ void __launch_bounds__(128) curved_stage_kernel(const CurvedArgs<Real
     constexpr int NQ = DIM + 1, NF = DIM + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int np = a.np, ng = a.ng, ngf = a.ngf, nfp = a.nfp;
-    double *sW = reinterpret_cast<double *>(smem_raw);  // [NQ][np]
-    double *sFc = sW + NQ * np;                          // [ng][DIM][NQ]
-    double *sFn = sFc + ng * DIM * NQ;                   // [NF][ngf][NQ]
-    double *sR = sFn + NF * ngf * NQ;                    // [NQ][np]
+    Real *sW = reinterpret_cast<Real *>(smem_raw);  // [NQ][np]
+    Real *sFc = sW + NQ * np;                        // [ng][DIM][NQ]
+    Real *sFn = sFc + ng * DIM * NQ;                 // [NF][ngf][NQ]
+    Real *sR = sFn + NF * ngf * NQ;                  // [NQ][np]
     int *sK = reinterpret_cast<int *>(sR + NQ * np);     // [NF][np] face position of node i, or -1
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long boff = (long long)blockIdx.y * a.bstride;
     const Real *win = a.win + boff;
-    const double v0[3] = {a.v0[0], a.v0[1], a.v0[2]};
+    const Real v0[3] = {a.v0[0], a.v0[1], a.v0[2]};
     for (int c = blockIdx.x; c < a.C; c += gridDim.x) {
         const int e = a.el[c];
         const long long ebase = (long long)e * np;
         for (int t = tid; t < NQ * np; t += nt) {
             const int q = t / np, i = t - q * np;
-            sW[t] = double(win[q * a.fstride + ebase + i]);
+            sW[t] = win[q * a.fstride + ebase + i];
         }
         for (int t = tid; t < NF * np; t += nt) sK[t] = -1;
         __syncthreads();
@@ -153,23 +153,23 @@ __global__ void __launch_bounds__(128) curved_stage_kernel(const CurvedArgs<Real
         for (int t = tid; t < nwork; t += nt) {
             if (t < ng) {
                 const int g = t;
-                double U[NQ];
+                Real U[NQ];
 #pragma unroll
-                for (int q = 0; q < NQ; ++q) U[q] = 0;
-                const double *ph = a.phi + (size_t)g * np;
+                for (int q = 0; q < NQ; ++q) U[q] = Real(0);
+                const Real *ph = a.phi + (size_t)g * np;
                 for (int j = 0; j < np; ++j) {
-                    const double p = __ldg(ph + j);
+                    const Real p = __ldg(ph + j);
 #pragma unroll
                     for (int q = 0; q < NQ; ++q) U[q] = fma(p, sW[q * np + j], U[q]);
                 }
-                double F[DIM][DIM + 1];
-                lee_flux<DIM>(U, v0, a.rc2, a.inv_rho, F);
-                const double *w = a.wm + ((size_t)c * ng + g) * DIM * DIM;
+                Real F[DIM][DIM + 1];
+                lee_flux<DIM, Real>(U, v0, a.rc2, a.inv_rho, F);
+                const Real *w = a.wm + ((size_t)c * ng + g) * DIM * DIM;
 #pragma unroll
                 for (int u = 0; u < DIM; ++u)
 #pragma unroll
                     for (int q = 0; q < NQ; ++q) {
-                        double s = 0;
+                        Real s = Real(0);
 #pragma unroll
                         for (int x = 0; x < DIM; ++x) s = fma(__ldg(w + x * DIM + u), F[x][q], s);
                         sFc[(g * DIM + u) * NQ + q] = s;
@@ -178,32 +178,32 @@ __global__ void __launch_bounds__(128) curved_stage_kernel(const CurvedArgs<Real
                 const int lf = (t - ng) / ngf, g = (t - ng) - lf * ngf;
                 const int2 cn = a.fconn[(size_t)c * NF + lf];
                 const int kind = (cn.y >> 5) & 3;
-                const double tau = (cn.y & 128) ? -1.0 : 1.0;
+                const Real tau = (cn.y & 128) ? Real(-1) : Real(1);
                 const uint8_t *own = fmap + (lf * 2) * nfp;
                 const uint8_t *nbm = own + nfp;
-                const double *fp = a.fphi + (size_t)g * nfp;
-                double qi[NQ], qo[NQ];
+                const Real *fp = a.fphi + (size_t)g * nfp;
+                Real qi[NQ], qo[NQ];
 #pragma unroll
-                for (int q = 0; q < NQ; ++q) { qi[q] = 0; qo[q] = 0; }
+                for (int q = 0; q < NQ; ++q) { qi[q] = Real(0); qo[q] = Real(0); }
                 const long long nbase = (long long)(kind == kKindInterior ? cn.x : 0) * np;
                 for (int k = 0; k < nfp; ++k) {
-                    const double p = __ldg(fp + k);
+                    const Real p = __ldg(fp + k);
                     const int vi = own[k];
 #pragma unroll
                     for (int q = 0; q < NQ; ++q) qi[q] = fma(p, sW[q * np + vi], qi[q]);
                     if (kind == kKindInterior) {
                         const long long at = nbase + nbm[k];
 #pragma unroll
-                        for (int q = 0; q < NQ; ++q) qo[q] = fma(p, double(__ldg(win + q * a.fstride + at)), qo[q]);
+                        for (int q = 0; q < NQ; ++q) qo[q] = fma(p, __ldg(win + q * a.fstride + at), qo[q]);
                     }
                 }
-                const double *fw = a.fw + (((size_t)c * NF + lf) * ngf + g) * 4;
-                double n[DIM];
+                const Real *fw = a.fw + (((size_t)c * NF + lf) * ngf + g) * 4;
+                Real n[DIM];
 #pragma unroll
                 for (int x = 0; x < DIM; ++x) n[x] = __ldg(fw + x);
-                const double wj = __ldg(fw + 3);
-                double Fn[NQ];
-                face_flux<DIM>(kind, tau, qi, qo, n, a.rc2, a.inv_rho, a.half_c0, a.c0, a.rho, v0, Fn);
+                const Real wj = __ldg(fw + 3);
+                Real Fn[NQ];
+                face_flux<DIM, Real>(kind, tau, qi, qo, n, a.rc2, a.inv_rho, a.half_c0, a.c0, a.rho, v0, Fn);
 #pragma unroll
                 for (int q = 0; q < NQ; ++q) sFn[(lf * ngf + g) * NQ + q] = wj * Fn[q];
             }
@@ -212,18 +212,18 @@ __global__ void __launch_bounds__(128) curved_stage_kernel(const CurvedArgs<Real
         // S - F at the nodes
         for (int t = tid; t < NQ * np; t += nt) {
             const int q = t / np, i = t - q * np;
-            double S = 0;
+            Real S = Real(0);
 #pragma unroll
             for (int u = 0; u < DIM; ++u) {
-                const double *dp = a.dphi + (size_t)u * ng * np + i;
+                const Real *dp = a.dphi + (size_t)u * ng * np + i;
                 for (int g = 0; g < ng; ++g) S = fma(__ldg(dp + (size_t)g * np), sFc[(g * DIM + u) * NQ + q], S);
             }
-            double Fl = 0;
+            Real Fl = Real(0);
 #pragma unroll
             for (int lf = 0; lf < NF; ++lf) {
                 const int k = sK[lf * np + i];
                 if (k < 0) continue;
-                double s = 0;
+                Real s = Real(0);
                 for (int g = 0; g < ngf; ++g) s = fma(__ldg(a.fphi + (size_t)g * nfp + k), sFn[(lf * ngf + g) * NQ + q], s);
                 Fl += s;
             }
@@ -231,16 +231,16 @@ __global__ void __launch_bounds__(128) curved_stage_kernel(const CurvedArgs<Real
         }
         __syncthreads();
         // r = dt M^-1 (S - F) and the stage update
-        const double *mi = a.minv + (size_t)c * np * np;
+        const Real *mi = a.minv + (size_t)c * np * np;
         Real *acc = a.acc + boff;
         Real *wout = a.wout + boff;
         const Real *uu = a.u + boff;
         for (int t = tid; t < NQ * np; t += nt) {
             const int q = t / np, i = t - q * np;
-            double s = 0;
+            Real s = Real(0);
             for (int j = 0; j < np; ++j) s = fma(__ldg(mi + (size_t)j * np + i), sR[q * np + j], s);
-            const Real r = Real(a.dt * s);
-            const Real qv = Real(sW[q * np + i]);
+            const Real r = a.dt * s;
+            const Real qv = sW[q * np + i];
             const long long idx = q * a.fstride + ebase + i;
             if (a.stage == 0) {
                 acc[idx] = r;

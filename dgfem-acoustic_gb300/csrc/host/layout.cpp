@@ -121,9 +121,9 @@ std::string build_curved(const dg_mesh_desc &m, int flux_sign, const RefElement 
             cn[0] = nb;
             cn[1] = tau < 0 ? 128 : 0;
         }
-        // the affine kernels skip this element
-        for (int lf = 0; lf < nf; ++lf) L.conn[((size_t)e * nf + lf) * 2 + 1] |= 256;
     }
+    for (int e = 0; e < K; ++e)
+        if (Cv.slot[e] < 0) Cv.affine.push_back(e);
     (void)re;
     return "";
 }
@@ -131,8 +131,7 @@ std::string build_curved(const dg_mesh_desc &m, int flux_sign, const RefElement 
 }  // namespace
 
 // connectivity word (see stage_kernel.cuh): bits 0-1 neighbour's local face,
-// 2-4 permutation, 5-6 kind (0 interior, 1 reflecting, 2 absorbing), 7 tau<0,
-// 8 curved element (left to the per-point form)
+// 2-4 permutation, 5-6 kind (0 interior, 1 reflecting, 2 absorbing), 7 tau<0
 std::string build_layout(const dg_mesh_desc &m, int flux_sign, Layout &L) {
     if (m.dim != 2 && m.dim != 3) return "dimension must be 2 or 3";
     if (m.order < 1 || m.order > 5) return "order must be in 1..5";

@@ -2,9 +2,9 @@
 // (dg_mesh_desc): per element the inverse Jacobian, per element face the
 // outward normal, detJf/detJe, neighbour, neighbour's local face, face
 // permutation, boundary kind and jump sign; plus the reference-element
-// operators and tables the stage kernels keep in shared memory.  Curved
-// elements get their connectivity words marked (bit 8) so that the affine
-// kernels leave them to the per-point form.
+// operators and tables the stage kernels keep in shared memory.  Meshes with
+// curved elements also get the list of the straight-sided ones, which the
+// affine kernels run over, leaving the curved ones to the per-point form.
 #pragma once
 #include <cstdint>
 #include <string>
@@ -23,6 +23,7 @@ struct CurvedLayout {
     int C = 0, ng = 0, ngf = 0;
     std::vector<int> el;          // [C] element ids, ascending
     std::vector<int> slot;        // [K] position in el, or -1
+    std::vector<int> affine;      // the other elements, ascending
     std::vector<double> minv;     // [C][np*np] inverse mass, row-major as the reference stores it
     std::vector<double> wm;       // [C][ng][dim*dim] w detJ J^-T at x*dim+u
     std::vector<double> wdet;     // [C][ng] w detJ

@@ -137,7 +137,8 @@ void free_ctx(dg_ctx *c) {
                     c->d_src_at, c->d_src_off, c->d_src_list, c->d_src_w, c->d_src_params, c->d_ulo,
                     c->d_bimg,  c->d_beb,     c->d_err,     c->d_rec_dof, c->d_trace,   c->d_step0,
                     c->d_geo32, c->d_cel,     c->d_cslot,   c->d_cminv,   c->d_cwm,     c->d_cwdet,
-                    c->d_cfw,   c->d_cphi,    c->d_cdphi,   c->d_cfphi,   c->d_cfconn,  c->d_cfmap};
+                    c->d_cfw,   c->d_cphi,    c->d_cdphi,   c->d_cfphi,   c->d_cfconn,  c->d_cfmap,
+                    c->d_cphi64, c->d_aff};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -153,7 +154,8 @@ void fill_args(dg_ctx *c, dgk::StageArgs<Real> &a, int stage, double dt) {
     a.conn = c->d_conn;
     a.ops = reinterpret_cast<const Real *>(c->d_ops);
     a.tabs = c->d_tabs;
-    a.K = c->K;
+    a.elist = c->d_aff;
+    a.K = c->naff;
     a.dt = Real(dt);
     a.rc2 = Real(c->rho0 * c->c0 * c->c0);
     a.inv_rho = Real(1.0 / c->rho0);
@@ -187,27 +189,27 @@ cudaError_t launch_curved(dg_ctx *c, int stage, double dt) {
     a.fstride = c->ndof;
     a.bstride = c->bstride;
     a.el = c->d_cel;
-    a.minv = c->d_cminv;
-    a.wm = c->d_cwm;
-    a.fw = c->d_cfw;
+    a.minv = static_cast<const Real *>(c->d_cminv);
+    a.wm = static_cast<const Real *>(c->d_cwm);
+    a.fw = static_cast<const Real *>(c->d_cfw);
     a.fconn = c->d_cfconn;
     a.fmap = c->d_cfmap;
-    a.phi = c->d_cphi;
-    a.dphi = c->d_cdphi;
-    a.fphi = c->d_cfphi;
+    a.phi = static_cast<const Real *>(c->d_cphi);
+    a.dphi = static_cast<const Real *>(c->d_cdphi);
+    a.fphi = static_cast<const Real *>(c->d_cfphi);
     a.C = c->curved;
     a.np = c->np;
     a.ng = c->cng;
     a.ngf = c->cngf;
     a.nfp = c->nfp;
     a.stage = stage == kEulerStage ? 4 : stage;
-    a.dt = dt;
-    a.rc2 = c->rho0 * c->c0 * c->c0;
-    a.inv_rho = 1.0 / c->rho0;
-    a.half_c0 = 0.5 * c->c0;
-    a.c0 = c->c0;
-    a.rho = c->rho0;
-    for (int k = 0; k < 3; ++k) a.v0[k] = c->v0[k];
+    a.dt = s.dt;
+    a.rc2 = s.rc2;
+    a.inv_rho = s.inv_rho;
+    a.half_c0 = s.half_c0;
+    a.c0 = s.c0;
+    a.rho = s.rho;
+    for (int k = 0; k < 3; ++k) a.v0[k] = s.v0[k];
     void *args[] = {&a};
     return cudaLaunchKernel(c->curved_fn, dim3(c->curved_grid, c->nbatch, 1), dim3(128, 1, 1), args,
                             c->curved_smem, c->stream);
@@ -372,6 +374,7 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
     c->c0 = ph->c0; c->rho0 = ph->rho0;
     for (int k = 0; k < 3; ++k) c->v0[k] = ph->v0[k];
     c->mixed = c->prec == DG_PREC_MIXED;
+    c->naff = lay.curved.C > 0 ? (int)lay.curved.affine.size() : K;
     if (c->mixed && lay.curved.C > 0) {
         free_ctx(c);
         return fail(DG_ERR_UNSUPPORTED, "curved elements run in the fp64 and fp32 forms, not the mixed form");
@@ -443,7 +446,7 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
                  "occupancy"))
             break;
         if (!fin(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device), "attribute")) break;
-        int ntiles = (K + c->ks.epb - 1) / c->ks.epb;
+        int ntiles = std::max(1, (c->naff + c->ks.epb - 1) / c->ks.epb);
         // resident blocks spread over the members (grid.y = member)
         const int resident = std::max(per_sm, 1) * nsm;
         c->grid = std::max(1, std::min(ntiles, (resident + nbatch - 1) / nbatch));
@@ -489,7 +492,7 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
                 rc = fail(DG_ERR_UNSUPPORTED, "no curved-element kernel for this precision");
                 break;
             }
-            c->curved_smem = dgk::curved_smem_bytes(dim, np, cv.ng, cv.ngf);
+            c->curved_smem = dgk::curved_smem_bytes(dim, np, cv.ng, cv.ngf, (int)c->rsize);
             if (!fin(cudaFuncSetAttribute(c->curved_fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)c->curved_smem),
                      "cudaFuncSetAttribute(curved)"))
@@ -500,13 +503,21 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
             };
             if (!up(cv.el.data(), cv.el.size() * 4, (void **)&c->d_cel)) break;
             if (!up(cv.slot.data(), cv.slot.size() * 4, (void **)&c->d_cslot)) break;
-            if (!up(cv.minv.data(), cv.minv.size() * 8, (void **)&c->d_cminv)) break;
-            if (!up(cv.wm.data(), cv.wm.size() * 8, (void **)&c->d_cwm)) break;
+            // element data in the context's precision; FP64 copies for the monitors
+            auto upr = [&](const std::vector<double> &v, void **dst) -> bool {
+                if (c->prec == DG_PREC_FP64) return up(v.data(), v.size() * 8, dst);
+                std::vector<float> f(v.begin(), v.end());
+                return up(f.data(), f.size() * 4, dst);
+            };
+            if (!upr(cv.minv, &c->d_cminv)) break;
+            if (!upr(cv.wm, &c->d_cwm)) break;
+            if (!upr(cv.fw, &c->d_cfw)) break;
+            if (!upr(cv.phi, &c->d_cphi)) break;
+            if (!upr(cv.dphi, &c->d_cdphi)) break;
+            if (!upr(cv.fphi, &c->d_cfphi)) break;
             if (!up(cv.wdet.data(), cv.wdet.size() * 8, (void **)&c->d_cwdet)) break;
-            if (!up(cv.fw.data(), cv.fw.size() * 8, (void **)&c->d_cfw)) break;
-            if (!up(cv.phi.data(), cv.phi.size() * 8, (void **)&c->d_cphi)) break;
-            if (!up(cv.dphi.data(), cv.dphi.size() * 8, (void **)&c->d_cdphi)) break;
-            if (!up(cv.fphi.data(), cv.fphi.size() * 8, (void **)&c->d_cfphi)) break;
+            if (!up(cv.phi.data(), cv.phi.size() * 8, (void **)&c->d_cphi64)) break;
+            if (!up(cv.affine.data(), cv.affine.size() * 4, (void **)&c->d_aff)) break;
             if (!up(cv.fconn.data(), cv.fconn.size() * 4, (void **)&c->d_cfconn)) break;
             if (!up(cv.fmap.data(), cv.fmap.size(), (void **)&c->d_cfmap)) break;
             int cper = 0;
@@ -864,13 +875,13 @@ int dg_profile_steps(dg_ctx *c, double *t, double dt, int nsteps, dg_kernel_time
     std::memset(out, 0, sizeof(*out));
     if (nsteps == 0) return DG_OK;
     // a pair of events around every launch
-    size_t need = (size_t)nsteps * 5 * 2;
+    size_t need = (size_t)nsteps * 9 * 2;
     while (c->events.size() < need) {
         cudaEvent_t ev;
         CK(cudaEventCreate(&ev));
         c->events.push_back(ev);
     }
-    std::vector<int> kind;  // 0..3 stage, 4 inject
+    std::vector<int> kind;  // 0..3 stage, 4 inject, 5 curved-element stage
     size_t ei = 0;
     double tt = *t;
     for (int k = 0; k < nsteps; ++k) {
@@ -883,9 +894,15 @@ int dg_profile_steps(dg_ctx *c, double *t, double dt, int nsteps, dg_kernel_time
         }
         for (int s = 0; s < 4; ++s) {
             CK(cudaEventRecord(c->events[ei++], c->stream));
-            CK(launch_stage(c, s, dt));
+            CK(launch_affine_stage(c, s, dt));
             CK(cudaEventRecord(c->events[ei++], c->stream));
             kind.push_back(s);
+            if (c->curved) {
+                CK(cudaEventRecord(c->events[ei++], c->stream));
+                CK(c->prec == DG_PREC_FP64 ? launch_curved<double>(c, s, dt) : launch_curved<float>(c, s, dt));
+                CK(cudaEventRecord(c->events[ei++], c->stream));
+                kind.push_back(5);
+            }
         }
         tt += dt;
     }
@@ -894,6 +911,7 @@ int dg_profile_steps(dg_ctx *c, double *t, double dt, int nsteps, dg_kernel_time
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, c->events[2 * j], c->events[2 * j + 1]));
         if (kind[j] == 4) { out->inject_ms += ms; out->inject_launches++; }
+        else if (kind[j] == 5) { out->curved_ms += ms; out->curved_launches++; }
         else { out->stage_ms[kind[j]] += ms; out->stage_launches[kind[j]]++; }
     }
     float tot = 0;
@@ -912,11 +930,11 @@ int dg_monitors(dg_ctx *c, double *energy, double *l2, long long *status) {
     if (c->prec == DG_PREC_FP64)
         monitor_kernel<double><<<blocks, 256, 0, c->stream>>>((const double *)c->d_u, c->ndof, c->K, c->np, c->nq,
                                                               c->d_mass, c->d_detj, c->rho0, c->c0, c->d_mon,
-                                                              c->d_bad, c->d_cslot, c->d_cwdet, c->d_cphi, c->cng);
+                                                              c->d_bad, c->d_cslot, c->d_cwdet, c->d_cphi64, c->cng);
     else
         monitor_kernel<float><<<blocks, 256, 0, c->stream>>>((const float *)c->d_u, c->ndof, c->K, c->np, c->nq,
                                                              c->d_mass, c->d_detj, c->rho0, c->c0, c->d_mon,
-                                                             c->d_bad, c->d_cslot, c->d_cwdet, c->d_cphi, c->cng);
+                                                             c->d_bad, c->d_cslot, c->d_cwdet, c->d_cphi64, c->cng);
     CK(cudaGetLastError());
     double h[8];
     unsigned long long bad = 0;

@@ -45,8 +45,7 @@ struct Shape {
 
 // Connectivity word of an element face: bits 0-1 neighbour's local face,
 // 2-4 face permutation, 5-6 kind (0 interior, 1 reflecting, 2 absorbing),
-// 7 negative jump sign, 8 curved element (its update comes from the per-point
-// kernel; the affine kernels skip it).
+// 7 negative jump sign.
 enum : int { kKindInterior = 0, kKindReflecting = 1, kKindAbsorbing = 2 };
 enum : int { kStageEuler = 5 };
 
@@ -63,7 +62,8 @@ struct StageArgs {
     const int2 *conn;      // [K][NF]       neighbour element, connectivity word
     const Real *ops;       // NOPS reference operators
     const uint8_t *tabs;   // NTAB tables
-    int K;
+    const int *elist = nullptr;  // elements to run (the straight-sided ones of a mesh with curved elements), or null: all
+    int K;                 // elements to run
     Real dt;
     Real rc2;      // rho0 c0^2
     Real inv_rho;  // 1 / rho0
@@ -117,8 +117,10 @@ __device__ __forceinline__ void stage_tile(const StageArgs<Real> &a, long long b
     const int le = active ? tid / NP : 0;
     const int i = active ? tid - le * NP : 0;
     const Real *win = a.win + boff;
-    const int e = tile * EPB + le;
-    const bool valid = active && (e < a.K);
+    const int idx = tile * EPB + le;
+    const bool valid = active && (idx < a.K);
+    // meshes with curved elements: the tiles run over the list of the others
+    const int e = (a.elist && valid) ? __ldg(&a.elist[idx]) : idx;
     const long long base = (long long)e * NP + i;
     Real q[NQ];
 #pragma unroll
@@ -264,8 +266,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<Real> &a, long long b
 #pragma unroll
         for (int f = 0; f < NQ; ++f) L[f] = fma(l, fn[f], L[f]);
     }
-    // curved elements (connectivity bit 8) belong to the per-point kernel
-    if (valid && !(__ldg(&a.conn[(long long)e * NF].y) & 256)) {
+    if (valid) {
         Real *acc = a.acc + boff;
         Real *wout = a.wout + boff;
         const Real *uu = a.u + boff;

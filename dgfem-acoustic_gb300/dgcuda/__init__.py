@@ -84,7 +84,8 @@ class Opts(C.Structure):
 
 class KernelTimes(C.Structure):
     _fields_ = [("stage_ms", C.c_double * 4), ("stage_launches", C.c_int * 4), ("inject_ms", C.c_double),
-                ("inject_launches", C.c_int), ("total_ms", C.c_double)]
+                ("inject_launches", C.c_int), ("total_ms", C.c_double), ("curved_ms", C.c_double),
+                ("curved_launches", C.c_int)]
 
 
 class LayoutView(C.Structure):
@@ -584,7 +585,7 @@ class Solver:
         _check(lib().dg_profile_steps(self._h, C.byref(tt), dt, nsteps, C.byref(kt)))
         return tt.value, {"stage_ms": list(kt.stage_ms), "stage_launches": list(kt.stage_launches),
                           "inject_ms": kt.inject_ms, "inject_launches": kt.inject_launches,
-                          "total_ms": kt.total_ms}
+                          "total_ms": kt.total_ms, "curved_ms": kt.curved_ms, "curved_launches": kt.curved_launches}
 
     def monitors(self) -> tuple[float, list[float], int]:
         e = C.c_double()

@@ -4,6 +4,8 @@ multi_source: one mesh, many Gaussian-in-space hard sources (one per batch
 member) with sine time signals, and pressure receivers.
 uneven: many box meshes of seeded sizes and orders, one Gaussian source
 each, reflecting and absorbing sides mixed.
+curved_cube: a unit cube whose nodes are moved by a smooth map, so that all
+or half of its (isoparametric) elements are curved.
 """
 from __future__ import annotations
 
@@ -105,3 +107,33 @@ def room(cells=(20, 12, 8), size=(20.0, 12.0, 8.0), order: int = 3, nobst: int =
     ic = (0, *free_point(), 2 * sigma ** 2, 1.0)
     train = [(0, *free_point(), 2 * sigma ** 2, 1.0) for _ in range(ntrain)]
     return mesh, pre, dt, ic, train
+
+
+def curved_cube(n: int = 24, order: int = 3, kind: str = "full", amplitude: float = 0.02,
+                side_names=("Absorbing",) * 6):
+    """Unit cube of n^3 hexes x 6 tets, nodes moved by a smooth map.  kind
+    "full": x += a sin(pi y) sin(pi z), y += a sin(pi x) cos(pi z),
+    z += a sin(2x + y), which curves every element; "half": y and z move by
+    a (x - 1/2)^3 sin / cos terms for x > 1/2 only, so the elements with
+    x <= 1/2 stay straight; "none": the straight cube.  Returns (mesh, pre)."""
+    mesh = Mesh.box_tet(n, n, n, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), order=order, side_names=side_names)
+    a = amplitude
+    if kind == "full":
+        def fn(x):
+            y = x.copy()
+            y[:, 0] = x[:, 0] + a * np.sin(np.pi * x[:, 1]) * np.sin(np.pi * x[:, 2])
+            y[:, 1] = x[:, 1] + a * np.sin(np.pi * x[:, 0]) * np.cos(np.pi * x[:, 2])
+            y[:, 2] = x[:, 2] + a * np.sin(2 * x[:, 0] + x[:, 1])
+            return y
+        mesh.warp(fn)
+    elif kind == "half":
+        def fn(x):
+            y = x.copy()
+            s = np.clip(x[:, 0] - 0.5, 0.0, None) ** 3
+            y[:, 1] = x[:, 1] + 8 * a * s * np.sin(np.pi * x[:, 2])
+            y[:, 2] = x[:, 2] + 8 * a * s * np.cos(np.pi * x[:, 1])
+            return y
+        mesh.warp(fn)
+    elif kind != "none":
+        raise ValueError("kind must be full, half or none")
+    return mesh, Precomp(mesh)

@@ -110,11 +110,13 @@ typedef struct dg_opts {
 
 /* Per-kernel timing of dg_profile_steps (CUDA events on the solver stream). */
 typedef struct dg_kernel_times {
-    double stage_ms[4];   /* summed device time of the stage kernels */
+    double stage_ms[4];   /* summed device time of the (affine) stage kernels */
     int stage_launches[4];
     double inject_ms;
     int inject_launches;
     double total_ms;      /* first event to last event */
+    double curved_ms;     /* summed device time of the curved-element stage kernel */
+    int curved_launches;
 } dg_kernel_times;
 
 void dg_default_opts(dg_opts *opts);
