@@ -58,8 +58,9 @@ struct dg_ctx {
     int curved_grid = 0;
     int naff = 0;                 // elements the affine kernels run (all when no element is curved)
     int *d_aff = nullptr;         // their ids when some element is curved
+    int cepc = 1, cestride = 0, cmstride = 0;  // elements per CTA group, element data / map strides
     int *d_cel = nullptr, *d_cslot = nullptr;
-    void *d_cminv = nullptr, *d_cwm = nullptr, *d_cfw = nullptr;   // context precision
+    void *d_cedata = nullptr;                                        // context precision
     void *d_cphi = nullptr, *d_cdphi = nullptr, *d_cfphi = nullptr;
     double *d_cwdet = nullptr, *d_cphi64 = nullptr;                // FP64, for the monitors
     int2 *d_cfconn = nullptr;

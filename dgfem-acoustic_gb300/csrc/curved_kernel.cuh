@@ -1,7 +1,12 @@
 // Stage kernel of curved (non-affine, isoparametric) elements: the per-point
 // form of the reference's right-hand side, with geometry that varies inside
-// an element.  One CTA per curved element (grid-stride), arithmetic and
-// element data in the context's precision (FP64 or FP32).  Per element:
+// an element.  Arithmetic and element data in the context's precision (FP64
+// or FP32).  A CTA takes a group of EPC curved elements at a time (grid-
+// stride over the groups): it first copies everything the group reads from
+// global memory into shared memory with asynchronous copies (the elements'
+// state, their neighbours' values at the shared face nodes, inverse mass,
+// metric terms and face point data), so that all those loads are in flight
+// together, then works on shared memory only.  Per element:
 //
 //   volume  U(g) = sum_j phi_j(g) q_j at the points g of the element rule,
 //           Fc_u(g) = sum_x [w detJ J^-T]_(x,u)(g) Flux_x(U(g)),
@@ -28,6 +33,7 @@
 #include <stdint.h>
 
 #include "stage_kernel.cuh"
+#include "tc_ptx.cuh"
 
 namespace dgk {
 
@@ -39,27 +45,81 @@ struct CurvedArgs {
     Real *wout;
     long long fstride, bstride;
     const int *el;         // [C] element ids
-    const Real *minv;      // [C][np*np] row-major inverse mass (applied as its transpose, as linEq)
-    const Real *wm;        // [C][ng][DIM*DIM] w detJ J^-T at x*DIM+u
-    const Real *fw;        // [C][NF][ngf][4] outward normal, w detJf
     const int2 *fconn;     // [C][NF] neighbour (-1), word: kind bits 5-6, jump sign bit 7
-    const uint8_t *fmap;   // [C][NF][2][nfp] own / neighbour element node of face node k
+    const Real *edata;     // [C][estride] inverse mass (row-major, applied as its transpose, as linEq),
+                           // w detJ J^-T [ng][DIM*DIM] at x*DIM+u, [NF][ngf][4] outward normal and w detJf
+                           // (layout: curved_edata)
+    const uint8_t *fmap;   // [C][fstride_b] own / neighbour element node of face node k: [NF][2][nfp]
     const Real *phi;       // [ng][np]
     const Real *dphi;      // [DIM][ng][np]
     const Real *fphi;      // [ngf][nfp]
     int C, np, ng, ngf, nfp;
+    int epc;               // elements per CTA group
+    int estride;           // Reals per element in edata (curved_edata().stride)
+    int mstride;           // bytes per element in fmap (a multiple of 16)
     int stage;             // 0-3 RK4 stages, 4 forward Euler
     Real dt, rc2, inv_rho, half_c0, c0, rho, v0[3];
 };
 
-// Shared memory for an element of np nodes (rsize = bytes of the arithmetic type).
-__host__ __device__ inline size_t curved_smem_bytes(int dim, int np, int ng, int ngf, int rsize) {
-    const int nq = dim + 1, nf = dim + 1;
-    size_t d = (size_t)nq * np        // state
-               + (size_t)ng * dim * nq  // contravariant flux at the points
-               + (size_t)nf * ngf * nq  // weighted numerical flux at the face points
-               + (size_t)nq * np;       // S - F
-    return d * rsize + (size_t)nf * np * sizeof(int);
+// Element data of one curved element, in Reals: inverse mass [np*np] at 0,
+// metric terms [ng][DIM*DIM] at off_wm, face point data [NF][ngf][4] at
+// off_fw, each block starting on a 16-byte boundary (offsets multiples of 4
+// Reals), total padded to 16 bytes.
+struct CurvedEdata {
+    int off_wm, off_fw, stride;
+};
+
+__host__ __device__ inline CurvedEdata curved_edata(int dim, int np, int ng, int ngf, int rsize) {
+    CurvedEdata d;
+    d.off_wm = (np * np + 3) / 4 * 4;
+    d.off_fw = d.off_wm + (ng * dim * dim + 3) / 4 * 4;
+    const int total = d.off_fw + (dim + 1) * ngf * 4;
+    d.stride = (total * rsize + 15) / 16 * 16 / rsize;
+    return d;
+}
+
+// Per-element shared-memory slot, in Reals.  Field values are stored four
+// to a node or point (q innermost, padded to 4 in 2D) so that one 16-byte
+// shared-memory load serves all fields.
+struct CurvedSlot {
+    int ed, w, nb, fc, fn, r;  // element data, state [np][4], neighbour face values [NF][nfp][4],
+                               // Fc [ng][DIM][4], Fn [NF][ngf][4], S - F [np][4]
+    int reals;
+};
+
+__host__ __device__ inline CurvedSlot curved_slot(int dim, int np, int ng, int ngf, int nfp, int estride) {
+    const int nf = dim + 1;
+    CurvedSlot s;
+    s.ed = 0;
+    s.w = s.ed + estride;
+    s.nb = s.w + 4 * np;
+    s.fc = s.nb + 4 * nf * nfp;
+    s.fn = s.fc + 4 * ng * dim;
+    s.r = s.fn + 4 * nf * ngf;
+    s.reals = s.r + 4 * np;
+    return s;
+}
+
+// Shared memory of a CTA: epc slots of Reals, then per slot the face node
+// maps (mstride bytes, 16-byte copies) and the face position table [NF][np]
+// (int).
+__host__ __device__ inline size_t curved_smem_bytes(int dim, int np, int ng, int ngf, int nfp, int estride, int mstride,
+                                                    int epc, int rsize) {
+    const CurvedSlot sl = curved_slot(dim, np, ng, ngf, nfp, estride);
+    const size_t ints = (size_t)(dim + 1) * np;
+    return (size_t)epc * ((size_t)sl.reals * rsize + ints * sizeof(int) + mstride);
+}
+
+template <typename Real>
+__device__ __forceinline__ void st4(Real *p, const Real (&v)[4]);
+template <>
+__device__ __forceinline__ void st4<float>(float *p, const float (&v)[4]) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+template <>
+__device__ __forceinline__ void st4<double>(double *p, const double (&v)[4]) {
+    *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+    *reinterpret_cast<double2 *>(p + 2) = make_double2(v[2], v[3]);
 }
 
 // Physical flux of the linearised Euler equations with uniform mean flow
@@ -121,140 +181,256 @@ __device__ __forceinline__ void face_flux(int kind, Real tau, const Real *own, c
 }
 
 template <int DIM, typename Real>
-__global__ void __launch_bounds__(128) curved_stage_kernel(const CurvedArgs<Real> a) {
+__global__ void __launch_bounds__(256) curved_stage_kernel(const CurvedArgs<Real> a) {
     constexpr int NQ = DIM + 1, NF = DIM + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int np = a.np, ng = a.ng, ngf = a.ngf, nfp = a.nfp;
-    Real *sW = reinterpret_cast<Real *>(smem_raw);  // [NQ][np]
-    Real *sFc = sW + NQ * np;                        // [ng][DIM][NQ]
-    Real *sFn = sFc + ng * DIM * NQ;                 // [NF][ngf][NQ]
-    Real *sR = sFn + NF * ngf * NQ;                  // [NQ][np]
-    int *sK = reinterpret_cast<int *>(sR + NQ * np);     // [NF][np] face position of node i, or -1
+    const int np = a.np, ng = a.ng, ngf = a.ngf, nfp = a.nfp, epc = a.epc;
+    const CurvedSlot sl = curved_slot(DIM, np, ng, ngf, nfp, a.estride);
+    Real *sReal = reinterpret_cast<Real *>(smem_raw);
+    uint8_t *sMall = reinterpret_cast<uint8_t *>(sReal + (size_t)epc * sl.reals);
+    int *sKall = reinterpret_cast<int *>(sMall + (size_t)epc * a.mstride);
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long boff = (long long)blockIdx.y * a.bstride;
     const Real *win = a.win + boff;
     const Real v0[3] = {a.v0[0], a.v0[1], a.v0[2]};
-    for (int c = blockIdx.x; c < a.C; c += gridDim.x) {
-        const int e = a.el[c];
-        const long long ebase = (long long)e * np;
-        for (int t = tid; t < NQ * np; t += nt) {
-            const int q = t / np, i = t - q * np;
-            sW[t] = win[q * a.fstride + ebase + i];
+    const int ngroups = (a.C + epc - 1) / epc;
+    const int edim = a.estride;
+    const CurvedEdata eo = curved_edata(DIM, np, ng, ngf, (int)sizeof(Real));
+    for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+        const int c0 = grp * epc;
+        const int ne = min(epc, a.C - c0);
+        // ---- copies: element data and face maps (16-byte chunks), state
+        {
+            const int chunks = edim * (int)sizeof(Real) / 16;
+            for (int t = tid; t < ne * chunks; t += nt) {
+                const int s = t / chunks, q = t - s * chunks;
+                dgtc::cp_async16(reinterpret_cast<char *>(sReal + (size_t)s * sl.reals + sl.ed) + q * 16,
+                                 reinterpret_cast<const char *>(a.edata + (size_t)(c0 + s) * edim) + q * 16, 16);
+            }
+            const int mch = a.mstride / 16;
+            for (int t = tid; t < ne * mch; t += nt) {
+                const int s = t / mch, q = t - s * mch;
+                dgtc::cp_async16(sMall + (size_t)s * a.mstride + q * 16, a.fmap + (size_t)(c0 + s) * a.mstride + q * 16,
+                                 16);
+            }
+            const int nw = NQ * np;
+            for (int t = tid; t < ne * nw; t += nt) {
+                const int s = t / nw, r = t - s * nw;
+                const int q = r / np, i = r - q * np;
+                const long long at = q * a.fstride + (long long)__ldg(&a.el[c0 + s]) * np + i;
+                Real *dst = sReal + (size_t)s * sl.reals + sl.w + i * 4 + q;
+                if (sizeof(Real) == 8) dgtc::cp_async8(dst, win + at, 8);
+                else dgtc::cp_async4(dst, win + at, 4);
+            }
+            for (int t = tid; t < ne * NF * np; t += nt) sKall[t] = -1;
         }
-        for (int t = tid; t < NF * np; t += nt) sK[t] = -1;
+        dgtc::cp_async_commit();
+        dgtc::cp_async_wait_all();
         __syncthreads();
-        const uint8_t *fmap = a.fmap + (size_t)c * NF * 2 * nfp;
-        for (int t = tid; t < NF * nfp; t += nt) {
-            const int lf = t / nfp, k = t - lf * nfp;
-            sK[lf * np + fmap[(lf * 2) * nfp + k]] = k;
-        }
-        // volume points and face points
-        const int nwork = ng + NF * ngf;
-        for (int t = tid; t < nwork; t += nt) {
-            if (t < ng) {
-                const int g = t;
-                Real U[NQ];
-#pragma unroll
-                for (int q = 0; q < NQ; ++q) U[q] = Real(0);
-                const Real *ph = a.phi + (size_t)g * np;
-                for (int j = 0; j < np; ++j) {
-                    const Real p = __ldg(ph + j);
-#pragma unroll
-                    for (int q = 0; q < NQ; ++q) U[q] = fma(p, sW[q * np + j], U[q]);
-                }
-                Real F[DIM][DIM + 1];
-                lee_flux<DIM, Real>(U, v0, a.rc2, a.inv_rho, F);
-                const Real *w = a.wm + ((size_t)c * ng + g) * DIM * DIM;
-#pragma unroll
-                for (int u = 0; u < DIM; ++u)
-#pragma unroll
-                    for (int q = 0; q < NQ; ++q) {
-                        Real s = Real(0);
-#pragma unroll
-                        for (int x = 0; x < DIM; ++x) s = fma(__ldg(w + x * DIM + u), F[x][q], s);
-                        sFc[(g * DIM + u) * NQ + q] = s;
-                    }
-            } else {
-                const int lf = (t - ng) / ngf, g = (t - ng) - lf * ngf;
-                const int2 cn = a.fconn[(size_t)c * NF + lf];
-                const int kind = (cn.y >> 5) & 3;
-                const Real tau = (cn.y & 128) ? Real(-1) : Real(1);
-                const uint8_t *own = fmap + (lf * 2) * nfp;
-                const uint8_t *nbm = own + nfp;
-                const Real *fp = a.fphi + (size_t)g * nfp;
-                Real qi[NQ], qo[NQ];
-#pragma unroll
-                for (int q = 0; q < NQ; ++q) { qi[q] = Real(0); qo[q] = Real(0); }
-                const long long nbase = (long long)(kind == kKindInterior ? cn.x : 0) * np;
-                for (int k = 0; k < nfp; ++k) {
-                    const Real p = __ldg(fp + k);
-                    const int vi = own[k];
-#pragma unroll
-                    for (int q = 0; q < NQ; ++q) qi[q] = fma(p, sW[q * np + vi], qi[q]);
-                    if (kind == kKindInterior) {
-                        const long long at = nbase + nbm[k];
-#pragma unroll
-                        for (int q = 0; q < NQ; ++q) qo[q] = fma(p, __ldg(win + q * a.fstride + at), qo[q]);
-                    }
-                }
-                const Real *fw = a.fw + (((size_t)c * NF + lf) * ngf + g) * 4;
-                Real n[DIM];
-#pragma unroll
-                for (int x = 0; x < DIM; ++x) n[x] = __ldg(fw + x);
-                const Real wj = __ldg(fw + 3);
-                Real Fn[NQ];
-                face_flux<DIM, Real>(kind, tau, qi, qo, n, a.rc2, a.inv_rho, a.half_c0, a.c0, a.rho, v0, Fn);
-#pragma unroll
-                for (int q = 0; q < NQ; ++q) sFn[(lf * ngf + g) * NQ + q] = wj * Fn[q];
+        // neighbour values at the face nodes (the maps are in shared memory now)
+        {
+            const int nn = NF * nfp * NQ;
+            for (int t = tid; t < ne * nn; t += nt) {
+                const int s = t / nn, r = t - s * nn;
+                const int lf = r / (nfp * NQ), kq = r - lf * nfp * NQ;
+                const int q = kq / nfp, k = kq - q * nfp;
+                const int2 cn = __ldg(&a.fconn[(size_t)(c0 + s) * NF + lf]);
+                const uint8_t *nbm = sMall + (size_t)s * a.mstride + (lf * 2 + 1) * nfp;
+                const bool interior = ((cn.y >> 5) & 3) == kKindInterior;
+                const long long at = interior ? q * a.fstride + (long long)cn.x * np + nbm[k] : 0;
+                Real *dst = sReal + (size_t)s * sl.reals + sl.nb + (lf * nfp + k) * 4 + q;
+                if (sizeof(Real) == 8) dgtc::cp_async8(dst, win + at, interior ? 8 : 0);
+                else dgtc::cp_async4(dst, win + at, interior ? 4 : 0);
+            }
+            for (int t = tid; t < ne * NF * nfp; t += nt) {
+                const int s = t / (NF * nfp), r = t - s * NF * nfp;
+                const int lf = r / nfp, k = r - lf * nfp;
+                sKall[(s * NF + lf) * np + sMall[(size_t)s * a.mstride + (lf * 2) * nfp + k]] = k;
             }
         }
-        __syncthreads();
-        // S - F at the nodes
-        for (int t = tid; t < NQ * np; t += nt) {
-            const int q = t / np, i = t - q * np;
-            Real S = Real(0);
+        dgtc::cp_async_commit();
+        // volume points need only the own state: start them while the
+        // neighbour values arrive
+        for (int t = tid; t < ne * ng; t += nt) {
+            const int s = t / ng, g = t - s * ng;
+            const Real *base = sReal + (size_t)s * sl.reals;
+            Real Ua[4] = {Real(0), Real(0), Real(0), Real(0)}, Ub[4] = {Real(0), Real(0), Real(0), Real(0)};
+            const Real *ph = a.phi + (size_t)g * np;
+            const int half = np / 2;
+            for (int j = 0; j < half; ++j) {
+                const Real p0 = __ldg(ph + j), p1 = __ldg(ph + j + half);
+                Real w0[4], w1[4];
+                load4<Real>(base + sl.w + j * 4, w0);
+                load4<Real>(base + sl.w + (j + half) * 4, w1);
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) {
+                    Ua[q] = fma(p0, w0[q], Ua[q]);
+                    Ub[q] = fma(p1, w1[q], Ub[q]);
+                }
+            }
+            if (np & 1) {
+                const Real p = __ldg(ph + np - 1);
+                Real w4[4];
+                load4<Real>(base + sl.w + (np - 1) * 4, w4);
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) Ua[q] = fma(p, w4[q], Ua[q]);
+            }
+            Real U[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) U[q] = Ua[q] + Ub[q];
+            Real F[DIM][DIM + 1];
+            lee_flux<DIM, Real>(U, v0, a.rc2, a.inv_rho, F);
+            const Real *w = base + sl.ed + eo.off_wm + g * DIM * DIM;
+            Real *fc = sReal + (size_t)s * sl.reals + sl.fc + g * DIM * 4;
 #pragma unroll
             for (int u = 0; u < DIM; ++u) {
-                const Real *dp = a.dphi + (size_t)u * ng * np + i;
-                for (int g = 0; g < ng; ++g) S = fma(__ldg(dp + (size_t)g * np), sFc[(g * DIM + u) * NQ + q], S);
+                Real o[4] = {Real(0), Real(0), Real(0), Real(0)};
+#pragma unroll
+                for (int q = 0; q < NQ; ++q)
+#pragma unroll
+                    for (int x = 0; x < DIM; ++x) o[q] = fma(w[x * DIM + u], F[x][q], o[q]);
+                st4<Real>(fc + u * 4, o);
             }
-            Real Fl = Real(0);
+        }
+        dgtc::cp_async_wait_all();
+        __syncthreads();
+        // face points
+        for (int t = tid; t < ne * NF * ngf; t += nt) {
+            const int s = t / (NF * ngf), r = t - s * NF * ngf;
+            const int lf = r / ngf, g = r - lf * ngf;
+            Real *base = sReal + (size_t)s * sl.reals;
+            const int2 cn = __ldg(&a.fconn[(size_t)(c0 + s) * NF + lf]);
+            const int kind = (cn.y >> 5) & 3;
+            const Real tau = (cn.y & 128) ? Real(-1) : Real(1);
+            const uint8_t *own = sMall + (size_t)s * a.mstride + (lf * 2) * nfp;
+            const Real *fp = a.fphi + (size_t)g * nfp;
+            const Real *nb = base + sl.nb + lf * nfp * 4;
+            Real qi[4] = {Real(0), Real(0), Real(0), Real(0)}, qo[4] = {Real(0), Real(0), Real(0), Real(0)};
+            for (int k = 0; k < nfp; ++k) {
+                const Real p = __ldg(fp + k);
+                Real a4[4], b4[4];
+                load4<Real>(base + sl.w + own[k] * 4, a4);
+                load4<Real>(nb + k * 4, b4);
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) {
+                    qi[q] = fma(p, a4[q], qi[q]);
+                    qo[q] = fma(p, b4[q], qo[q]);
+                }
+            }
+            Real w4[4];
+            load4<Real>(base + sl.ed + eo.off_fw + (lf * ngf + g) * 4, w4);
+            Real n[DIM];
+#pragma unroll
+            for (int x = 0; x < DIM; ++x) n[x] = w4[x];
+            Real Fn[NQ];
+            face_flux<DIM, Real>(kind, tau, qi, qo, n, a.rc2, a.inv_rho, a.half_c0, a.c0, a.rho, v0, Fn);
+            Real o[4] = {Real(0), Real(0), Real(0), Real(0)};
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) o[q] = w4[3] * Fn[q];
+            st4<Real>(base + sl.fn + (lf * ngf + g) * 4, o);
+        }
+        __syncthreads();
+        // S - F at the nodes, all fields of a node in one thread
+        for (int t = tid; t < ne * np; t += nt) {
+            const int s = t / np, i = t - s * np;
+            Real *base = sReal + (size_t)s * sl.reals;
+            // one accumulator set per reference direction: DIM x NQ independent chains
+            Real Su[DIM][4];
+#pragma unroll
+            for (int u = 0; u < DIM; ++u)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) Su[u][q] = Real(0);
+            const Real *dp = a.dphi + i;
+            const Real *fc = base + sl.fc;
+            for (int g = 0; g < ng; ++g) {
+#pragma unroll
+                for (int u = 0; u < DIM; ++u) {
+                    const Real d = __ldg(dp + ((size_t)u * ng + g) * np);
+                    Real f4[4];
+                    load4<Real>(fc + (g * DIM + u) * 4, f4);
+#pragma unroll
+                    for (int q = 0; q < NQ; ++q) Su[u][q] = fma(d, f4[q], Su[u][q]);
+                }
+            }
+            Real S[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                S[q] = Su[0][q];
+#pragma unroll
+                for (int u = 1; u < DIM; ++u) S[q] += Su[u][q];
+            }
+            const int *sK = sKall + (size_t)s * NF * np;
 #pragma unroll
             for (int lf = 0; lf < NF; ++lf) {
                 const int k = sK[lf * np + i];
                 if (k < 0) continue;
-                Real s = Real(0);
-                for (int g = 0; g < ngf; ++g) s = fma(__ldg(a.fphi + (size_t)g * nfp + k), sFn[(lf * ngf + g) * NQ + q], s);
-                Fl += s;
+                const Real *fn = base + sl.fn + lf * ngf * 4;
+                for (int g = 0; g < ngf; ++g) {
+                    const Real p = __ldg(a.fphi + (size_t)g * nfp + k);
+                    Real f4[4];
+                    load4<Real>(fn + g * 4, f4);
+#pragma unroll
+                    for (int q = 0; q < NQ; ++q) S[q] = fma(-p, f4[q], S[q]);
+                }
             }
-            sR[q * np + i] = S - Fl;
+            st4<Real>(base + sl.r + i * 4, S);
         }
         __syncthreads();
         // r = dt M^-1 (S - F) and the stage update
-        const Real *mi = a.minv + (size_t)c * np * np;
         Real *acc = a.acc + boff;
         Real *wout = a.wout + boff;
         const Real *uu = a.u + boff;
-        for (int t = tid; t < NQ * np; t += nt) {
-            const int q = t / np, i = t - q * np;
-            Real s = Real(0);
-            for (int j = 0; j < np; ++j) s = fma(__ldg(mi + (size_t)j * np + i), sR[q * np + j], s);
-            const Real r = a.dt * s;
-            const Real qv = sW[q * np + i];
-            const long long idx = q * a.fstride + ebase + i;
-            if (a.stage == 0) {
-                acc[idx] = r;
-                wout[idx] = fma(Real(0.5), r, qv);
-            } else if (a.stage == 1) {
-                acc[idx] = fma(Real(2), r, acc[idx]);
-                wout[idx] = fma(Real(0.5), r, uu[idx]);
-            } else if (a.stage == 2) {
-                acc[idx] = fma(Real(2), r, acc[idx]);
-                wout[idx] = uu[idx] + r;
-            } else if (a.stage == 3) {
-                wout[idx] = uu[idx] + (acc[idx] + r) * (Real(1) / Real(6));
-            } else {
-                wout[idx] = qv + r;
+        for (int t = tid; t < ne * np; t += nt) {
+            const int s = t / np, i = t - s * np;
+            const Real *base = sReal + (size_t)s * sl.reals;
+            const Real *mi = base + sl.ed;
+            // two interleaved halves of the node sum: 2 x NQ independent chains
+            Real sa[4] = {Real(0), Real(0), Real(0), Real(0)}, sb[4] = {Real(0), Real(0), Real(0), Real(0)};
+            const int half = np / 2;
+            for (int j = 0; j < half; ++j) {
+                const Real m0 = mi[j * np + i], m1 = mi[(j + half) * np + i];
+                Real r0[4], r1[4];
+                load4<Real>(base + sl.r + j * 4, r0);
+                load4<Real>(base + sl.r + (j + half) * 4, r1);
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) {
+                    sa[q] = fma(m0, r0[q], sa[q]);
+                    sb[q] = fma(m1, r1[q], sb[q]);
+                }
+            }
+            if (np & 1) {
+                const int j = np - 1;
+                const Real m = mi[j * np + i];
+                Real r4[4];
+                load4<Real>(base + sl.r + j * 4, r4);
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) sa[q] = fma(m, r4[q], sa[q]);
+            }
+            Real sum[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) sum[q] = sa[q] + sb[q];
+            Real q4[4];
+            load4<Real>(base + sl.w + i * 4, q4);
+            const long long ebase = (long long)__ldg(&a.el[c0 + s]) * np + i;
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                const Real rv = a.dt * sum[q];
+                const Real qv = q4[q];
+                const long long idx = q * a.fstride + ebase;
+                if (a.stage == 0) {
+                    acc[idx] = rv;
+                    wout[idx] = fma(Real(0.5), rv, qv);
+                } else if (a.stage == 1) {
+                    acc[idx] = fma(Real(2), rv, acc[idx]);
+                    wout[idx] = fma(Real(0.5), rv, uu[idx]);
+                } else if (a.stage == 2) {
+                    acc[idx] = fma(Real(2), rv, acc[idx]);
+                    wout[idx] = uu[idx] + rv;
+                } else if (a.stage == 3) {
+                    wout[idx] = uu[idx] + (acc[idx] + rv) * (Real(1) / Real(6));
+                } else {
+                    wout[idx] = qv + rv;
+                }
             }
         }
         __syncthreads();

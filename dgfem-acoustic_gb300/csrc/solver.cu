@@ -136,9 +136,8 @@ void free_ctx(dg_ctx *c) {
                     c->d_t0,    c->d_stage64, c->d_mass,    c->d_detj,    c->d_mon,     c->d_bad,
                     c->d_src_at, c->d_src_off, c->d_src_list, c->d_src_w, c->d_src_params, c->d_ulo,
                     c->d_bimg,  c->d_beb,     c->d_err,     c->d_rec_dof, c->d_trace,   c->d_step0,
-                    c->d_geo32, c->d_cel,     c->d_cslot,   c->d_cminv,   c->d_cwm,     c->d_cwdet,
-                    c->d_cfw,   c->d_cphi,    c->d_cdphi,   c->d_cfphi,   c->d_cfconn,  c->d_cfmap,
-                    c->d_cphi64, c->d_aff};
+                    c->d_geo32, c->d_cel,     c->d_cslot,   c->d_cedata,  c->d_cwdet,   c->d_cphi,
+                    c->d_cdphi, c->d_cfphi,   c->d_cfconn,  c->d_cfmap,   c->d_cphi64,  c->d_aff};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -189,9 +188,7 @@ cudaError_t launch_curved(dg_ctx *c, int stage, double dt) {
     a.fstride = c->ndof;
     a.bstride = c->bstride;
     a.el = c->d_cel;
-    a.minv = static_cast<const Real *>(c->d_cminv);
-    a.wm = static_cast<const Real *>(c->d_cwm);
-    a.fw = static_cast<const Real *>(c->d_cfw);
+    a.edata = static_cast<const Real *>(c->d_cedata);
     a.fconn = c->d_cfconn;
     a.fmap = c->d_cfmap;
     a.phi = static_cast<const Real *>(c->d_cphi);
@@ -202,6 +199,9 @@ cudaError_t launch_curved(dg_ctx *c, int stage, double dt) {
     a.ng = c->cng;
     a.ngf = c->cngf;
     a.nfp = c->nfp;
+    a.epc = c->cepc;
+    a.estride = c->cestride;
+    a.mstride = c->cmstride;
     a.stage = stage == kEulerStage ? 4 : stage;
     a.dt = s.dt;
     a.rc2 = s.rc2;
@@ -211,7 +211,7 @@ cudaError_t launch_curved(dg_ctx *c, int stage, double dt) {
     a.rho = s.rho;
     for (int k = 0; k < 3; ++k) a.v0[k] = s.v0[k];
     void *args[] = {&a};
-    return cudaLaunchKernel(c->curved_fn, dim3(c->curved_grid, c->nbatch, 1), dim3(128, 1, 1), args,
+    return cudaLaunchKernel(c->curved_fn, dim3(c->curved_grid, c->nbatch, 1), dim3(256, 1, 1), args,
                             c->curved_smem, c->stream);
 }
 
@@ -492,7 +492,25 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
                 rc = fail(DG_ERR_UNSUPPORTED, "no curved-element kernel for this precision");
                 break;
             }
-            c->curved_smem = dgk::curved_smem_bytes(dim, np, cv.ng, cv.ngf, (int)c->rsize);
+            // element data packed per element (inverse mass, metric, face point data), padded to 16 bytes
+            const int rs = (int)c->rsize;
+            const int nmi = np * np, nwm = cv.ng * dim * dim, nfw = nf * cv.ngf * 4;
+            const dgk::CurvedEdata eo = dgk::curved_edata(dim, np, cv.ng, cv.ngf, rs);
+            c->cestride = eo.stride;
+            c->cmstride = (nf * 2 * nfp + 15) / 16 * 16;
+            // elements per CTA group: about one node per thread in the node phases,
+            // within a shared-memory budget (FP64 is bound by its arithmetic pipe
+            // anyway, FP32 by load/store issue, which larger groups help)
+            c->cepc = std::max(1, std::min(16, 256 / np));
+            auto smem_for = [&](int epc) {
+                return dgk::curved_smem_bytes(dim, np, cv.ng, cv.ngf, nfp, c->cestride, c->cmstride, epc, rs);
+            };
+            while (c->cepc > 1 && smem_for(c->cepc) > 100 * 1024) --c->cepc;
+            c->curved_smem = smem_for(c->cepc);
+            if (c->curved_smem > 227 * 1024) {
+                rc = fail(DG_ERR_UNSUPPORTED, "curved element data too large for shared memory at this order");
+                break;
+            }
             if (!fin(cudaFuncSetAttribute(c->curved_fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)c->curved_smem),
                      "cudaFuncSetAttribute(curved)"))
@@ -503,15 +521,32 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
             };
             if (!up(cv.el.data(), cv.el.size() * 4, (void **)&c->d_cel)) break;
             if (!up(cv.slot.data(), cv.slot.size() * 4, (void **)&c->d_cslot)) break;
-            // element data in the context's precision; FP64 copies for the monitors
+            {
+                std::vector<double> ed((size_t)cv.C * c->cestride, 0.0);
+                std::vector<uint8_t> mp((size_t)cv.C * c->cmstride, 0);
+                for (int k = 0; k < cv.C; ++k) {
+                    double *d = &ed[(size_t)k * c->cestride];
+                    std::copy_n(&cv.minv[(size_t)k * nmi], nmi, d);
+                    std::copy_n(&cv.wm[(size_t)k * nwm], nwm, d + eo.off_wm);
+                    std::copy_n(&cv.fw[(size_t)k * nfw], nfw, d + eo.off_fw);
+                    std::copy_n(&cv.fmap[(size_t)k * nf * 2 * nfp], nf * 2 * nfp, &mp[(size_t)k * c->cmstride]);
+                }
+                bool ok;
+                if (c->prec == DG_PREC_FP64) {
+                    ok = up(ed.data(), ed.size() * 8, &c->d_cedata);
+                } else {
+                    std::vector<float> f(ed.begin(), ed.end());
+                    ok = up(f.data(), f.size() * 4, &c->d_cedata);
+                }
+                if (!ok) break;
+                if (!up(mp.data(), mp.size(), (void **)&c->d_cfmap)) break;
+            }
+            // reference operators in the context's precision; FP64 copies for the monitors
             auto upr = [&](const std::vector<double> &v, void **dst) -> bool {
                 if (c->prec == DG_PREC_FP64) return up(v.data(), v.size() * 8, dst);
                 std::vector<float> f(v.begin(), v.end());
                 return up(f.data(), f.size() * 4, dst);
             };
-            if (!upr(cv.minv, &c->d_cminv)) break;
-            if (!upr(cv.wm, &c->d_cwm)) break;
-            if (!upr(cv.fw, &c->d_cfw)) break;
             if (!upr(cv.phi, &c->d_cphi)) break;
             if (!upr(cv.dphi, &c->d_cdphi)) break;
             if (!upr(cv.fphi, &c->d_cfphi)) break;
@@ -519,13 +554,13 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
             if (!up(cv.phi.data(), cv.phi.size() * 8, (void **)&c->d_cphi64)) break;
             if (!up(cv.affine.data(), cv.affine.size() * 4, (void **)&c->d_aff)) break;
             if (!up(cv.fconn.data(), cv.fconn.size() * 4, (void **)&c->d_cfconn)) break;
-            if (!up(cv.fmap.data(), cv.fmap.size(), (void **)&c->d_cfmap)) break;
             int cper = 0;
-            if (!fin(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cper, c->curved_fn, 128, c->curved_smem),
+            if (!fin(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cper, c->curved_fn, 256, c->curved_smem),
                      "occupancy(curved)"))
                 break;
             const int cres = std::max(cper, 1) * nsm;
-            c->curved_grid = std::max(1, std::min(cv.C, (cres + nbatch - 1) / nbatch));
+            const int ngroups = (cv.C + c->cepc - 1) / c->cepc;
+            c->curved_grid = std::max(1, std::min(ngroups, (cres + nbatch - 1) / nbatch));
         }
         if (!fin(cudaStreamSynchronize(c->stream), "sync")) break;
     } while (0);
