@@ -2,11 +2,12 @@
 // form of the reference's right-hand side, with geometry that varies inside
 // an element.  Arithmetic and element data in the context's precision (FP64
 // or FP32).  A CTA takes a group of EPC curved elements at a time (grid-
-// stride over the groups): it first copies everything the group reads from
-// global memory into shared memory with asynchronous copies (the elements'
-// state, their neighbours' values at the shared face nodes, inverse mass,
-// metric terms and face point data), so that all those loads are in flight
-// together, then works on shared memory only.  Per element:
+// stride over the groups): it first copies the group's state and its
+// neighbours' values at the shared face nodes into shared memory with
+// asynchronous copies, so that all those scattered loads are in flight
+// together; the per-element matrices (inverse mass, metric terms, face point
+// data) are read through L1 where they are used, which keeps the shared
+// memory per CTA small enough for 4-5 CTAs per SM.  Per element:
 //
 //   volume  U(g) = sum_j phi_j(g) q_j at the points g of the element rule,
 //           Fc_u(g) = sum_x [w detJ J^-T]_(x,u)(g) Flux_x(U(g)),
@@ -63,8 +64,7 @@ struct CurvedArgs {
 
 // Element data of one curved element, in Reals: inverse mass [np*np] at 0,
 // metric terms [ng][DIM*DIM] at off_wm, face point data [NF][ngf][4] at
-// off_fw, each block starting on a 16-byte boundary (offsets multiples of 4
-// Reals), total padded to 16 bytes.
+// off_fw, each block starting on a 16-byte boundary, total padded to 16 bytes.
 struct CurvedEdata {
     int off_wm, off_fw, stride;
 };
@@ -82,16 +82,15 @@ __host__ __device__ inline CurvedEdata curved_edata(int dim, int np, int ng, int
 // to a node or point (q innermost, padded to 4 in 2D) so that one 16-byte
 // shared-memory load serves all fields.
 struct CurvedSlot {
-    int ed, w, nb, fc, fn, r;  // element data, state [np][4], neighbour face values [NF][nfp][4],
-                               // Fc [ng][DIM][4], Fn [NF][ngf][4], S - F [np][4]
+    int w, nb, fc, fn, r;  // state [np][4], neighbour face values [NF][nfp][4], Fc [ng][DIM][4],
+                           // Fn [NF][ngf][4], S - F [np][4]
     int reals;
 };
 
-__host__ __device__ inline CurvedSlot curved_slot(int dim, int np, int ng, int ngf, int nfp, int estride) {
+__host__ __device__ inline CurvedSlot curved_slot(int dim, int np, int ng, int ngf, int nfp) {
     const int nf = dim + 1;
     CurvedSlot s;
-    s.ed = 0;
-    s.w = s.ed + estride;
+    s.w = 0;
     s.nb = s.w + 4 * np;
     s.fc = s.nb + 4 * nf * nfp;
     s.fn = s.fc + 4 * ng * dim;
@@ -103,9 +102,9 @@ __host__ __device__ inline CurvedSlot curved_slot(int dim, int np, int ng, int n
 // Shared memory of a CTA: epc slots of Reals, then per slot the face node
 // maps (mstride bytes, 16-byte copies) and the face position table [NF][np]
 // (int).
-__host__ __device__ inline size_t curved_smem_bytes(int dim, int np, int ng, int ngf, int nfp, int estride, int mstride,
-                                                    int epc, int rsize) {
-    const CurvedSlot sl = curved_slot(dim, np, ng, ngf, nfp, estride);
+__host__ __device__ inline size_t curved_smem_bytes(int dim, int np, int ng, int ngf, int nfp, int mstride, int epc,
+                                                    int rsize) {
+    const CurvedSlot sl = curved_slot(dim, np, ng, ngf, nfp);
     const size_t ints = (size_t)(dim + 1) * np;
     return (size_t)epc * ((size_t)sl.reals * rsize + ints * sizeof(int) + mstride);
 }
@@ -185,7 +184,7 @@ __global__ void __launch_bounds__(256) curved_stage_kernel(const CurvedArgs<Real
     constexpr int NQ = DIM + 1, NF = DIM + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int np = a.np, ng = a.ng, ngf = a.ngf, nfp = a.nfp, epc = a.epc;
-    const CurvedSlot sl = curved_slot(DIM, np, ng, ngf, nfp, a.estride);
+    const CurvedSlot sl = curved_slot(DIM, np, ng, ngf, nfp);
     Real *sReal = reinterpret_cast<Real *>(smem_raw);
     uint8_t *sMall = reinterpret_cast<uint8_t *>(sReal + (size_t)epc * sl.reals);
     int *sKall = reinterpret_cast<int *>(sMall + (size_t)epc * a.mstride);
@@ -201,12 +200,6 @@ __global__ void __launch_bounds__(256) curved_stage_kernel(const CurvedArgs<Real
         const int ne = min(epc, a.C - c0);
         // ---- copies: element data and face maps (16-byte chunks), state
         {
-            const int chunks = edim * (int)sizeof(Real) / 16;
-            for (int t = tid; t < ne * chunks; t += nt) {
-                const int s = t / chunks, q = t - s * chunks;
-                dgtc::cp_async16(reinterpret_cast<char *>(sReal + (size_t)s * sl.reals + sl.ed) + q * 16,
-                                 reinterpret_cast<const char *>(a.edata + (size_t)(c0 + s) * edim) + q * 16, 16);
-            }
             const int mch = a.mstride / 16;
             for (int t = tid; t < ne * mch; t += nt) {
                 const int s = t / mch, q = t - s * mch;
@@ -280,7 +273,7 @@ __global__ void __launch_bounds__(256) curved_stage_kernel(const CurvedArgs<Real
             for (int q = 0; q < 4; ++q) U[q] = Ua[q] + Ub[q];
             Real F[DIM][DIM + 1];
             lee_flux<DIM, Real>(U, v0, a.rc2, a.inv_rho, F);
-            const Real *w = base + sl.ed + eo.off_wm + g * DIM * DIM;
+            const Real *w = a.edata + (size_t)(c0 + s) * edim + eo.off_wm + g * DIM * DIM;
             Real *fc = sReal + (size_t)s * sl.reals + sl.fc + g * DIM * 4;
 #pragma unroll
             for (int u = 0; u < DIM; ++u) {
@@ -288,7 +281,7 @@ __global__ void __launch_bounds__(256) curved_stage_kernel(const CurvedArgs<Real
 #pragma unroll
                 for (int q = 0; q < NQ; ++q)
 #pragma unroll
-                    for (int x = 0; x < DIM; ++x) o[q] = fma(w[x * DIM + u], F[x][q], o[q]);
+                    for (int x = 0; x < DIM; ++x) o[q] = fma(__ldg(w + x * DIM + u), F[x][q], o[q]);
                 st4<Real>(fc + u * 4, o);
             }
         }
@@ -318,7 +311,11 @@ __global__ void __launch_bounds__(256) curved_stage_kernel(const CurvedArgs<Real
                 }
             }
             Real w4[4];
-            load4<Real>(base + sl.ed + eo.off_fw + (lf * ngf + g) * 4, w4);
+            {
+                const Real *fwp = a.edata + (size_t)(c0 + s) * edim + eo.off_fw + (lf * ngf + g) * 4;
+#pragma unroll
+                for (int x = 0; x < 4; ++x) w4[x] = __ldg(fwp + x);
+            }
             Real n[DIM];
 #pragma unroll
             for (int x = 0; x < DIM; ++x) n[x] = w4[x];
@@ -383,12 +380,12 @@ __global__ void __launch_bounds__(256) curved_stage_kernel(const CurvedArgs<Real
         for (int t = tid; t < ne * np; t += nt) {
             const int s = t / np, i = t - s * np;
             const Real *base = sReal + (size_t)s * sl.reals;
-            const Real *mi = base + sl.ed;
+            const Real *mi = a.edata + (size_t)(c0 + s) * edim;
             // two interleaved halves of the node sum: 2 x NQ independent chains
             Real sa[4] = {Real(0), Real(0), Real(0), Real(0)}, sb[4] = {Real(0), Real(0), Real(0), Real(0)};
             const int half = np / 2;
             for (int j = 0; j < half; ++j) {
-                const Real m0 = mi[j * np + i], m1 = mi[(j + half) * np + i];
+                const Real m0 = __ldg(mi + j * np + i), m1 = __ldg(mi + (j + half) * np + i);
                 Real r0[4], r1[4];
                 load4<Real>(base + sl.r + j * 4, r0);
                 load4<Real>(base + sl.r + (j + half) * 4, r1);
@@ -400,7 +397,7 @@ __global__ void __launch_bounds__(256) curved_stage_kernel(const CurvedArgs<Real
             }
             if (np & 1) {
                 const int j = np - 1;
-                const Real m = mi[j * np + i];
+                const Real m = __ldg(mi + j * np + i);
                 Real r4[4];
                 load4<Real>(base + sl.r + j * 4, r4);
 #pragma unroll

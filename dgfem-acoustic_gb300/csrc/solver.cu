@@ -499,13 +499,13 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
             c->cestride = eo.stride;
             c->cmstride = (nf * 2 * nfp + 15) / 16 * 16;
             // elements per CTA group: about one node per thread in the node phases,
-            // within a shared-memory budget (FP64 is bound by its arithmetic pipe
-            // anyway, FP32 by load/store issue, which larger groups help)
+            // within 48 KB of shared memory per CTA (4-5 CTAs per SM; 32 KB and
+            // 100 KB measured slower)
             c->cepc = std::max(1, std::min(16, 256 / np));
             auto smem_for = [&](int epc) {
-                return dgk::curved_smem_bytes(dim, np, cv.ng, cv.ngf, nfp, c->cestride, c->cmstride, epc, rs);
+                return dgk::curved_smem_bytes(dim, np, cv.ng, cv.ngf, nfp, c->cmstride, epc, rs);
             };
-            while (c->cepc > 1 && smem_for(c->cepc) > 100 * 1024) --c->cepc;
+            while (c->cepc > 1 && smem_for(c->cepc) > 48 * 1024) --c->cepc;
             c->curved_smem = smem_for(c->cepc);
             if (c->curved_smem > 227 * 1024) {
                 rc = fail(DG_ERR_UNSUPPORTED, "curved element data too large for shared memory at this order");
