@@ -99,6 +99,9 @@ int main(int argc, char **argv) {
     log("Element dimension : " + std::to_string(pre.dim));
     log("Element Order : " + std::to_string(pre.order));
     log("Number of Faces : " + std::to_string(pre.F));
+    if (pre.ncurved > 0)
+        log("Curved elements : " + std::to_string(pre.ncurved) + " (per-point geometry on " +
+            std::to_string(pre.ng) + " element / " + std::to_string(pre.ngf) + " face points)");
     const size_t ndof = (size_t)pre.K * pre.np;
 
     // initial conditions (dgalerkin.cpp:37-50)

@@ -60,6 +60,24 @@ __global__ void join_kernel(const float *hi, const float *lo, double *dst, long 
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     for (; i < n; i += (long long)gridDim.x * blockDim.x) dst[i] = double(hi[i]) + double(lo[i]);
 }
+__global__ void copy_kernel(const double *src, double *dst, long long n) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; i < n; i += (long long)gridDim.x * blockDim.x) dst[i] = src[i];
+}
+
+// Host arrays the GPU can address (pinned or registered host memory): the
+// device-side address, else null.  The conversion kernels then read or write
+// such an array themselves over the host link (NVLink-C2C on Grace), in one
+// pass and without a staging copy per field.
+const void *host_device_view(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+const int kHostIoBlocks = 2048;  // grid of the host-link kernels: many loads in flight
 
 // FP64 monitors: thread per element, u^T M u per field, non-finite count.
 // Curved elements (cslot[e] >= 0) use their own mass matrix, applied as the
@@ -591,6 +609,16 @@ int set_member(dg_ctx *c, int member, const double *const u[4]) {
     for (int f = 0; f < c->nq; ++f) {
         const long long off = moff + f * c->ndof;
         char *dst = (char *)c->d_u + off * c->rsize;
+        if (const double *hv = static_cast<const double *>(host_device_view(u[f]))) {
+            if (c->prec == DG_PREC_FP64)
+                copy_kernel<<<kHostIoBlocks, 256, 0, c->stream>>>(hv, (double *)dst, c->ndof);
+            else if (c->mixed)
+                split_kernel<<<kHostIoBlocks, 256, 0, c->stream>>>(hv, (float *)dst, c->d_ulo + off, c->ndof);
+            else
+                cast_kernel<float><<<kHostIoBlocks, 256, 0, c->stream>>>(hv, (float *)dst, c->ndof);
+            CK(cudaGetLastError());
+            continue;
+        }
         if (c->prec == DG_PREC_FP64) {
             CK(cudaMemcpyAsync(dst, u[f], (size_t)c->ndof * 8, cudaMemcpyHostToDevice, c->stream));
         } else {
@@ -615,6 +643,16 @@ int get_member(dg_ctx *c, int member, double *const u[4]) {
         if (!u[f]) continue;
         const long long off = moff + f * c->ndof;
         const char *src = (const char *)c->d_u + off * c->rsize;
+        if (double *hv = static_cast<double *>(const_cast<void *>(host_device_view(u[f])))) {
+            if (c->prec == DG_PREC_FP64)
+                copy_kernel<<<kHostIoBlocks, 256, 0, c->stream>>>((const double *)src, hv, c->ndof);
+            else if (c->mixed)
+                join_kernel<<<kHostIoBlocks, 256, 0, c->stream>>>((const float *)src, c->d_ulo + off, hv, c->ndof);
+            else
+                uncast_kernel<float><<<kHostIoBlocks, 256, 0, c->stream>>>((const float *)src, hv, c->ndof);
+            CK(cudaGetLastError());
+            continue;
+        }
         if (c->prec == DG_PREC_FP64) {
             CK(cudaMemcpyAsync(u[f], src, (size_t)c->ndof * 8, cudaMemcpyDeviceToHost, c->stream));
         } else {
