@@ -144,26 +144,7 @@ int dgm_precompute(const dgm_mesh *m, int nbc, const int *tags, const int *refl,
 
 int dgm_get_desc(const dgm_precomp *h, dg_mesh_desc *d) {
     if (!h || !d) return fail(DG_ERR_ARG, "null argument");
-    const Precomp &p = h->p;
-    d->dim = p.dim; d->order = p.order; d->num_el = p.K; d->el_num_nodes = p.np;
-    d->f_num = p.F; d->f_num_per_el = p.nf; d->f_num_nodes = p.nfp; d->fc = p.fc;
-    d->el_jacobians = p.el_jac.data(); d->el_jacobian_dets = p.el_detj.data();
-    d->f_normals = p.f_normal.data(); d->f_jacobian_dets = p.f_detj.data();
-    d->el_f_ids = p.el_f_ids.data(); d->el_f_orientation = p.el_f_orient.data();
-    d->f_nbr_el_ids = p.f_nbr.data(); d->f_n_to_el_n_ids = p.f_n_to_el_n.data();
-    d->f_bc = p.f_bc.data(); d->f_is_boundary = p.f_is_bnd.data();
-    const bool qp = p.ncurved > 0;
-    d->el_num_int_pts = qp ? p.ng : 0;
-    d->el_int_param_coords = qp ? p.el_qp.data() : nullptr;
-    d->el_basis_fcts = qp ? p.el_phi.data() : nullptr;
-    d->el_ugrad_basis_fcts = qp ? p.el_dphi.data() : nullptr;
-    d->el_jacobians_qp = qp ? p.el_jac_qp.data() : nullptr;
-    d->el_jacobian_dets_qp = qp ? p.el_detj_qp.data() : nullptr;
-    d->f_num_int_pts = qp ? p.ngf : 0;
-    d->f_int_param_coords = qp ? p.f_qp.data() : nullptr;
-    d->f_basis_fcts = qp ? p.f_phi.data() : nullptr;
-    d->f_normals_qp = qp ? p.f_normal_qp.data() : nullptr;
-    d->f_jacobian_dets_qp = qp ? p.f_detj_qp.data() : nullptr;
+    fill_desc(h->p, *d);
     return DG_OK;
 }
 

@@ -124,13 +124,7 @@ int main(int argc, char **argv) {
         return EXIT_SUCCESS;
     }
     dg_mesh_desc desc;
-    desc.dim = pre.dim; desc.order = pre.order; desc.num_el = pre.K; desc.el_num_nodes = pre.np;
-    desc.f_num = pre.F; desc.f_num_per_el = pre.nf; desc.f_num_nodes = pre.nfp; desc.fc = pre.fc;
-    desc.el_jacobians = pre.el_jac.data(); desc.el_jacobian_dets = pre.el_detj.data();
-    desc.f_normals = pre.f_normal.data(); desc.f_jacobian_dets = pre.f_detj.data();
-    desc.el_f_ids = pre.el_f_ids.data(); desc.el_f_orientation = pre.el_f_orient.data();
-    desc.f_nbr_el_ids = pre.f_nbr.data(); desc.f_n_to_el_n_ids = pre.f_n_to_el_n.data();
-    desc.f_bc = pre.f_bc.data(); desc.f_is_boundary = pre.f_is_bnd.data();
+    dg::fill_desc(pre, desc);
     dg_phys_desc phys;
     phys.c0 = cfg.c0; phys.rho0 = cfg.rho0;
     for (int k = 0; k < 3; ++k) phys.v0[k] = cfg.v0[k];

@@ -183,6 +183,30 @@ std::string face_points(const RefElement &re, NodeFn X, Precomp &P) {
 
 }  // namespace
 
+void fill_desc(const Precomp &p, dg_mesh_desc &d) {
+    d = dg_mesh_desc();
+    d.dim = p.dim; d.order = p.order; d.num_el = p.K; d.el_num_nodes = p.np;
+    d.f_num = p.F; d.f_num_per_el = p.nf; d.f_num_nodes = p.nfp; d.fc = p.fc;
+    d.el_jacobians = p.el_jac.data(); d.el_jacobian_dets = p.el_detj.data();
+    d.f_normals = p.f_normal.data(); d.f_jacobian_dets = p.f_detj.data();
+    d.el_f_ids = p.el_f_ids.data(); d.el_f_orientation = p.el_f_orient.data();
+    d.f_nbr_el_ids = p.f_nbr.data(); d.f_n_to_el_n_ids = p.f_n_to_el_n.data();
+    d.f_bc = p.f_bc.data(); d.f_is_boundary = p.f_is_bnd.data();
+    if (p.ncurved > 0) {
+        d.el_num_int_pts = p.ng;
+        d.el_int_param_coords = p.el_qp.data();
+        d.el_basis_fcts = p.el_phi.data();
+        d.el_ugrad_basis_fcts = p.el_dphi.data();
+        d.el_jacobians_qp = p.el_jac_qp.data();
+        d.el_jacobian_dets_qp = p.el_detj_qp.data();
+        d.f_num_int_pts = p.ngf;
+        d.f_int_param_coords = p.f_qp.data();
+        d.f_basis_fcts = p.f_phi.data();
+        d.f_normals_qp = p.f_normal_qp.data();
+        d.f_jacobian_dets_qp = p.f_detj_qp.data();
+    }
+}
+
 std::string precompute(const RawMesh &m, const std::vector<std::pair<int, bool>> &physical_bcs, Precomp &P) {
     P = Precomp();
     if (m.dim != 2 && m.dim != 3) return "only 2D and 3D meshes are supported";

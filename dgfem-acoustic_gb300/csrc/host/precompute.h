@@ -31,6 +31,7 @@
 #include <utility>
 #include <vector>
 
+#include "../../../include/dgcuda.h"
 #include "mesh_io.h"
 #include "refel.h"
 
@@ -65,6 +66,11 @@ struct Precomp {
     std::vector<double> f_normal_qp;    // [F][ngf][3] after the boundary flip
     std::vector<double> f_detj_qp;      // [F][ngf]
 };
+
+// The reference Mesh arrays of a precompute as the solver's descriptor
+// (first-point arrays, and the per-point arrays when some element is
+// curved); pointers into P, which must outlive the descriptor.
+void fill_desc(const Precomp &P, dg_mesh_desc &d);
 
 // physical_bcs: (physical tag, reflecting?) for the boundary groups the
 // configuration names, ascending tag order (configParser.cpp:117-132).

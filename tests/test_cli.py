@@ -96,7 +96,7 @@ def test_cli_curved_mesh_matches_oracle(tmp_path):
     dt = D.cfl_dt(pre, 340.0)
     conf = tmp_path / "c.conf"
     save = tmp_path / "out.msh"
-    conf.write_text(CONF.format(tend=(20 - 0.5) * dt, dt=repr(dt), rate=repr(10 * dt * 0.999), sdur=repr(8 * dt),
+    conf.write_text(CONF.format(tend=(30 - 0.5) * dt, dt=repr(dt), rate=repr(10 * dt * 0.999), sdur=repr(8 * dt),
                                 save=save, method="Runge-Kutta"))
     exe = D.PKG / "lib" / "dgalerkin"
     r = subprocess.run([str(exe), str(msh), str(conf)], capture_output=True, text=True, timeout=300)
