@@ -505,6 +505,7 @@ def uneven_section(D, args, local):
     with ClockSampler(local) as clk:
         t, ms = ms_.rk4_steps_timed(t, dts, args.uneven_steps)
     info = ms_.info()
+    names = [f"one launch, {b}-thread CTAs" if b else "one launch per order" for b in info["block_threads"]]
     ms_.close()
     # the same meshes, one single-mesh context each, stepped one after the other
     nsep = max(3, args.uneven_steps // 10)
@@ -522,8 +523,8 @@ def uneven_section(D, args, local):
                        f"{min(tets)}-{max(tets)} tets per mesh ({sum(tets)} tets), orders {sorted(set(orders))}, "
                        "one Gaussian source each, mixed reflecting/absorbing sides, FP32",
             "unit": UNIT, "value": value, "steps": args.uneven_steps, "ms_per_step": ms / args.uneven_steps,
-            "tile_config": {"chosen_block_threads": info["block_threads"][chosen],
-                            "candidates_ms_per_step": dict(zip(map(str, info["block_threads"]), cand))},
+            "tile_config": {"chosen": names[chosen],
+                            "candidates_ms_per_step": dict(zip(names, cand))},
             "separate_contexts_ms_per_step": sep_ms,
             "one_launch_over_separate": sep_ms / (ms / args.uneven_steps),
             "clocks": clk.summary()}

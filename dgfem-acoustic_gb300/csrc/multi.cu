@@ -1,5 +1,6 @@
 // Uneven multi-mesh batches: many 3D meshes of different sizes and orders
-// stepped together, one persistent launch per RK4 stage for all of them.
+// stepped together, one persistent launch per RK4 stage for all of them, or
+// (configuration kMultiPerOrder) one per order present.
 //
 // Work is a list of items (mesh, tile of that mesh's elements), sorted by
 // order, that the CTAs of a persistent grid take in turn; a CTA loads the
@@ -27,10 +28,12 @@
 
 namespace dgk {
 
-// Block sizes the multi-mesh kernel is compiled for (the autotuner's
-// candidates).
+// Block sizes the one-launch kernel is compiled for; configuration
+// kMultiPerOrder launches one persistent kernel per order present instead,
+// each sized for its order (the autotuner's fourth candidate).
 constexpr int kMultiBlocks[3] = {128, 256, 512};
-constexpr int kMultiCfgs = 3;
+constexpr int kMultiPerOrder = 3;
+constexpr int kMultiCfgs = 4;
 
 __host__ __device__ constexpr int multi_np(int p) { return (p + 1) * (p + 2) * (p + 3) / 6; }
 __host__ __device__ constexpr int multi_epb(int bt, int p) { return bt / multi_np(p) > 0 ? bt / multi_np(p) : 1; }
@@ -86,6 +89,37 @@ __global__ void __launch_bounds__(BT) multi_stage_kernel(const MultiMesh<Real> *
     }
 }
 
+// Elements per CTA of the per-order launches: those of the single-mesh
+// kernels (about 128-256 threads per CTA).
+__host__ __device__ constexpr int order_epb(int p) {
+    return multi_np(p) <= 4 ? 32 : multi_np(p) <= 10 ? 16 : multi_np(p) <= 21 ? 8 : 4;
+}
+
+// One order's items (a contiguous range of the sorted item list), with its
+// operators loaded into shared memory once per CTA.
+template <typename Real, int STAGE, int P>
+__global__ void __launch_bounds__(order_epb(P) * multi_np(P))
+    multi_order_kernel(const MultiMesh<Real> *meshes, const int2 *items, int nitems, const Real *ops,
+                       const uint8_t *tabs) {
+    using S = Shape<3, P>;
+    constexpr int EPB = order_epb(P);
+    constexpr int NT = EPB * S::NP;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Real *sOps = reinterpret_cast<Real *>(smem_raw);
+    Real *sQ = sOps + S::NOPS_PAD;
+    Real *sFn = sQ + EPB * S::NP * 4;
+    uint8_t *sTab = reinterpret_cast<uint8_t *>(sFn + EPB * S::NSLOT * 4);
+    const int tid = threadIdx.x;
+    for (int k = tid; k < S::NOPS; k += NT) sOps[k] = ops[k];
+    for (int k = tid; k < S::NTAB; k += NT) sTab[k] = tabs[k];
+    __syncthreads();
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int2 w = items[it];
+        const StageArgs<Real> a = meshes[w.x].st[STAGE - 1];
+        stage_tile<3, P, Real, STAGE, EPB>(a, 0, w.y, sQ, sFn, sOps, sTab, tid);
+    }
+}
+
 // Hard sources of a multi-mesh batch: node j is the arena value at[j] of
 // mesh node_mesh[j], whose time is t0[mesh] + kstep*dt[mesh] (repeated
 // additions, as the reference loop).
@@ -113,9 +147,18 @@ __global__ void multi_inject_kernel(Real *p, const long long *at, const int *nod
 
 template <typename Real>
 struct MultiKernels {
-    const void *stage[kMultiCfgs][4];
+    const void *stage[kMultiCfgs][4];   // one-launch configurations (the per-order slot is unused)
+    const void *order[6][4];            // per-order kernels by order and stage
     const void *inject;
 };
+
+template <typename Real, int P>
+void fill_order(MultiKernels<Real> &k) {
+    k.order[P][0] = (const void *)&multi_order_kernel<Real, 1, P>;
+    k.order[P][1] = (const void *)&multi_order_kernel<Real, 2, P>;
+    k.order[P][2] = (const void *)&multi_order_kernel<Real, 3, P>;
+    k.order[P][3] = (const void *)&multi_order_kernel<Real, 4, P>;
+}
 
 template <typename Real, int C>
 void fill_cfg(MultiKernels<Real> &k) {
@@ -128,9 +171,15 @@ void fill_cfg(MultiKernels<Real> &k) {
 template <typename Real>
 MultiKernels<Real> multi_kernels() {
     MultiKernels<Real> k;
+    std::memset(&k, 0, sizeof(k));
     fill_cfg<Real, 0>(k);
     fill_cfg<Real, 1>(k);
     fill_cfg<Real, 2>(k);
+    fill_order<Real, 1>(k);
+    fill_order<Real, 2>(k);
+    fill_order<Real, 3>(k);
+    fill_order<Real, 4>(k);
+    fill_order<Real, 5>(k);
     k.inject = (const void *)&multi_inject_kernel<Real>;
     return k;
 }
@@ -156,11 +205,14 @@ struct dg_multi {
     void *d_ops_tab = nullptr;   // device array of the ops pointers by order
     void *d_tabs_tab = nullptr;  // device array of the table pointers by order
     void *d_meshes = nullptr;    // MultiMesh<Real>[nmesh]
-    int2 *d_items[dgk::kMultiCfgs] = {nullptr, nullptr, nullptr};
-    int nitems[dgk::kMultiCfgs] = {0, 0, 0};
+    int2 *d_items[dgk::kMultiCfgs] = {nullptr, nullptr, nullptr, nullptr};
+    int nitems[dgk::kMultiCfgs] = {0, 0, 0, 0};
     dgk::MultiSmem sm[dgk::kMultiCfgs];
-    size_t smem[dgk::kMultiCfgs] = {0, 0, 0};
-    int grid[dgk::kMultiCfgs] = {0, 0, 0};
+    size_t smem[dgk::kMultiCfgs] = {0, 0, 0, 0};
+    int grid[dgk::kMultiCfgs] = {0, 0, 0, 0};
+    // per-order configuration: item range, grid and shared memory of each order
+    int ord_start[6] = {0, 0, 0, 0, 0, 0}, ord_n[6] = {0, 0, 0, 0, 0, 0}, ord_grid[6] = {0, 0, 0, 0, 0, 0};
+    size_t ord_smem[6] = {0, 0, 0, 0, 0, 0};
     int cfg = 1;
     std::vector<double> cur_dt;  // dt per mesh baked into the device stage arguments
     // sources
@@ -274,6 +326,24 @@ template <typename Real>
 cudaError_t launch_multi_stage(dg_multi *c, int stage) {
     static const dgk::MultiKernels<Real> ks = dgk::multi_kernels<Real>();
     const int k = c->cfg;
+    if (k == dgk::kMultiPerOrder) {
+        // one launch per order, highest first (running the orders on
+        // concurrent streams measured slower: the persistent grids compete)
+        const dgk::MultiMesh<Real> *meshes = (const dgk::MultiMesh<Real> *)c->d_meshes;
+        for (int p = 5; p >= 1; --p) {
+            if (!c->ord_n[p]) continue;
+            const int2 *items = c->d_items[k] + c->ord_start[p];
+            int n = c->ord_n[p];
+            const Real *ops = (const Real *)c->d_ops[p];
+            const uint8_t *tabs = c->d_tabs[p];
+            void *args[] = {&meshes, &items, &n, &ops, &tabs};
+            const int threads = dgk::order_epb(p) * dgk::multi_np(p);
+            cudaError_t e = cudaLaunchKernel(ks.order[p][stage], dim3(c->ord_grid[p]), dim3(threads), args,
+                                             c->ord_smem[p], c->stream);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
     const dgk::MultiMesh<Real> *meshes = (const dgk::MultiMesh<Real> *)c->d_meshes;
     const int2 *items = c->d_items[k];
     int n = c->nitems[k];
@@ -311,6 +381,36 @@ int setup_cfgs(dg_multi *c) {
     int nsm = 0;
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
     for (int k = 0; k < dgk::kMultiCfgs; ++k) {
+        if (k == dgk::kMultiPerOrder) {
+            // items grouped by order, tiles of the single-mesh kernels' size
+            std::vector<int2> items;
+            for (int p = 5; p >= 1; --p) {
+                c->ord_start[p] = (int)items.size();
+                for (int i = 0; i < c->nmesh; ++i) {
+                    if (c->m[i].order != p) continue;
+                    const int epb = dgk::order_epb(p);
+                    const int nt = (c->m[i].K + epb - 1) / epb;
+                    for (int t = 0; t < nt; ++t) items.push_back(make_int2(i, t));
+                }
+                c->ord_n[p] = (int)items.size() - c->ord_start[p];
+                if (!c->ord_n[p]) continue;
+                const int np = dgk::multi_np(p), nfp = (p + 1) * (p + 2) / 2, epb = dgk::order_epb(p);
+                const int nops_pad = (3 * np * np + 4 * nfp * np + 3) / 4 * 4;
+                c->ord_smem[p] = (size_t)(nops_pad + epb * np * 4 + epb * 4 * nfp * 4) * c->rsize +
+                                 (4 * nfp + 6 * nfp + 15) / 16 * 16;
+                int per_sm = 0;
+                for (int s = 0; s < 4; ++s)
+                    CK(cudaFuncSetAttribute(ks.order[p][s], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)c->ord_smem[p]));
+                CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks.order[p][0], epb * np, c->ord_smem[p]));
+                if (per_sm < 1) return fail(DG_ERR_UNSUPPORTED, "per-order multi-mesh kernel does not fit on an SM");
+                c->ord_grid[p] = std::max(1, std::min(c->ord_n[p], per_sm * nsm));
+            }
+            c->nitems[k] = (int)items.size();
+            CK(cudaMalloc(&c->d_items[k], std::max<size_t>(items.size(), 1) * sizeof(int2)));
+            CK(cudaMemcpy(c->d_items[k], items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice));
+            continue;
+        }
         const int bt = dgk::kMultiBlocks[k];
         dgk::MultiSmem sm = {0, 0, 0};
         int tab = 0;
@@ -698,7 +798,7 @@ int dg_multi_info(dg_multi *c, long long *dofs_per_field, int *ncfg, int *cfg, i
     if (ncfg) *ncfg = dgk::kMultiCfgs;
     if (cfg) *cfg = c->cfg;
     if (block_threads)
-        for (int k = 0; k < dgk::kMultiCfgs; ++k) block_threads[k] = dgk::kMultiBlocks[k];
+        for (int k = 0; k < dgk::kMultiCfgs; ++k) block_threads[k] = k == dgk::kMultiPerOrder ? 0 : dgk::kMultiBlocks[k];
     return DG_OK;
 }
 

@@ -253,7 +253,8 @@ int dg_rk4_steps_noalloc(const dg_device_layout *layout, double *u, double *t, d
  * mesh per process): nmesh 3D meshes of any sizes and orders 1-5, each with
  * its own medium and mean flow, stepped together by one persistent launch
  * per RK4 stage (a list of (mesh, element tile) work items shared by the
- * CTAs), chunks of steps captured in CUDA graphs.  FP64 or FP32.  Every mesh
+ * CTAs), or one per order present (configuration 3), chunks of steps
+ * captured in CUDA graphs.  FP64 or FP32.  Every mesh
  * has its own time t[i] and step dt[i]. */
 typedef struct dg_multi dg_multi;
 int dg_multi_create(int nmesh, const dg_mesh_desc *meshes, const dg_phys_desc *phys, const dg_opts *opts,
@@ -266,10 +267,13 @@ int dg_multi_set_sources(dg_multi *ctx, int nsrc, const int *mesh, const int *of
                          const double *weights, const double *params);
 int dg_multi_rk4_steps(dg_multi *ctx, double *t, const double *dt, int nsteps);
 int dg_multi_rk4_steps_timed(dg_multi *ctx, double *t, const double *dt, int nsteps, double *ms);
-/* Tile configurations: CTA sizes (block_threads[k]); elements per CTA =
- * block threads / element nodes for each order.  dg_multi_autotune times
- * each on trial_steps steps of the batch (the state is restored), keeps the
- * fastest and reports ms per step of every candidate. */
+/* Configurations: 0-2 make one persistent launch per stage for all meshes
+ * with CTAs of block_threads[k] threads (elements per CTA = block threads /
+ * element nodes for each order); 3 (block_threads 0) makes one persistent
+ * launch per order present, each with the CTA size and shared memory of the
+ * single-mesh kernels of that order.  dg_multi_autotune times each on
+ * trial_steps steps of the batch (the state is restored), keeps the fastest
+ * and reports ms per step of every candidate. */
 int dg_multi_set_config(dg_multi *ctx, int cfg);
 int dg_multi_autotune(dg_multi *ctx, const double *dt, int trial_steps, int *chosen, double *ms_per_step);
 int dg_multi_info(dg_multi *ctx, long long *dofs_per_field, int *ncfg, int *cfg, int *block_threads);
