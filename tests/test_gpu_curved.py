@@ -145,3 +145,32 @@ def test_mixed_form_rejects_curved_elements():
     with pytest.raises(D.DGError) as ei:
         D.Solver(pre, C0, RHO0, precision="mixed")
     assert ei.value.code == -3
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-5)])
+def test_curved_batch_sources_and_receivers(precision, tol):
+    """Members of a batch on a partly curved mesh, each with its own pulse
+    and source (reference type or Gaussian-weighted), against their own
+    oracle runs; receivers record the pressure after every step."""
+    from test_gpu_batch import batch_sources, member_inputs, oracle_member
+
+    m, pre = curved_mesh(3, 2, warp=bump3)
+    assert 0 < pre.num_curved < pre.num_el
+    dt = 0.5 * D.cfl_dt(pre, C0)
+    inputs = member_inputs(pre, 3, seed=21)
+    rec = np.random.default_rng(2).choice(pre.ndof, 5, replace=False).astype(np.int32)
+    nsteps = 17
+    sol = D.Solver(pre, C0, RHO0, precision=precision, flux="upwind", nbatch=3)
+    for k, inp in enumerate(inputs):
+        sol.set_state(inp[0], member=k)
+    sol.set_batch_sources(batch_sources(pre, inputs))
+    sol.set_receivers(rec, max_steps=nsteps)
+    t = sol.rk4_steps(0.0, dt, nsteps)
+    tr = sol.traces()
+    for k, inp in enumerate(inputs):
+        got = sol.get_state(member=k)
+        t_ref, ref = oracle_member(m, dt, inp, nsteps, upwind=True)
+        assert t == t_ref
+        for q in range(4):
+            assert rel(got[q], ref[q]) <= tol, (k, q, rel(got[q], ref[q]))
+        assert np.array_equal(tr[k, :, -1], got[0][rec])

@@ -100,6 +100,33 @@ def test_graph_and_direct_launches_agree():
     assert np.array_equal(a, b)
 
 
+def test_config1_fp64_1000_steps_matches_oracle():
+    """The reference's CPU-runnable case in full: [-1,1]^2 as 64x64 cells x 2
+    triangles (8192 elements), order 3, reflecting walls, Gaussian pulse at
+    the origin (size 0.02), dt from CFL 0.5, 1000 RK4 steps.  The oracle runs
+    its de-duplicated face loop (bit-identical to the reference's nested
+    loop, tests/test_oracle.py) on every host core."""
+    import os
+
+    mesh = D.Mesh.box_tri(64, 64, (-1.0, -1.0), (1.0, 1.0), order=3, side_names=("Reflecting",) * 4)
+    pre = D.Precomp(mesh)
+    assert pre.num_el == 8192
+    dt = D.cfl_dt(pre, C0)
+    u0 = pre.initial_state([(0, 0.0, 0.0, 0.0, 0.02, 1.0)])
+    sol = D.Solver(pre, C0, RHO0)
+    sol.set_state(u0)
+    t = sol.rk4_steps(0.0, dt, 1000)
+    got = sol.get_state()
+    orc = O.Oracle(mesh.raw(), dt, C0, RHO0, bcs=mesh.bcs(), num_threads=os.cpu_count() or 1)
+    orc.set_state(u0)
+    t_ref, _ = orc.run(0.0, 1000, dedup=True)
+    ref = orc.get_state()
+    assert t == t_ref
+    for q in range(3):
+        assert rel_l2(got[q], ref[q]) <= FP64_TOL, (q, rel_l2(got[q], ref[q]))
+    assert np.all(got[3] == 0)
+
+
 @pytest.mark.parametrize("dim,order", [(2, 3), (3, 3)])
 def test_fp32_close_to_oracle(dim, order):
     got, ref, dim = run_pair(dim, order, "mixed", precision="fp32", flux="upwind")
