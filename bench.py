@@ -545,8 +545,8 @@ def curved_flops(pre, info) -> float:
 def curved_section(D, args, local):
     """Curved (isoparametric) elements: unit cube n^3 x 6 tets, order 3, its
     nodes moved by a smooth map that curves every element ("full") or the
-    elements with x > 1/2 ("half"), against the straight cube; FP64 and FP32
-    contexts; RK4.  Per variant the whole-step rate, and the per-point
+    elements with x > 1/2 ("half"), against the straight cube; FP64, FP32 and
+    mixed contexts; RK4.  Per variant the whole-step rate, and the per-point
     kernel's device time per launch (CUDA events) with its FP64/FP32
     arithmetic rate and HBM bytes rate.  CPU baseline: the oracle (per-point
     form for every element, as the reference) on a smaller fully curved cube."""
@@ -561,7 +561,7 @@ def curved_section(D, args, local):
         dt = D.cfl_dt(pre, C0)
         u0 = pre.initial_state([(0, 0.5, 0.5, 0.5, 2 * SIGMA ** 2, 1.0)])
         units = pre.ndof * 4 * 4
-        for prec in ("fp64", "fp32"):
+        for prec in ("fp64", "fp32", "mixed"):
             s = D.Solver(pre, C0, RHO0, precision=prec, flux=FLUX, device=local)
             s.set_state(u0)
             t = s.rk4_steps(0.0, dt, args.warmup)
@@ -574,6 +574,7 @@ def curved_section(D, args, local):
             if kt["curved_launches"]:
                 cms = kt["curved_ms"] / kt["curved_launches"]
                 rb = 8 if prec == "fp64" else 4
+                # the mixed form also reads the state's low part and writes it in the last stage
                 C, ng, ngf = info["curved"], info["curved_points"], info["curved_face_points"]
                 # per curved element: inverse mass, metric, face data (context precision), state
                 # (stage input, u, acc read; acc, next input written: about 5 values per DOF)
@@ -586,7 +587,7 @@ def curved_section(D, args, local):
             out["variants"].append(v)
             s.close()
         log(f"[bench] curved {kind}: {pre.num_curved}/{pre.num_el} curved, "
-            + ", ".join(f"{x['form']} {x['value'] / 1e9:.2f} G" for x in out["variants"][-2:]))
+            + ", ".join(f"{x['form']} {x['value'] / 1e9:.2f} G" for x in out["variants"][-3:]))
     if not args.no_cpu_baseline:
         sys.path.insert(0, str(ROOT / "oracle"))
         import oracle_py as O

@@ -63,6 +63,9 @@ struct dg_ctx {
     void *d_cedata = nullptr;                                        // context precision
     void *d_cphi = nullptr, *d_cdphi = nullptr, *d_cfphi = nullptr;
     double *d_cwdet = nullptr, *d_cphi64 = nullptr;                // FP64, for the monitors
+    unsigned long long *d_cmask = nullptr;  // mixed form: curved elements per tensor-core tile
+    int *d_blist = nullptr;                 // mixed form: element blocks with a straight element
+    int nblk = 0;
     int2 *d_cfconn = nullptr;
     uint8_t *d_cfmap = nullptr;
     // graph cache

@@ -60,6 +60,11 @@ struct CurvedArgs {
     int mstride;           // bytes per element in fmap (a multiple of 16)
     int stage;             // 0-3 RK4 stages, 4 forward Euler
     Real dt, rc2, inv_rho, half_c0, c0, rho, v0[3];
+    // state kept as an FP32 pair (mixed-form contexts): the low part of u and
+    // where the new low part goes (u's for RK4, the Euler target's); null
+    // otherwise
+    const Real *ulo = nullptr;
+    Real *olo = nullptr;
 };
 
 // Element data of one curved element, in Reals: inverse mass [np*np] at 0,
@@ -414,6 +419,31 @@ __global__ void __launch_bounds__(256) curved_stage_kernel(const CurvedArgs<Real
                 const Real rv = a.dt * sum[q];
                 const Real qv = q4[q];
                 const long long idx = q * a.fstride + ebase;
+                if (a.ulo) {
+                    // the mixed form's update of a state kept as an FP32 pair
+                    // (the same formulas as its tensor-core stage kernel)
+                    const Real pu = uu[idx], pl = a.ulo[boff + idx];
+                    if (a.stage == 0) {
+                        acc[idx] = rv;
+                        wout[idx] = pu + (pl + Real(0.5) * rv);
+                    } else if (a.stage == 1) {
+                        acc[idx] = fma(Real(2), rv, acc[idx]);
+                        wout[idx] = pu + (pl + Real(0.5) * rv);
+                    } else if (a.stage == 2) {
+                        acc[idx] = fma(Real(2), rv, acc[idx]);
+                        wout[idx] = pu + (pl + rv);
+                    } else {
+                        const Real dlt = a.stage == 4 ? rv : (acc[idx] + rv) * (Real(1) / Real(6));
+                        const Real s = pu + dlt;
+                        const Real bp = s - pu;
+                        Real e = (pu - (s - bp)) + (dlt - bp);
+                        e += pl;
+                        const Real nh = s + e;
+                        wout[idx] = nh;
+                        a.olo[boff + idx] = e - (nh - s);
+                    }
+                    continue;
+                }
                 if (a.stage == 0) {
                     acc[idx] = rv;
                     wout[idx] = fma(Real(0.5), rv, qv);

@@ -71,6 +71,12 @@ struct MixedArgs {
     float rc2, inv_rho, half_c0, c0, rho;
     float v0[3];
     int *err;              // set to 1 on a wait timeout
+    // meshes with curved elements: bit le of cmask[block] marks element
+    // block*ELEMS + le as curved (its update comes from the per-point kernel,
+    // this kernel leaves it alone); null when no element is curved
+    const unsigned long long *cmask;
+    const int *blist;      // element blocks to run (those with a straight element), or null: all
+    int nblk;              // entries of blist
 };
 
 

@@ -351,6 +351,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     static_assert(NX >= 1, "at least three accumulators");
     static_assert(MS::ACC + (MS::NACC - 1) * NPAD + (NWG - 1) * NPP + 8 * NCH <= MS::TMEM_COLS,
                   "epilogue loads stay inside the allocation");
+    static_assert(ELEMS <= 64, "curved-element mask holds 64 elements per tile");
     extern __shared__ __align__(1024) unsigned char smem[];
     float *sA = reinterpret_cast<float *>(smem + MS::OFF_A);
     float *sMax = reinterpret_cast<float *>(smem + MS::OFF_MAX);
@@ -404,12 +405,16 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     // is reused from L2).
     // (tile counts stay below 2^31, checked on the host: 32-bit division,
     // none at all for a single member)
-    const long long ntiles = (long long)((a.K + ELEMS - 1) / ELEMS) * a.nbatch;
+    // meshes with curved elements: only the element blocks in a.blist (those
+    // with at least one straight element)
+    const long long nblocks = a.blist ? (long long)a.nblk : (long long)((a.K + ELEMS - 1) / ELEMS);
+    const long long ntiles = nblocks * a.nbatch;
     const unsigned nbu = (unsigned)a.nbatch;
     auto tile_base = [&](long long T, long long &eb, long long &mo) {
         const unsigned t32 = (unsigned)T;
         const unsigned et = nbu == 1u ? t32 : t32 / nbu;
-        eb = (long long)et * ELEMS;
+        const unsigned blk = a.blist ? (unsigned)__ldg(&a.blist[et]) : et;
+        eb = (long long)blk * ELEMS;
         mo = (long long)(t32 - et * nbu) * a.bstride;
     };
     if ((long long)blockIdx.x < ntiles) {
@@ -646,7 +651,8 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
                 }
             }
             __syncthreads();
-            if (vec && ebase + ELEMS <= a.K) {
+            const unsigned long long cm = a.cmask ? a.cmask[ebase / ELEMS] : 0ull;
+            if (vec && ebase + ELEMS <= a.K && cm == 0ull) {
                 constexpr int W = ELEMS * NP / 4;
                 for (int idx = tid; idx < NQ * W; idx += NT) {
                     const int f = idx / W, w = idx - f * W;
@@ -657,7 +663,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             } else {
                 for (int idx = tid; idx < NQ * ELEMS * NP; idx += NT) {
                     const int f = idx / (ELEMS * NP), rem = idx - f * (ELEMS * NP);
-                    if (ebase + rem / NP >= a.K) continue;
+                    if (ebase + rem / NP >= a.K || ((cm >> (rem / NP)) & 1ull)) continue;
                     const long long g = moff + f * a.fstride + ebase * NP + rem;
                     out_lo[g] = sO0[idx];
                     a.wout[g] = sO1[idx];

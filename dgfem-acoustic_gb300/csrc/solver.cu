@@ -155,7 +155,8 @@ void free_ctx(dg_ctx *c) {
                     c->d_src_at, c->d_src_off, c->d_src_list, c->d_src_w, c->d_src_params, c->d_ulo,
                     c->d_bimg,  c->d_beb,     c->d_err,     c->d_rec_dof, c->d_trace,   c->d_step0,
                     c->d_geo32, c->d_cel,     c->d_cslot,   c->d_cedata,  c->d_cwdet,   c->d_cphi,
-                    c->d_cdphi, c->d_cfphi,   c->d_cfconn,  c->d_cfmap,   c->d_cphi64,  c->d_aff};
+                    c->d_cdphi, c->d_cfphi,   c->d_cfconn,  c->d_cfmap,   c->d_cphi64,  c->d_aff,
+                    c->d_cmask, c->d_blist};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -228,13 +229,21 @@ cudaError_t launch_curved(dg_ctx *c, int stage, double dt) {
     a.c0 = s.c0;
     a.rho = s.rho;
     for (int k = 0; k < 3; ++k) a.v0[k] = s.v0[k];
+    if (c->mixed) {
+        // the state is an FP32 pair: low part in, new low part out (RK4: u's;
+        // forward Euler: the target buffer's, swapped in after the step)
+        a.ulo = reinterpret_cast<const Real *>(c->d_ulo);
+        a.olo = stage == kEulerStage ? static_cast<Real *>(c->d_acc) : reinterpret_cast<Real *>(c->d_ulo);
+    }
     void *args[] = {&a};
     return cudaLaunchKernel(c->curved_fn, dim3(c->curved_grid, c->nbatch, 1), dim3(256, 1, 1), args,
                             c->curved_smem, c->stream);
 }
 
 cudaError_t launch_stage(dg_ctx *c, int stage, double dt) {
-    cudaError_t e = launch_affine_stage(c, stage, dt);
+    // no straight element at all: nothing for the affine / tensor-core kernel
+    const bool none = c->curved > 0 && (c->mixed ? c->nblk == 0 : c->naff == 0);
+    cudaError_t e = none ? cudaSuccess : launch_affine_stage(c, stage, dt);
     if (e != cudaSuccess || c->curved == 0) return e;
     return c->prec == DG_PREC_FP64 ? launch_curved<double>(c, stage, dt) : launch_curved<float>(c, stage, dt);
 }
@@ -259,7 +268,10 @@ cudaError_t launch_affine_stage(dg_ctx *c, int stage, double dt) {
         a.bimg = c->d_bimg;
         a.beb = c->d_beb;
         a.tabs = s.tabs;
-        a.K = s.K;
+        a.K = c->K;  // element blocks of the whole mesh; curved elements are masked
+        a.cmask = c->d_cmask;
+        a.blist = c->d_blist;
+        a.nblk = c->nblk;
         a.dt = s.dt;
         a.rc2 = s.rc2;
         a.inv_rho = s.inv_rho;
@@ -393,10 +405,7 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
     for (int k = 0; k < 3; ++k) c->v0[k] = ph->v0[k];
     c->mixed = c->prec == DG_PREC_MIXED;
     c->naff = lay.curved.C > 0 ? (int)lay.curved.affine.size() : K;
-    if (c->mixed && lay.curved.C > 0) {
-        free_ctx(c);
-        return fail(DG_ERR_UNSUPPORTED, "curved elements run in the fp64 and fp32 forms, not the mixed form");
-    }
+
     // the mixed form keeps FP32 stage data and uses the FP32 helper kernels
     if (!dgk::get_kernels(c->mixed ? DG_PREC_FP32 : c->prec, dim, m->order, &c->ks)) {
         free_ctx(c);
@@ -571,6 +580,24 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
             if (!up(cv.wdet.data(), cv.wdet.size() * 8, (void **)&c->d_cwdet)) break;
             if (!up(cv.phi.data(), cv.phi.size() * 8, (void **)&c->d_cphi64)) break;
             if (!up(cv.affine.data(), cv.affine.size() * 4, (void **)&c->d_aff)) break;
+            if (c->mixed) {
+                // per element block of the tensor-core kernel: which elements are curved
+                const int el = c->mks.elems_per_tile;
+                std::vector<unsigned long long> msk((K + el - 1) / el, 0ull);
+                for (int e : cv.el) msk[e / el] |= 1ull << (e % el);
+                if (!up(msk.data(), msk.size() * 8, (void **)&c->d_cmask)) break;
+                // blocks whose elements are all curved are left to the per-point kernel
+                std::vector<int> bl;
+                for (size_t b = 0; b < msk.size(); ++b) {
+                    const int n = std::min(el, K - (int)b * el);
+                    const unsigned long long full = n == 64 ? ~0ull : ((1ull << n) - 1ull);
+                    if (msk[b] != full) bl.push_back((int)b);
+                }
+                c->nblk = (int)bl.size();
+                if (!up(bl.data(), bl.size() * 4, (void **)&c->d_blist)) break;
+                const long long mt = (long long)c->nblk * nbatch;
+                c->grid = (int)std::max(1LL, std::min(mt, (long long)nsm));
+            }
             if (!up(cv.fconn.data(), cv.fconn.size() * 4, (void **)&c->d_cfconn)) break;
             int cper = 0;
             if (!fin(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cper, c->curved_fn, 256, c->curved_smem),

@@ -140,11 +140,42 @@ def test_curved_msh_round_trip_runs(tmp_path):
         assert rel(got[q], ref[q]) <= 1e-10
 
 
-def test_mixed_form_rejects_curved_elements():
-    m, pre = curved_mesh(3, 2)
-    with pytest.raises(D.DGError) as ei:
-        D.Solver(pre, C0, RHO0, precision="mixed")
-    assert ei.value.code == -3
+@pytest.mark.parametrize("dim,order,warp", [(3, 3, "bump"), (3, 2, "full"), (2, 3, "full")])
+def test_mixed_form_on_curved_meshes(dim, order, warp):
+    """Mixed form on curved meshes: straight elements on the tensor-core
+    kernel, curved ones on the per-point kernel in FP32 with the same FP32-pair
+    state update; 1e-6 relative L2 against the oracle over a short run, as
+    for straight meshes."""
+    m, pre = curved_mesh(dim, order, warp=bump3 if warp == "bump" else None)
+    v0 = (30.0, -20.0, 10.0 if dim == 3 else 0.0)
+    s, ref = run_pair(m, pre, 15, precision="mixed", flux="upwind", v0=v0)
+    assert s.info()["curved"] == pre.num_curved
+    got = s.get_state()
+    for q in range(dim + 1):
+        assert rel(got[q], ref[q]) <= 1e-6, (q, rel(got[q], ref[q]))
+
+
+def test_mixed_form_on_curved_mesh_batch_euler_and_long_run():
+    """Forward Euler and a batch in the mixed form on a partly curved mesh,
+    and 400 RK4 steps against the FP64 form (1e-5)."""
+    m, pre = curved_mesh(3, 3, warp=bump3)
+    s, ref = run_pair(m, pre, 9, precision="mixed", flux="upwind", method="euler")
+    got = s.get_state()
+    for q in range(4):
+        assert rel(got[q], ref[q]) <= 1e-6, (q, rel(got[q], ref[q]))
+    dt = 0.5 * D.cfl_dt(pre, C0)
+    us = [initial(pre, seed=k) for k in range(2)]
+    mx = D.Solver(pre, C0, RHO0, precision="mixed", flux="upwind", nbatch=2)
+    f64 = D.Solver(pre, C0, RHO0, precision="fp64", flux="upwind", nbatch=2)
+    for k, u in enumerate(us):
+        mx.set_state(u, member=k)
+        f64.set_state(u, member=k)
+    mx.rk4_steps(0.0, dt, 400)
+    f64.rk4_steps(0.0, dt, 400)
+    for k in range(2):
+        a, b = mx.get_state(member=k), f64.get_state(member=k)
+        for q in range(4):
+            assert rel(a[q], b[q]) <= 1e-5, (k, q, rel(a[q], b[q]))
 
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32", 1e-5)])
