@@ -612,7 +612,7 @@ def parareal_section(D, args, local):
     parareal (one fine step per application) for a pulse at another
     position; fine propagator = the FP64 DG over all slices as one batch.
     Compared with parareal without the network (identity coarse propagator)
-    and with the serial FP64 DG, which judges the error."""
+    and with the serial FP64 DG, against which the error is measured."""
     from dgcuda import workloads as W
 
     t0 = time.time()

@@ -11,8 +11,8 @@
 //   U[0] = u0;  U[n+1] = G(U[n])                                   (k = 0)
 //   U[n+1] <- G(U_new[n]) + F(U_old[n]) - G(U_old[n])               (k >= 1)
 // After k iterations the first k slices are exact, so parareal always ends
-// at the DG answer by iteration N; the DG is the judge of its error (the
-// update size) and the fallback (iterations up to N).
+// at the DG answer by iteration N; the DG measures its error (the update
+// size) and is the fallback (iterations up to N).
 #include <cuda_runtime.h>
 
 #include <algorithm>

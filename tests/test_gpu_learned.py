@@ -1,6 +1,6 @@
 """The learned part: the GPU MLP kernels against the float64 NumPy oracle
 (forward, loss and gradients), training, and parareal with the identity and
-with the learned coarse propagator, judged by the serial FP64 DG."""
+with the learned coarse propagator, measured against the serial FP64 DG."""
 from __future__ import annotations
 
 import numpy as np
