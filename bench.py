@@ -612,7 +612,8 @@ def parareal_section(D, args, local):
     parareal (one fine step per application) for a pulse at another
     position; fine propagator = the FP64 DG over all slices as one batch.
     Compared with parareal without the network (identity coarse propagator)
-    and with the serial FP64 DG, against which the error is measured."""
+    and with the serial FP64 DG, against which the error is measured; the
+    network runs with FP32 inference and with BF16 tensor-core inference."""
     from dgcuda import workloads as W
 
     t0 = time.time()
@@ -640,7 +641,19 @@ def parareal_section(D, args, local):
            "training": {"pairs": L.num_samples(), "epochs": args.parareal_epochs, "final_loss": loss,
                         "collect_s": t_collect, "train_s": t_train},
            "serial_fp64_ms": ms_serial}
-    for name, lrn in (("learned", L), ("identity", None)):
+    # one coarse application (features, network, energy-stable update) with
+    # FP32 and with BF16 tensor-core inference
+    napp = 200
+    for mode in ("fp32", "bf16"):
+        L.set_inference(mode)
+        L.apply(u0, 5)
+        w0 = time.perf_counter()
+        L.apply(u0, napp)
+        out[f"coarse_application_ms_{mode}"] = (time.perf_counter() - w0) * 1e3 / napp
+    L.set_inference("fp32")
+    for name, lrn, mode in (("learned", L, "fp32"), ("learned_bf16", L, "bf16"), ("identity", None, "fp32")):
+        if lrn is not None:
+            lrn.set_inference(mode)
         w0 = time.perf_counter()
         u, it, hist = D.parareal(pre, C0, RHO0, u0, nsl, sst, dt, tol=args.parareal_tol, max_iter=nsl, learned=lrn,
                                  flux=FLUX)

@@ -13,6 +13,7 @@
 // After k iterations the first k slices are exact, so parareal always ends
 // at the DG answer by iteration N; the DG measures its error (the update
 // size) and is the fallback (iterations up to N).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,6 +26,9 @@
 
 #include "../../include/dgcuda.h"
 #include "ctx.h"
+#include "mlp_common.cuh"
+
+using dgk::gelu_f;
 #include "host/capi_common.h"
 #include "host/layout.h"
 
@@ -49,10 +53,6 @@ int cuda_fail(cudaError_t e, const char *what) {
 // gelu_out, C receives the pre-activation and gelu_out the GELU of it.
 constexpr int GB = 64, GK = 16;
 
-__device__ __forceinline__ float gelu_f(float x) {
-    const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
-    return 0.5f * x * (1.0f + tanhf(u));
-}
 __device__ __forceinline__ float gelu_grad(float x) {
     const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
     const float t = tanhf(u);
@@ -262,11 +262,15 @@ __global__ void __launch_bounds__(128) features_kernel(FeatArgs a, float *X, flo
 // u[f*ndof + e*np + i] = alpha * (u + out_scale[f] * escale[e] * Y[e][f*np + i])
 __global__ void apply_increment_kernel(double *u, long long ndof, int K, int np, int nq, const float *Y,
                                        const float *escale, double s0, double s1, double s2, double s3,
-                                       double alpha) {
+                                       const double *alpha_p) {
+    const double alpha = *alpha_p;
+    if (alpha == 0.0) return;  // a non-finite prediction leaves the state unchanged
     const double sc[4] = {s0, s1, s2, s3};
     const long long n = (long long)K * np * nq;
+    const unsigned npq = (unsigned)(np * nq);
+    const bool i32 = n < (1LL << 31);
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const long long e = t / (np * nq);
+        const long long e = i32 ? (long long)((unsigned)t / npq) : t / (np * nq);
         const int r = (int)(t - e * np * nq), f = r / np, i = r - f * np;
         const long long at = f * ndof + e * np + i;
         u[at] = alpha * (u[at] + sc[f] * (double)escale[e] * (double)Y[t]);
@@ -284,9 +288,12 @@ __global__ void energy_products_kernel(const double *u, long long ndof, int K, i
                                        const double *detj, double wp, double wv, double *part) {
     const double sc[4] = {s0, s1, s2, s3};
     const long long n = (long long)K * np * nq;
+    const unsigned npq = (unsigned)(np * nq);
+    const bool i32 = n < (1LL << 31);
     double ud = 0.0, dd = 0.0, uu = 0.0;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const long long e = t / (np * nq);
+        // 32-bit division while the index fits
+        const long long e = i32 ? (long long)((unsigned)t / npq) : t / (np * nq);
         const int r = (int)(t - e * np * nq), f = r / np, i = r - f * np;
         const double d = sc[f] * (double)escale[e] * (double)Y[t];
         const double w = detj[e] * (f == 0 ? wp : wv);
@@ -330,6 +337,20 @@ __global__ void sum_parts_kernel(const double *part, int nparts, double *out) {
     }
     if (threadIdx.x == 0)
         for (int k = 0; k < 3; ++k) out[k] = r[k][0];
+}
+
+// Step factor of a coarse application from its energy products (prod =
+// <u,d>, <d,d>, <u,u>): 1, or sqrt(E(u) / E(u + d)) if u + d has more energy;
+// 0 when the prediction is not finite.  Running statistics in stats: sum of
+// the factors, their minimum, the number of applications.
+__global__ void step_factor_kernel(const double *prod, double *alpha_out, double *stats) {
+    const double e_old = prod[2], e_new = prod[2] + 2.0 * prod[0] + prod[1];
+    double alpha = 1.0;
+    if (e_new > e_old && e_new > 0.0) alpha = sqrt(e_old / e_new);
+    stats[0] += alpha;
+    stats[1] = fmin(stats[1], alpha);
+    stats[2] += 1.0;
+    *alpha_out = (isfinite(e_new) && isfinite(alpha)) ? alpha : 0.0;
 }
 
 // Training targets: (u1 - u0) per element in output order, divided by the
@@ -382,6 +403,17 @@ int grid_for(long long n) { return (int)std::max<long long>(1, std::min<long lon
 
 }  // namespace
 
+// FP32 -> BF16 (round to nearest even), zero-padded: dst[r][c] for c < kp
+// (cols < width copied, the rest 0), r < rows.
+// Row-major with 32-bit indices: rows * kp < 2^31 (checked by the caller).
+__global__ void to_bf16_kernel(const float *src, int rows, int width, int lds, __nv_bfloat16 *dst, int kp) {
+    const unsigned n = (unsigned)rows * (unsigned)kp;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned r = i / (unsigned)kp, c = i - r * (unsigned)kp;
+        dst[i] = __float2bfloat16_rn((int)c < width ? src[(size_t)r * lds + c] : 0.0f);
+    }
+}
+
 // ---------------------------------------------------------------- the MLP
 
 struct dg_mlp {
@@ -398,11 +430,28 @@ struct dg_mlp {
     double *d_loss = nullptr;
     cudaStream_t stream = nullptr;
     int device = 0;
+    // BF16 tensor-core inference: weights rounded to BF16, padded to [np][kp]
+    // (np a multiple of 16, kp of 64), refreshed when the FP32 weights change;
+    // BF16 activations [cap][kp of the next layer]
+    std::vector<int> npad, kpad;
+    std::vector<__nv_bfloat16 *> wbf;
+    bool bf_dirty = true;
+    int bf_cap = 0;
+    std::vector<__nv_bfloat16 *> abf;  // abf[l]: BF16 input of layer l
+    int *d_err = nullptr;
 };
 
 namespace {
 
+void free_bf16_buffers(dg_mlp *n) {
+    for (auto *p : n->abf)
+        if (p) cudaFree(p);
+    n->abf.clear();
+    n->bf_cap = 0;
+}
+
 void free_mlp_buffers(dg_mlp *n) {
+    free_bf16_buffers(n);
     for (float *p : n->Z) cudaFree(p);
     for (size_t l = 1; l < n->A.size(); ++l) cudaFree(n->A[l]);
     n->Z.clear();
@@ -434,6 +483,64 @@ int ensure_rows(dg_mlp *n, int rows) {
     CK(cudaMalloc(&n->d_X, (size_t)cap * n->nin * 4));
     CK(cudaMalloc(&n->d_rows, (size_t)cap * 4));
     n->cap = cap;
+    return DG_OK;
+}
+
+// BF16 weights and activation buffers of the tensor-core inference path.
+int ensure_bf16(dg_mlp *n, int rows) {
+    if (n->width > 256 || n->nout > 256) return fail(DG_ERR_UNSUPPORTED, "BF16 inference needs layers of at most 256");
+    if ((long long)rows * ((n->nin + 63) / 64 * 64) >= (1LL << 31) || (long long)rows * 256 >= (1LL << 31))
+        return fail(DG_ERR_UNSUPPORTED, "too many rows for BF16 inference");
+    if (n->wbf.empty()) {
+        for (int l = 0; l < n->layers; ++l) {
+            n->npad.push_back((n->dout[l] + 15) / 16 * 16);
+            n->kpad.push_back((n->din[l] + 63) / 64 * 64);
+            __nv_bfloat16 *w = nullptr;
+            CK(cudaMalloc(&w, (size_t)n->npad[l] * n->kpad[l] * 2));
+            CK(cudaMemset(w, 0, (size_t)n->npad[l] * n->kpad[l] * 2));
+            n->wbf.push_back(w);
+        }
+        CK(cudaMalloc(&n->d_err, sizeof(int)));
+        CK(cudaMemset(n->d_err, 0, sizeof(int)));
+        n->bf_dirty = true;
+    }
+    if (n->bf_dirty) {
+        for (int l = 0; l < n->layers; ++l)
+            to_bf16_kernel<<<grid_for((long long)n->dout[l] * n->kpad[l]), 256, 0, n->stream>>>(
+                n->d_p + n->woff[l], n->dout[l], n->din[l], n->din[l], n->wbf[l], n->kpad[l]);
+        CK(cudaGetLastError());
+        n->bf_dirty = false;
+    }
+    if (rows > n->bf_cap) {
+        free_bf16_buffers(n);
+        const int cap = std::max(rows, 1024);
+        n->abf.assign(n->layers, nullptr);
+        for (int l = 0; l < n->layers; ++l) {
+            // padding columns stay zero: the kernels write columns < din only
+            CK(cudaMalloc(&n->abf[l], (size_t)cap * n->kpad[l] * 2));
+            CK(cudaMemset(n->abf[l], 0, (size_t)cap * n->kpad[l] * 2));
+        }
+        n->bf_cap = cap;
+    }
+    return DG_OK;
+}
+
+// Inference of `rows` rows of X (device, FP32) on the tensor cores with BF16
+// weights and activations and FP32 accumulation; output in n->d_Y (FP32).
+int mlp_forward_bf16(dg_mlp *n, const float *X, int rows) {
+    int rc = ensure_rows(n, rows);
+    if (rc == DG_OK) rc = ensure_bf16(n, rows);
+    if (rc != DG_OK) return rc;
+    to_bf16_kernel<<<grid_for((long long)rows * n->kpad[0]), 256, 0, n->stream>>>(X, rows, n->nin, n->nin, n->abf[0],
+                                                                                n->kpad[0]);
+    for (int l = 0; l < n->layers; ++l) {
+        const bool last = l + 1 == n->layers;
+        const int r = dgk::tc_linear(n->stream, rows, n->dout[l], n->npad[l], n->kpad[l], n->abf[l], n->wbf[l],
+                                     n->d_p + n->boff[l], !last, last ? nullptr : n->abf[l + 1],
+                                     last ? n->d_Y : nullptr, last ? n->nout : n->kpad[l + 1], n->d_err);
+        if (r != 0) return fail(DG_ERR_CUDA, "tensor-core linear layer launch failed");
+    }
+    CK(cudaGetLastError());
     return DG_OK;
 }
 
@@ -504,6 +611,7 @@ int mlp_adam(dg_mlp *n, float lr) {
     adam_kernel<<<grid_for(n->nparam), 256, 0, n->stream>>>(n->d_p, n->d_g, n->d_m, n->d_v, n->nparam, lr, b1, b2,
                                                            eps, c1, c2);
     CK(cudaGetLastError());
+    n->bf_dirty = true;
     return DG_OK;
 }
 
@@ -564,6 +672,9 @@ void dg_mlp_destroy(dg_mlp *n) {
     if (!n) return;
     cudaSetDevice(n->device);
     free_mlp_buffers(n);
+    for (auto *w : n->wbf)
+        if (w) cudaFree(w);
+    if (n->d_err) cudaFree(n->d_err);
     for (float *q : {n->d_p, n->d_g, n->d_m, n->d_v})
         if (q) cudaFree(q);
     if (n->d_loss) cudaFree(n->d_loss);
@@ -584,6 +695,23 @@ int dg_mlp_set_params(dg_mlp *n, const float *p) {
     if (!n || !p) return fail(DG_ERR_ARG, "null argument");
     CK(cudaSetDevice(n->device));
     CK(cudaMemcpy(n->d_p, p, (size_t)n->nparam * 4, cudaMemcpyHostToDevice));
+    n->bf_dirty = true;
+    return DG_OK;
+}
+
+int dg_mlp_forward_bf16(dg_mlp *n, const float *X, int rows, float *Y) {
+    if (!n || !X || !Y || rows < 1) return fail(DG_ERR_ARG, "bad arguments");
+    CK(cudaSetDevice(n->device));
+    int rc = ensure_rows(n, rows);
+    if (rc != DG_OK) return rc;
+    CK(cudaMemcpyAsync(n->d_X, X, (size_t)rows * n->nin * 4, cudaMemcpyHostToDevice, n->stream));
+    rc = mlp_forward_bf16(n, n->d_X, rows);
+    if (rc != DG_OK) return rc;
+    CK(cudaMemcpyAsync(Y, n->d_Y, (size_t)rows * n->nout * 4, cudaMemcpyDeviceToHost, n->stream));
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, n->d_err, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
+    CK(cudaStreamSynchronize(n->stream));
+    if (err) return fail(DG_ERR_CUDA, "tensor-core wait timed out in BF16 inference");
     return DG_OK;
 }
 
@@ -643,15 +771,15 @@ struct dg_learned {
     float *d_feat = nullptr;  // [K][nin]
     float *d_escale = nullptr;  // [K] input scale of each element
     double *d_detj = nullptr;   // [K] element Jacobian determinants
-    double *d_prod = nullptr;   // energy products of a coarse application
+    double *d_prod = nullptr;   // energy products of a coarse application, then its step factor
     double *d_parts = nullptr;  // their per-block partial sums
-    double alpha_sum = 0, alpha_min = 1;  // step factors of the applications so far
-    long long applications = 0;
+    double *d_stats = nullptr;  // step factors so far: sum, minimum, count
     std::vector<float *> samples_x, samples_t;  // device blocks of training rows
     std::vector<int> sample_rows;
     long long total_rows = 0;
     double *d_u0 = nullptr, *d_u1 = nullptr;  // FP64 scratch states
     int device = 0;
+    bool bf16 = false;  // coarse steps infer with BF16 tensor cores
 };
 
 namespace {
@@ -676,15 +804,16 @@ FeatArgs feat_args(dg_learned *L, const double *u) {
     return a;
 }
 
-// One coarse application on an FP64 state (device, member layout).
-int coarse_apply(dg_learned *L, double *u, cudaStream_t s) {
+// One coarse application on an FP64 state (device, member layout), enqueued
+// on the network's stream with no host synchronisation: features, network,
+// energy products, step factor (on the device) and the update.
+int coarse_apply(dg_learned *L, double *u) {
     dg_ctx *c = L->fine;
+    dg_mlp *n = L->net;
+    cudaStream_t s = n->stream;
     features_kernel<<<c->K, 128, 0, s>>>(feat_args(L, u), L->d_feat, L->d_escale);
     CK(cudaGetLastError());
-    dg_mlp *n = L->net;
-    // the MLP runs on its own stream: order it after the features
-    CK(cudaStreamSynchronize(s));
-    int rc = mlp_forward(n, L->d_feat, c->K);
+    int rc = L->bf16 ? mlp_forward_bf16(n, L->d_feat, c->K) : mlp_forward(n, L->d_feat, c->K);
     if (rc != DG_OK) return rc;
     // energy-stable step: u + d, scaled back to E(u) if it has more energy
     // (the upwind DG propagator with these walls never gains energy)
@@ -692,29 +821,14 @@ int coarse_apply(dg_learned *L, double *u, cudaStream_t s) {
     double os[4];
     for (int f = 0; f < 4; ++f) os[f] = (double)L->out_scale[f] * L->tscale[f];
     const int nb = grid_for(nv);
-    energy_products_kernel<<<nb, 256, 0, n->stream>>>(u, c->ndof, c->K, c->np, c->nq, n->d_Y, L->d_escale, os[0],
-                                                       os[1], os[2], os[3], L->d_detj,
-                                                       1.0 / (c->rho0 * c->c0 * c->c0), c->rho0, L->d_parts);
-    sum_parts_kernel<<<1, 256, 0, n->stream>>>(L->d_parts, nb, L->d_prod);
-    double pr[3];
-    CK(cudaMemcpyAsync(pr, L->d_prod, 24, cudaMemcpyDeviceToHost, n->stream));
-    CK(cudaStreamSynchronize(n->stream));
-    const double e_old = pr[2], e_new = pr[2] + 2.0 * pr[0] + pr[1];
-    double alpha = 1.0;
-    if (e_new > e_old && e_new > 0.0) alpha = std::sqrt(e_old / e_new);
-    const bool finite = std::isfinite(e_new) && std::isfinite(alpha);
-    L->alpha_sum += alpha;
-    L->alpha_min = std::min(L->alpha_min, alpha);
-    L->applications += 1;
-    if (!finite) {
-        // a non-finite prediction leaves the state unchanged
-        alpha = 0.0;
-    } else {
-        apply_increment_kernel<<<grid_for(nv), 256, 0, n->stream>>>(u, c->ndof, c->K, c->np, c->nq, n->d_Y,
-                                                                     L->d_escale, os[0], os[1], os[2], os[3], alpha);
-    }
+    energy_products_kernel<<<nb, 256, 0, s>>>(u, c->ndof, c->K, c->np, c->nq, n->d_Y, L->d_escale, os[0], os[1],
+                                              os[2], os[3], L->d_detj, 1.0 / (c->rho0 * c->c0 * c->c0), c->rho0,
+                                              L->d_parts);
+    sum_parts_kernel<<<1, 256, 0, s>>>(L->d_parts, nb, L->d_prod);
+    step_factor_kernel<<<1, 1, 0, s>>>(L->d_prod, L->d_prod + 3, L->d_stats);
+    apply_increment_kernel<<<grid_for(nv), 256, 0, s>>>(u, c->ndof, c->K, c->np, c->nq, n->d_Y, L->d_escale, os[0],
+                                                         os[1], os[2], os[3], L->d_prod + 3);
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(n->stream));
     return DG_OK;
 }
 
@@ -766,7 +880,12 @@ int dg_learned_create(const dg_mesh_desc *mesh, const dg_phys_desc *phys, int fl
     if (e == cudaSuccess) e = cudaMemcpy(L->d_geo, lay.geo.data(), lay.geo.size() * 8, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&L->d_feat, (size_t)c->K * L->nin * 4);
     if (e == cudaSuccess) e = cudaMalloc(&L->d_escale, (size_t)c->K * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&L->d_prod, 24);
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_prod, 32);
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_stats, 24);
+    if (e == cudaSuccess) {
+        const double st[3] = {0.0, 1.0, 0.0};
+        e = cudaMemcpy(L->d_stats, st, 24, cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMalloc(&L->d_parts, (size_t)3 * 4096 * 8);
     if (e == cudaSuccess) e = cudaMalloc(&L->d_detj, (size_t)c->K * 8);
     if (e == cudaSuccess) e = cudaMemcpy(L->d_detj, mesh->el_jacobian_dets, (size_t)c->K * 8, cudaMemcpyHostToDevice);
@@ -785,7 +904,8 @@ void dg_learned_destroy(dg_learned *L) {
     for (float *p : L->samples_x) cudaFree(p);
     for (float *p : L->samples_t) cudaFree(p);
     for (void *p : {(void *)L->d_conn, (void *)L->d_tabs, (void *)L->d_geo, (void *)L->d_feat, (void *)L->d_escale,
-                    (void *)L->d_prod, (void *)L->d_parts, (void *)L->d_detj, (void *)L->d_u0, (void *)L->d_u1})
+                    (void *)L->d_prod, (void *)L->d_parts, (void *)L->d_detj, (void *)L->d_u0, (void *)L->d_u1,
+                    (void *)L->d_stats})
         if (p) cudaFree(p);
     if (L->net) dg_mlp_destroy(L->net);
     if (L->fine) dg_destroy(L->fine);
@@ -800,11 +920,24 @@ int dg_learned_info(dg_learned *L, int *nin, int *nout, dg_mlp **net) {
     return DG_OK;
 }
 
+int dg_learned_set_inference(dg_learned *L, int bf16) {
+    if (!L) return fail(DG_ERR_ARG, "null argument");
+    if (bf16 && (L->net->width > 256 || L->net->nout > 256))
+        return fail(DG_ERR_UNSUPPORTED, "BF16 inference needs layers of at most 256");
+    L->bf16 = bf16 != 0;
+    return DG_OK;
+}
+
 int dg_learned_step_stats(dg_learned *L, long long *applications, double *alpha_mean, double *alpha_min) {
     if (!L) return fail(DG_ERR_ARG, "null argument");
-    if (applications) *applications = L->applications;
-    if (alpha_mean) *alpha_mean = L->applications ? L->alpha_sum / L->applications : 0.0;
-    if (alpha_min) *alpha_min = L->alpha_min;
+    CK(cudaSetDevice(L->device));
+    double st[3];
+    CK(cudaMemcpyAsync(st, L->d_stats, 24, cudaMemcpyDeviceToHost, L->net->stream));
+    CK(cudaStreamSynchronize(L->net->stream));
+    const long long napp = (long long)st[2];
+    if (applications) *applications = napp;
+    if (alpha_mean) *alpha_mean = napp ? st[0] / (double)napp : 0.0;
+    if (alpha_min) *alpha_min = st[1];
     return DG_OK;
 }
 
@@ -967,9 +1100,10 @@ int dg_learned_apply(dg_learned *L, double *const u[4], int napps) {
     for (int f = 0; f < c->nq; ++f)
         CK(cudaMemcpy(L->d_u0 + f * c->ndof, u[f], (size_t)c->ndof * 8, cudaMemcpyHostToDevice));
     for (int k = 0; k < napps; ++k) {
-        int rc = coarse_apply(L, L->d_u0, L->net->stream);
+        int rc = coarse_apply(L, L->d_u0);
         if (rc != DG_OK) return rc;
     }
+    CK(cudaStreamSynchronize(L->net->stream));
     for (int f = 0; f < c->nq; ++f)
         CK(cudaMemcpy(u[f], L->d_u0 + f * c->ndof, (size_t)c->ndof * 8, cudaMemcpyDeviceToHost));
     return DG_OK;
@@ -1015,9 +1149,10 @@ int dg_parareal(dg_learned *learned, const dg_mesh_desc *mesh, const dg_phys_des
             return fail(DG_ERR_ARG, "learned propagator built for another mesh");
         CK(cudaStreamSynchronize(s));
         for (int k = 0; k < slice_steps / learned->coarse_steps; ++k) {
-            int r = coarse_apply(learned, dst, learned->net->stream);
+            int r = coarse_apply(learned, dst);
             if (r != DG_OK) return r;
         }
+        CK(cudaStreamSynchronize(learned->net->stream));
         return DG_OK;
     };
     do {

@@ -1,6 +1,7 @@
 // Inline-PTX wrappers for the sm_100-family tensor-core path (tcgen05): tensor
-// memory allocation, stores and loads, BF16 MMA with A in tensor memory and B
-// in shared memory, commit to an mbarrier, and bounded mbarrier waits.
+// memory allocation, stores and loads, BF16 MMA with A in tensor memory or
+// shared memory and B in shared memory, commit to an mbarrier, and bounded
+// mbarrier waits.
 //
 // Shared-memory matrix descriptor (K-major, no swizzle): 8x16-byte core
 // matrices; LBO = byte distance between the two K-adjacent core matrices of
@@ -91,6 +92,17 @@ __device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, ui
         "setp.ne.u32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
         "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// D[tmem] (+)= A[smem desc] * B[smem desc]^T, kind::f16 (BF16, FP32 accumulate).
+__device__ __forceinline__ void mma_bf16_ss(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                            uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.u32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
 

@@ -160,6 +160,8 @@ def _declare(L: C.CDLL) -> None:
         "dg_mlp_get_params": (C.c_int, [vp, P_f]),
         "dg_mlp_set_params": (C.c_int, [vp, P_f]),
         "dg_mlp_forward": (C.c_int, [vp, P_f, C.c_int, P_f]),
+        "dg_mlp_forward_bf16": (C.c_int, [vp, P_f, C.c_int, P_f]),
+        "dg_learned_set_inference": (C.c_int, [vp, C.c_int]),
         "dg_mlp_loss_grad": (C.c_int, [vp, P_f, P_f, C.c_int, P_d, P_f]),
         "dg_mlp_train_step": (C.c_int, [vp, P_f, P_f, C.c_int, C.c_double, P_d]),
         "dg_learned_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(PhysDesc), C.c_int, C.c_int, C.c_int,
@@ -756,10 +758,13 @@ class MLP:
         p = np.ascontiguousarray(p, dtype=np.float32)
         _check(lib().dg_mlp_set_params(self._h, _fptr(p)))
 
-    def forward(self, X: np.ndarray) -> np.ndarray:
+    def forward(self, X: np.ndarray, bf16: bool = False) -> np.ndarray:
+        """Inference; bf16=True runs it on the tensor cores (BF16 inputs,
+        weights and hidden activations, FP32 accumulation)."""
         X = np.ascontiguousarray(X, dtype=np.float32)
-        Y = np.zeros((X.shape[0], self.nout), dtype=np.float32)
-        _check(lib().dg_mlp_forward(self._h, _fptr(X), X.shape[0], _fptr(Y)))
+        Y = np.empty((X.shape[0], self.nout), dtype=np.float32)
+        fn = lib().dg_mlp_forward_bf16 if bf16 else lib().dg_mlp_forward
+        _check(fn(self._h, _fptr(X), X.shape[0], _fptr(Y)))
         return Y
 
     def loss_grad(self, X: np.ndarray, T: np.ndarray) -> tuple[float, np.ndarray]:
@@ -815,6 +820,10 @@ class Learned:
         loss = C.c_double()
         _check(lib().dg_learned_train(self._h, epochs, batch, lr, seed, C.byref(loss)))
         return loss.value
+
+    def set_inference(self, mode: str) -> None:
+        """Coarse steps infer in "fp32" (default) or "bf16" (tensor cores)."""
+        _check(lib().dg_learned_set_inference(self._h, {"fp32": 0, "bf16": 1}[mode]))
 
     def step_stats(self) -> dict:
         n, am, amin = C.c_longlong(), C.c_double(), C.c_double()

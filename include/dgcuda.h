@@ -292,6 +292,11 @@ int dg_mlp_get_params(dg_mlp *net, float *params);
 int dg_mlp_set_params(dg_mlp *net, const float *params);
 /* X [rows][nin] -> Y [rows][nout] (host arrays). */
 int dg_mlp_forward(dg_mlp *net, const float *X, int rows, float *Y);
+/* The same inference on the tcgen05 tensor cores: inputs, weights and hidden
+ * activations rounded to BF16 (weights refreshed whenever the FP32 master
+ * weights change), FP32 accumulation, bias and GELU in FP32; layers of at
+ * most 256 outputs (DG_ERR_UNSUPPORTED otherwise). */
+int dg_mlp_forward_bf16(dg_mlp *net, const float *X, int rows, float *Y);
 /* Mean squared error over rows x nout against T and its gradient (packed
  * like the parameters; grad may be NULL). */
 int dg_mlp_loss_grad(dg_mlp *net, const float *X, const float *T, int rows, double *loss, float *grad);
@@ -315,6 +320,8 @@ int dg_learned_train(dg_learned *learned, int epochs, int batch, double lr, unsi
 /* Each coarse application adds alpha x the predicted increment, alpha <= 1
  * the largest factor that does not raise the discrete energy (lumped mass);
  * the number of applications so far and their mean and least alpha. */
+/* Coarse steps infer with BF16 tensor cores (1) or FP32 (0, the default). */
+int dg_learned_set_inference(dg_learned *learned, int bf16);
 int dg_learned_step_stats(dg_learned *learned, long long *applications, double *alpha_mean, double *alpha_min);
 /* napps coarse applications on a host state, in place. */
 int dg_learned_apply(dg_learned *learned, double *const u[4], int napps);

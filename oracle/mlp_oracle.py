@@ -72,3 +72,24 @@ def loss_grad(p, X, T, nin, width, nout, hidden):
             dz = (dz @ W) * gelu_grad(zs[l - 1])
     g = np.concatenate([np.concatenate([gw.ravel(), gb]) for gw, gb in grads])
     return loss, g
+
+
+def bf16(x):
+    """Round to BF16 (round to nearest, ties to even) and back to float64."""
+    b = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    b = ((b + 0x7FFF + ((b >> 16) & 1)) >> 16) << 16
+    return b.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def forward_bf16(p, X, nin, width, nout, hidden):
+    """What the tensor-core inference computes: inputs, weights and hidden
+    activations rounded to BF16, products and sums exact here (FP32
+    accumulation on the device), biases and GELU unrounded."""
+    layers = unpack(np.asarray(p, np.float64), nin, width, nout, hidden)
+    a = bf16(np.asarray(X, np.float32))
+    for l, (W, b) in enumerate(layers):
+        z = a @ bf16(W.astype(np.float32)).T + b.astype(np.float32)
+        if l + 1 < len(layers):
+            a = bf16(gelu(z).astype(np.float32))
+        else:
+            return z

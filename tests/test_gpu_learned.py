@@ -39,6 +39,31 @@ def test_mlp_forward_loss_and_gradients_match_oracle(nin, width, nout, hidden, r
     net.close()
 
 
+@pytest.mark.parametrize("nin,width,nout,hidden,rows", [(40, 64, 12, 3, 300), (37, 70, 13, 2, 1000),
+                                                         (261, 256, 80, 3, 517), (8, 16, 3, 1, 128)])
+def test_mlp_bf16_tensor_core_inference(nin, width, nout, hidden, rows):
+    """tcgen05 BF16 inference against its NumPy emulation (BF16 inputs,
+    weights and hidden activations; a hidden value rounding the other way at
+    a BF16 tie bound is the only difference) and against FP32 inference."""
+    rng = np.random.default_rng(nin + rows)
+    net = D.MLP(nin, width, nout, hidden, seed=5)
+    p = (rng.standard_normal(net.params().size) * 0.2).astype(np.float32)
+    net.set_params(p)
+    X = rng.standard_normal((rows, nin)).astype(np.float32)
+    Y = net.forward(X, bf16=True)
+    Ye = M.forward_bf16(p, X, nin, width, nout, hidden)
+    Yf = net.forward(X)
+    assert rel(Y, Ye) <= 2e-3, rel(Y, Ye)
+    assert rel(Y, Yf) <= 3e-2, rel(Y, Yf)
+    # new weights reach the BF16 copy
+    net.set_params(p * 0.5)
+    Y2 = net.forward(X, bf16=True)
+    assert rel(Y2, M.forward_bf16(p * 0.5, X, nin, width, nout, hidden)) <= 2e-3
+    # deterministic
+    assert np.array_equal(net.forward(X, bf16=True), Y2)
+    net.close()
+
+
 def test_mlp_training_reduces_the_loss():
     rng = np.random.default_rng(0)
     X = rng.uniform(-1, 1, (2048, 6)).astype(np.float32)
@@ -108,6 +133,32 @@ def test_learned_coarse_propagator_beats_the_identity():
     assert it <= nslices
     # and after as many iterations as slices it is the serial DG to rounding
     # (needs a bit-reproducible coarse step: G(U) - G(U) cancels exactly)
+    out, it, _ = D.parareal(pre, C0, RHO0, u0, nslices, steps, dt, tol=0.0, max_iter=nslices, learned=L)
+    assert it == nslices
+    for q in range(4):
+        assert rel(out[q], ref[q]) <= 1e-11
+
+
+def test_bf16_inference_in_the_coarse_propagator():
+    """The coarse propagator with tensor-core BF16 inference: close to its
+    FP32 inference, bit-reproducible, and parareal with it still reaches the
+    serial DG after N iterations."""
+    mesh, pre = room(4, 3, 3)
+    dt = D.cfl_dt(pre, C0)
+    L = D.Learned(pre, C0, RHO0, width=128, hidden_layers=3, coarse_steps=1, dt=dt, seed=2)
+    u0 = pre.initial_state([(0, 0.5, 0.5, 0.4, 0.02, 1.0)])
+    L.collect(u0, nsnap=20)
+    L.train(epochs=5, batch=512)
+    a32 = L.apply(u0, 4)
+    L.set_inference("bf16")
+    a16 = L.apply(u0, 4)
+    assert np.array_equal(a16, L.apply(u0, 4))
+    assert rel(a16[0], a32[0]) <= 2e-2
+    nslices, steps = 4, 5
+    s = D.Solver(pre, C0, RHO0, flux="upwind")
+    s.set_state(u0)
+    s.rk4_steps(0.0, dt, nslices * steps)
+    ref = s.get_state()
     out, it, _ = D.parareal(pre, C0, RHO0, u0, nslices, steps, dt, tol=0.0, max_iter=nslices, learned=L)
     assert it == nslices
     for q in range(4):

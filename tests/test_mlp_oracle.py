@@ -31,3 +31,10 @@ def test_gelu_derivative():
     h = 1e-6
     fd = (M.gelu(x + h) - M.gelu(x - h)) / (2 * h)
     assert np.allclose(M.gelu_grad(x), fd, atol=1e-8)
+
+
+def test_bf16_rounding_known_answers():
+    """Round to nearest, ties to even, on 8 significant bits."""
+    x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -9, 1.0 + 2 ** -7 + 2 ** -8, -np.pi, 0.0, 65504.0], np.float32)
+    want = [1.0, 1.0, 1.0 + 2 ** -7, 1.0 + 2 ** -6, -3.140625, 0.0, 65536.0]
+    assert np.array_equal(M.bf16(x), np.array(want))
