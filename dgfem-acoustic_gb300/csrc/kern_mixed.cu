@@ -66,18 +66,18 @@ struct MixedWarpGroups {
     static constexpr int value = MIXED_WG;
 };
 
-template <int DIM, int P>
-bool fill(MixedKernelSet *ks) {
+template <int DIM, int P, bool MASKED>
+bool fill_variant(MixedKernelSet *ks) {
     using MS = MixedShape<DIM, P>;
     if constexpr (!MS::FITS) {
         return false;
     } else {
         constexpr int W = MixedWarpGroups<DIM, P>::value;
-        ks->stage[0] = (const void *)&mixed_stage_kernel<DIM, P, 1, W>;
-        ks->stage[1] = (const void *)&mixed_stage_kernel<DIM, P, 2, W>;
-        ks->stage[2] = (const void *)&mixed_stage_kernel<DIM, P, 3, W>;
-        ks->stage[3] = (const void *)&mixed_stage_kernel<DIM, P, 4, W>;
-        ks->euler = (const void *)&mixed_stage_kernel<DIM, P, kStageEuler, W>;
+        ks->stage[0] = (const void *)&mixed_stage_kernel<DIM, P, 1, W, MASKED>;
+        ks->stage[1] = (const void *)&mixed_stage_kernel<DIM, P, 2, W, MASKED>;
+        ks->stage[2] = (const void *)&mixed_stage_kernel<DIM, P, 3, W, MASKED>;
+        ks->stage[3] = (const void *)&mixed_stage_kernel<DIM, P, 4, W, MASKED>;
+        ks->euler = (const void *)&mixed_stage_kernel<DIM, P, kStageEuler, W, MASKED>;
         ks->elems_per_tile = MS::ELEMS;
         ks->threads = 128 * W;
         ks->smem = MS::SMEM_LAUNCH;
@@ -87,23 +87,30 @@ bool fill(MixedKernelSet *ks) {
     }
 }
 
+// Meshes with curved elements take the masked kernels (element-block list and
+// per-block masks); the others the plain ones.
+template <int DIM, int P>
+bool fill(MixedKernelSet *ks, bool masked) {
+    return masked ? fill_variant<DIM, P, true>(ks) : fill_variant<DIM, P, false>(ks);
+}
+
 }  // namespace
 
-bool get_mixed_kernels(int dim, int order, MixedKernelSet *ks) {
+bool get_mixed_kernels(int dim, int order, bool masked, MixedKernelSet *ks) {
     if (dim == 2) {
         switch (order) {
-            case 1: return fill<2, 1>(ks);
-            case 2: return fill<2, 2>(ks);
-            case 3: return fill<2, 3>(ks);
-            case 4: return fill<2, 4>(ks);
-            case 5: return fill<2, 5>(ks);
+            case 1: return fill<2, 1>(ks, masked);
+            case 2: return fill<2, 2>(ks, masked);
+            case 3: return fill<2, 3>(ks, masked);
+            case 4: return fill<2, 4>(ks, masked);
+            case 5: return fill<2, 5>(ks, masked);
         }
     } else if (dim == 3) {
         switch (order) {
-            case 1: return fill<3, 1>(ks);
-            case 2: return fill<3, 2>(ks);
-            case 3: return fill<3, 3>(ks);
-            case 4: return fill<3, 4>(ks);
+            case 1: return fill<3, 1>(ks, masked);
+            case 2: return fill<3, 2>(ks, masked);
+            case 3: return fill<3, 3>(ks, masked);
+            case 4: return fill<3, 4>(ks, masked);
         }
     }
     return false;

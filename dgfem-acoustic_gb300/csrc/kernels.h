@@ -47,7 +47,9 @@ struct MixedKernelSet {
     void (*b_image)(const double *ops, std::vector<uint8_t> &img, std::vector<int> &eb) = nullptr;
 };
 
-bool get_mixed_kernels(int dim, int order, MixedKernelSet *out);
+// masked: the variant for meshes with curved elements (MixedArgs::blist and
+// cmask in use).
+bool get_mixed_kernels(int dim, int order, bool masked, MixedKernelSet *out);
 
 // Arguments of the mixed-precision stage kernels.
 struct MixedArgs {

@@ -334,7 +334,7 @@ __device__ __forceinline__ void build_rows(const MixedArgs &a, unsigned char *sm
     }
 }
 
-template <int DIM, int P, int STAGE, int NWG>
+template <int DIM, int P, int STAGE, int NWG, bool MASKED>
 __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedArgs a) {
     using MS = MixedShape<DIM, P>;
     constexpr int NP = MS::NP, NQ = MS::NQ;
@@ -405,15 +405,16 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     // is reused from L2).
     // (tile counts stay below 2^31, checked on the host: 32-bit division,
     // none at all for a single member)
-    // meshes with curved elements: only the element blocks in a.blist (those
-    // with at least one straight element)
-    const long long nblocks = a.blist ? (long long)a.nblk : (long long)((a.K + ELEMS - 1) / ELEMS);
+    // MASKED (meshes with curved elements): only the element blocks in
+    // a.blist (those with at least one straight element), curved elements
+    // left alone
+    const long long nblocks = MASKED ? (long long)a.nblk : (long long)((a.K + ELEMS - 1) / ELEMS);
     const long long ntiles = nblocks * a.nbatch;
     const unsigned nbu = (unsigned)a.nbatch;
     auto tile_base = [&](long long T, long long &eb, long long &mo) {
         const unsigned t32 = (unsigned)T;
         const unsigned et = nbu == 1u ? t32 : t32 / nbu;
-        const unsigned blk = a.blist ? (unsigned)__ldg(&a.blist[et]) : et;
+        const unsigned blk = MASKED ? (unsigned)__ldg(&a.blist[et]) : et;
         eb = (long long)blk * ELEMS;
         mo = (long long)(t32 - et * nbu) * a.bstride;
     };
@@ -651,7 +652,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
                 }
             }
             __syncthreads();
-            const unsigned long long cm = a.cmask ? a.cmask[ebase / ELEMS] : 0ull;
+            const unsigned long long cm = MASKED ? a.cmask[ebase / ELEMS] : 0ull;
             if (vec && ebase + ELEMS <= a.K && cm == 0ull) {
                 constexpr int W = ELEMS * NP / 4;
                 for (int idx = tid; idx < NQ * W; idx += NT) {

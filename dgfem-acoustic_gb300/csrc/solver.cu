@@ -411,7 +411,7 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
         free_ctx(c);
         return fail(DG_ERR_UNSUPPORTED, "no kernel compiled for this order");
     }
-    if (c->mixed && !dgk::get_mixed_kernels(dim, m->order, &c->mks)) {
+    if (c->mixed && !dgk::get_mixed_kernels(dim, m->order, lay.curved.C > 0, &c->mks)) {
         free_ctx(c);
         return fail(DG_ERR_UNSUPPORTED, "the mixed form supports orders 1-4 in 3D and 1-5 in 2D");
     }
