@@ -724,15 +724,20 @@ def main():
     ap.add_argument("--curved-cpu-cells", type=int, default=6)
     ap.add_argument("--curved-only", action="store_true",
                     help="run the curved-element section alone (profiling case) and print it as one JSON line")
+    ap.add_argument("--parareal-only", action="store_true",
+                    help="run the learned parareal section alone (profiling case) and print it as one JSON line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least three untimed warm-up steps
     world, rank, local, pg = dist_init()
-    if args.curved_only:
+    if args.curved_only or args.parareal_only:
         import dgcuda as D
 
         ensure_built()
         if rank == 0:
-            print(json.dumps({"curved": curved_section(D, args, local)}), flush=True)
+            if args.curved_only:
+                print(json.dumps({"curved": curved_section(D, args, local)}), flush=True)
+            else:
+                print(json.dumps({"learned_parareal": parareal_section(D, args, local)}), flush=True)
     elif args.impl == "reference":
         reference_arm(args, world, rank, pg)
     else:

@@ -214,17 +214,24 @@ struct FeatArgs {
     float inv_geo;
 };
 
+// One warp per element (four per block): its DOFs, the neighbours' traces at
+// its face nodes, wall kinds and inverse Jacobian, the DOF/trace part
+// divided by its largest magnitude (written to escale).
 __global__ void __launch_bounds__(128) features_kernel(FeatArgs a, float *X, float *escale) {
-    const int e = blockIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int e = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (e >= a.K) return;
     float *x = X + (size_t)e * a.nin;
     const uint8_t *fmask = a.tabs, *perm = a.tabs + a.nf * a.nfp;
     const int own = a.nq * a.np, tr = a.nf * a.nfp * a.nq;
-    for (int t = threadIdx.x; t < own; t += blockDim.x) {
+    float m = 0.0f;
+    for (int t = lane; t < own; t += 32) {
         const int f = t / a.np, i = t - f * a.np;
-        x[t] = (float)a.u[f * a.ndof + (long long)e * a.np + i] * a.inv_scale[f];
+        const float v = (float)a.u[f * a.ndof + (long long)e * a.np + i] * a.inv_scale[f];
+        x[t] = v;
+        m = fmaxf(m, fabsf(v));
     }
-    for (int t = threadIdx.x; t < tr; t += blockDim.x) {
+    for (int t = lane; t < tr; t += 32) {
         const int lf = t / (a.nfp * a.nq), rem = t - lf * a.nfp * a.nq;
         const int k = rem / a.nq, f = rem - k * a.nq;
         const int2 cn = a.conn[(long long)e * a.nf + lf];
@@ -235,28 +242,20 @@ __global__ void __launch_bounds__(128) features_kernel(FeatArgs a, float *X, flo
             v = (float)a.u[f * a.ndof + (long long)cn.x * a.np + nvi] * a.inv_scale[f];
         }
         x[own + t] = v;
+        m = fmaxf(m, fabsf(v));
     }
-    for (int lf = threadIdx.x; lf < a.nf; lf += blockDim.x) {
+    for (int lf = lane; lf < a.nf; lf += 32) {
         const int kind = (a.conn[(long long)e * a.nf + lf].y >> 5) & 3;
         x[own + tr + 2 * lf] = kind == 1 ? 1.0f : 0.0f;
         x[own + tr + 2 * lf + 1] = kind == 2 ? 1.0f : 0.0f;
     }
-    for (int g = threadIdx.x; g < a.dim * a.dim; g += blockDim.x)
+    for (int g = lane; g < a.dim * a.dim; g += 32)
         x[own + tr + 2 * a.nf + g] = (float)a.geo[(long long)e * a.dim * a.dim + g] * a.inv_geo;
-    __syncthreads();
-    __shared__ float red[128];
-    float m = 0.0f;
-    for (int t = threadIdx.x; t < own + tr; t += blockDim.x) m = fmaxf(m, fabsf(x[t]));
-    red[threadIdx.x] = m;
-    __syncthreads();
-    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
-        if (threadIdx.x < k) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + k]);
-        __syncthreads();
-    }
-    const float sc = red[0];
-    const float inv = sc > 0.0f ? 1.0f / sc : 0.0f;
-    for (int t = threadIdx.x; t < own + tr; t += blockDim.x) x[t] *= inv;
-    if (threadIdx.x == 0) escale[e] = sc;
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    const float inv = m > 0.0f ? 1.0f / m : 0.0f;
+    __syncwarp();
+    for (int t = lane; t < own + tr; t += 32) x[t] *= inv;
+    if (lane == 0) escale[e] = m;
 }
 
 // u[f*ndof + e*np + i] = alpha * (u + out_scale[f] * escale[e] * Y[e][f*np + i])
@@ -302,23 +301,30 @@ __global__ void energy_products_kernel(const double *u, long long ndof, int K, i
         dd += w * d * d;
         uu += w * uv * uv;
     }
-    __shared__ double r0[256], r1[256], r2[256];
-    r0[threadIdx.x] = ud;
-    r1[threadIdx.x] = dd;
-    r2[threadIdx.x] = uu;
-    __syncthreads();
-    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
-        if (threadIdx.x < k) {
-            r0[threadIdx.x] += r0[threadIdx.x + k];
-            r1[threadIdx.x] += r1[threadIdx.x + k];
-            r2[threadIdx.x] += r2[threadIdx.x + k];
-        }
-        __syncthreads();
+    // fixed-order reduction: warp shuffles, then the block's warps in order
+    for (int o = 16; o > 0; o >>= 1) {
+        ud += __shfl_down_sync(0xffffffffu, ud, o);
+        dd += __shfl_down_sync(0xffffffffu, dd, o);
+        uu += __shfl_down_sync(0xffffffffu, uu, o);
     }
+    __shared__ double wsum[3][8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        wsum[0][warp] = ud;
+        wsum[1][warp] = dd;
+        wsum[2][warp] = uu;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
-        part[3 * blockIdx.x] = r0[0];
-        part[3 * blockIdx.x + 1] = r1[0];
-        part[3 * blockIdx.x + 2] = r2[0];
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            a0 += wsum[0][k];
+            a1 += wsum[1][k];
+            a2 += wsum[2][k];
+        }
+        part[3 * blockIdx.x] = a0;
+        part[3 * blockIdx.x + 1] = a1;
+        part[3 * blockIdx.x + 2] = a2;
     }
 }
 
@@ -400,6 +406,8 @@ __global__ void diff_norm_kernel(const double *a, const double *b, long long n, 
 }
 
 int grid_for(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4096)); }
+// energy products: a fixed grid (fixed reduction order, bit-reproducible)
+const int kEnergyBlocks = 512;
 
 }  // namespace
 
@@ -811,7 +819,7 @@ int coarse_apply(dg_learned *L, double *u) {
     dg_ctx *c = L->fine;
     dg_mlp *n = L->net;
     cudaStream_t s = n->stream;
-    features_kernel<<<c->K, 128, 0, s>>>(feat_args(L, u), L->d_feat, L->d_escale);
+    features_kernel<<<(c->K + 3) / 4, 128, 0, s>>>(feat_args(L, u), L->d_feat, L->d_escale);
     CK(cudaGetLastError());
     int rc = L->bf16 ? mlp_forward_bf16(n, L->d_feat, c->K) : mlp_forward(n, L->d_feat, c->K);
     if (rc != DG_OK) return rc;
@@ -820,7 +828,7 @@ int coarse_apply(dg_learned *L, double *u) {
     const long long nv = (long long)c->K * c->np * c->nq;
     double os[4];
     for (int f = 0; f < 4; ++f) os[f] = (double)L->out_scale[f] * L->tscale[f];
-    const int nb = grid_for(nv);
+    const int nb = kEnergyBlocks;
     energy_products_kernel<<<nb, 256, 0, s>>>(u, c->ndof, c->K, c->np, c->nq, n->d_Y, L->d_escale, os[0], os[1],
                                               os[2], os[3], L->d_detj, 1.0 / (c->rho0 * c->c0 * c->c0), c->rho0,
                                               L->d_parts);
@@ -977,7 +985,7 @@ int dg_learned_collect(dg_learned *L, const double *const u0[4], int nsnap, int 
         rc = dg_rk4_steps(c, &t, L->dt, L->coarse_steps);
         if (rc != DG_OK) return rc;
         CK(cudaMemcpy(L->d_u1, c->d_u, sb, cudaMemcpyDeviceToDevice));
-        features_kernel<<<c->K, 128>>>(feat_args(L, L->d_u0), L->d_feat, L->d_escale);
+        features_kernel<<<(c->K + 3) / 4, 128>>>(feat_args(L, L->d_u0), L->d_feat, L->d_escale);
         CK(cudaGetLastError());
         // activity: the elements' input scales
         CK(cudaMemcpy(act.data(), L->d_escale, (size_t)c->K * 4, cudaMemcpyDeviceToHost));
