@@ -18,6 +18,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "mlp_common.cuh"
 #include "tc_ptx.cuh"
@@ -30,6 +31,7 @@ constexpr int kRows = 128;   // rows per CTA (the MMA's M)
 constexpr int kChunk = 64;   // K per chunk (four MMAs of K = 16)
 constexpr int kStepA = kRows * 32;  // bytes of one K = 16 step of the X tile
 constexpr int kMaxCols = 128;       // output columns per CTA
+constexpr int kMaxDevices = 64;
 
 // Byte offset of the 16-byte unit (row r, K unit u of 8 values) inside a
 // chunk tile of R rows: K step u/2, then 8-row group, K half, row in group.
@@ -190,12 +192,15 @@ int tc_linear(cudaStream_t s, int M, int N, int np, int kp, const void *X, const
     while ((int)tcols < npc) tcols <<= 1;
     const size_t bufBytes = (size_t)kStepA * 4 + (size_t)npc * 32 * 4;
     const size_t smem = 2 * bufBytes + 32;
-    static bool attr_set = false;
-    if (!attr_set) {
+    // the shared-memory limit is a per-device attribute of the kernel
+    static std::atomic<bool> attr_set[kMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return -2;
+    if (!attr_set[dev].load()) {
         if (cudaFuncSetAttribute(tc_linear_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(2 * ((size_t)kStepA * 4 + (size_t)kMaxCols * 32 * 4) + 32)) != cudaSuccess)
             return -2;
-        attr_set = true;
+        attr_set[dev].store(true);
     }
     const dim3 grid((M + kRows - 1) / kRows, (np + kMaxCols - 1) / kMaxCols);
     tc_linear_kernel<<<grid, 128, smem, s>>>(M, N, np, kp, static_cast<const __nv_bfloat16 *>(X),
