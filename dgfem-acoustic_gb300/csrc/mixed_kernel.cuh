@@ -334,6 +334,26 @@ __device__ __forceinline__ void build_rows(const MixedArgs &a, unsigned char *sm
     }
 }
 
+// Largest magnitude of each A row over the K-steps of each warp group's
+// slicing range: sMax[g*128 + r] for part g of row r (items (g, r) spread over
+// the threads first, first + stride, ...).
+template <int DIM, int P, int NWG>
+__device__ __forceinline__ void row_maxima(unsigned char *smem, int first, int stride) {
+    using MS = MixedShape<DIM, P>;
+    constexpr int KSTEPS = MS::KSTEPS, KTOT = MS::KTOT, KSTR = MS::KSTR;
+    constexpr int KSP = (KSTEPS + NWG - 1) / NWG;
+    const float *sA = reinterpret_cast<const float *>(smem + MS::OFF_A);
+    float *sMax = reinterpret_cast<float *>(smem + MS::OFF_MAX);
+    for (int w = first; w < NWG * 128; w += stride) {
+        const int g = w >> 7, r = w & 127;
+        const int k0 = g * KSP * 16, k1 = min((g + 1) * KSP * 16, KTOT);
+        const float *arow = &sA[r * KSTR];
+        float m = 0.0f;
+        for (int k = k0; k < k1; ++k) m = fmaxf(m, fabsf(arow[k]));
+        sMax[w] = m;
+    }
+}
+
 template <int DIM, int P, int STAGE, int NWG, bool MASKED>
 __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedArgs a) {
     using MS = MixedShape<DIM, P>;
@@ -441,6 +461,9 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             dgtc::cp_async_commit();
             build_rows<DIM, P>(a, smem, eb, 0, tid, NT);
             __syncthreads();
+            // the row maxima of every later tile are taken right after its
+            // rows, while the previous tile's MMAs run
+            row_maxima<DIM, P, NWG>(smem, tid, NT);
         }
     }
     int cb = 0;  // connectivity buffer of the current tile
@@ -489,7 +512,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             }
         }
         const float *arow = &sA[r * KSTR];
-        {
+        if constexpr (!OVERLAP) {
             float m = 0.0f;
             if (row_ok)
                 for (int k = ks0 * 16; k < ks1 * 16 && k < KTOT; ++k) m = fmaxf(m, fabsf(arow[k]));
@@ -575,6 +598,8 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
                     issue_conn_copies<DIM, P>(a, smem, e2, cb, tid - 32, NT - 32);
                 }
                 build_rows<DIM, P>(a, smem, nebase, cb ^ 1, tid - 32, NT - 32);
+                asm volatile("bar.sync 1, %0;" ::"r"(NT - 32) : "memory");
+                row_maxima<DIM, P, NWG>(smem, tid - 32, NT - 32);
             }
             dgtc::cp_async_commit();
         }
