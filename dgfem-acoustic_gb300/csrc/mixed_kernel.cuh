@@ -52,15 +52,23 @@ struct MixedShape {
     static constexpr int KSTEPS = KPAD / 16;
     static constexpr int NPAD = (NP + 15) / 16 * 16;
     static constexpr int ELEMS = 128 / NQ;          // elements per tile
-    static constexpr int ACOLS = KPAD / 2;          // tensor-memory columns per A slice
-    static constexpr int ACC = 4 * ACOLS;           // first accumulator column
     static constexpr int TMEM_COLS = 512;
-    static constexpr bool FITS = ACC + 3 * NPAD <= TMEM_COLS;
     // Level scheme (where it fits): one accumulator per level L = i+j of the
     // slice pairs (0..3).  The B slices of a K-step lie side by side along N,
     // so A slice i meets B slices 0..3-i in one MMA of N = (4-i) x NPAD,
-    // accumulating into levels i..3: four MMAs per K-step.
-    static constexpr bool LEVELS = ACC + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256;
+    // accumulating into levels i..3: four MMAs per K-step.  Where the four A
+    // slices of all K-steps and the four levels do not fit in tensor memory
+    // together (3D order 4), the K-steps go in two passes that reuse the A
+    // columns (the second pass is sliced once the first pass's MMAs are done).
+    static constexpr bool LEVELS_ONE = 4 * (KPAD / 2) + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256;
+    static constexpr int KPASS_TWO = (KSTEPS + 1) / 2;
+    static constexpr bool LEVELS_TWO = !LEVELS_ONE && 4 * KPASS_TWO * 8 + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256;
+    static constexpr int NPASS = LEVELS_TWO ? 2 : 1;
+    static constexpr int KPASS = NPASS == 2 ? KPASS_TWO : KSTEPS;  // K-steps per pass
+    static constexpr bool LEVELS = LEVELS_ONE || LEVELS_TWO;
+    static constexpr int ACOLS = KPASS * 8;         // tensor-memory columns per A slice (one pass)
+    static constexpr int ACC = 4 * ACOLS;           // first accumulator column
+    static constexpr bool FITS = ACC + 3 * NPAD <= TMEM_COLS;
     // Pair scheme (otherwise): one MMA per slice pair; accumulator 0 for
     // i+j = 0, 1 for i+j = 1 (both exact), NX more for the seven pairs with
     // i+j = 2, 3 (spread so that the MMAs of consecutive pairs do not wait on
@@ -531,58 +539,75 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
         // below the FP32 resolution of any non-negligible row)
         const bool live = row_ok && ea > -110;
         const float sc = live ? exp2i(8 - ea) : 0.0f;
+        // K-steps of each pass (one pass unless tensor memory is short); the
+        // pass's K-steps are spread over the warp groups for the slicing
+        constexpr int NPASS = MS::NPASS, KPASS = MS::KPASS;
+        constexpr int KSPP = (KPASS + NWG - 1) / NWG;
 #pragma unroll 1
-        for (int c = ks0; c < ks1; ++c) {
-            uint32_t w[4][8];
-#pragma unroll
-            for (int h = 0; h < 8; ++h) {
-                const int k = c * 16 + 2 * h;
-                const float x0 = (live && k < KTOT) ? arow[k] : 0.0f;
-                const float x1 = (live && k + 1 < KTOT) ? arow[k + 1] : 0.0f;
-                float m0[4], m1[4];
-                slice4(x0, sc, m0);
-                slice4(x1, sc, m1);
-#pragma unroll
-                for (int sl = 0; sl < 4; ++sl) w[sl][h] = bf16x2_bits(m0[sl], m1[sl]);
+        for (int pass = 0; pass < NPASS; ++pass) {
+            const int kb = pass * KPASS, ke = kb + KPASS < KSTEPS ? kb + KPASS : KSTEPS;
+            const int c0 = NPASS == 1 ? ks0 : (kb + part * KSPP < ke ? kb + part * KSPP : ke);
+            const int c1 = NPASS == 1 ? ks1 : (c0 + KSPP < ke ? c0 + KSPP : ke);
+            if (pass > 0) {
+                // the previous pass's MMAs read the A columns about to be rewritten
+                if (!dgtc::mbar_wait_bounded(bar, phase, 1u << 30)) *sFail = 1;
+                phase ^= 1u;
+                dgtc::fence_after_sync();
             }
-            __syncwarp();
-#pragma unroll
-            for (int sl = 0; sl < 4; ++sl)
-                dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, sl * ACOLS + c * 8), w[sl]);
-        }
-        dgtc::tmem_st_wait();
-        dgtc::fence_before_sync();
-        __syncthreads();
-
-        // 4. tensor-core contraction, issued by thread 0 K-step by K-step
-        if (tid == 0) {
-            dgtc::fence_after_sync();
-            if constexpr (MS::LEVELS) {
-                // A slice 0 at K-step 0 starts all four levels
 #pragma unroll 1
-                for (int t = 0; t < KSTEPS; ++t) {
-                    const uint64_t bd = dgtc::desc_kmajor(sB + t * 4 * MS::BTILE, 128, 256);
+            for (int c = c0; c < c1; ++c) {
+                uint32_t w[4][8];
 #pragma unroll
-                    for (int ia = 0; ia < 4; ++ia)
-                        dgtc::mma_bf16_ts(tbase + MS::ACC + ia * NPAD, tbase + ia * ACOLS + t * 8, bd,
-                                          dgtc::idesc_bf16_f32(128, (4 - ia) * NPAD), (t > 0 || ia > 0) ? 1u : 0u);
+                for (int h = 0; h < 8; ++h) {
+                    const int k = c * 16 + 2 * h;
+                    const float x0 = (live && k < KTOT) ? arow[k] : 0.0f;
+                    const float x1 = (live && k + 1 < KTOT) ? arow[k + 1] : 0.0f;
+                    float m0[4], m1[4];
+                    slice4(x0, sc, m0);
+                    slice4(x1, sc, m1);
+#pragma unroll
+                    for (int sl = 0; sl < 4; ++sl) w[sl][h] = bf16x2_bits(m0[sl], m1[sl]);
                 }
-            } else {
-                unsigned started = 0;  // bit per accumulator
-#pragma unroll 1
-                for (int t = 0; t < KSTEPS; ++t) {
+                __syncwarp();
 #pragma unroll
-                    for (int pi = 0; pi < 10; ++pi) {
-                        const int ia = kPairA[pi], jb = kPairB[pi];
-                        const int slot = pi == 0 ? 0 : pi < 3 ? 1 : 2 + (pi - 3) % NX;
-                        const uint64_t bd = dgtc::desc_kmajor(sB + (t * 4 + jb) * MS::BTILE, 128, 256);
-                        dgtc::mma_bf16_ts(tbase + MS::ACC + slot * NPAD, tbase + ia * ACOLS + t * 8, bd, idesc,
-                                          (started >> slot) & 1u);
-                        started |= 1u << slot;
+                for (int sl = 0; sl < 4; ++sl)
+                    dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, sl * ACOLS + (c - kb) * 8), w[sl]);
+            }
+            dgtc::tmem_st_wait();
+            dgtc::fence_before_sync();
+            __syncthreads();
+
+            // 4. tensor-core contraction, issued by thread 0 K-step by K-step
+            if (tid == 0 && !*sFail) {
+                dgtc::fence_after_sync();
+                if constexpr (MS::LEVELS) {
+                    // A slice 0 at K-step 0 starts all four levels
+#pragma unroll 1
+                    for (int t = kb; t < ke; ++t) {
+                        const uint64_t bd = dgtc::desc_kmajor(sB + t * 4 * MS::BTILE, 128, 256);
+#pragma unroll
+                        for (int ia = 0; ia < 4; ++ia)
+                            dgtc::mma_bf16_ts(tbase + MS::ACC + ia * NPAD, tbase + ia * ACOLS + (t - kb) * 8, bd,
+                                              dgtc::idesc_bf16_f32(128, (4 - ia) * NPAD),
+                                              (t > 0 || ia > 0) ? 1u : 0u);
+                    }
+                } else {
+                    unsigned started = 0;  // bit per accumulator
+#pragma unroll 1
+                    for (int t = 0; t < KSTEPS; ++t) {
+#pragma unroll
+                        for (int pi = 0; pi < 10; ++pi) {
+                            const int ia = kPairA[pi], jb = kPairB[pi];
+                            const int slot = pi == 0 ? 0 : pi < 3 ? 1 : 2 + (pi - 3) % NX;
+                            const uint64_t bd = dgtc::desc_kmajor(sB + (t * 4 + jb) * MS::BTILE, 128, 256);
+                            dgtc::mma_bf16_ts(tbase + MS::ACC + slot * NPAD, tbase + ia * ACOLS + t * 8, bd, idesc,
+                                              (started >> slot) & 1u);
+                            started |= 1u << slot;
+                        }
                     }
                 }
+                dgtc::mma_commit(bar);
             }
-            dgtc::mma_commit(bar);
         }
         __syncwarp();
         if constexpr (OVERLAP) {
