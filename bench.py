@@ -207,8 +207,8 @@ def stage_bytes(pre, real_bytes: int, pair_state: bool = False, geo_bytes: int =
     Stage 1 reads u, writes acc and w; stages 2-3 read w, u, acc and write
     acc, w; stage 4 reads w, u, acc and writes u.  With the state kept as an
     FP32 pair (mixed form) every read of u also reads its low part and stage 4
-    writes both.  geo_bytes: size of an inverse-Jacobian entry (FP64, or FP32
-    in the mixed form)."""
+    writes both.  geo_bytes: size of an inverse-Jacobian entry (FP64 in the
+    FP64 form, FP32 in the others)."""
     nq = pre.dim + 1
     n = pre.ndof * nq
     geo = pre.num_el * (pre.dim * pre.dim * geo_bytes + pre.nf * 4 * real_bytes + pre.nf * 8)
@@ -298,7 +298,7 @@ FORMS = {
 def roofline_for(sol, pre, form, t, dt, nprof):
     _, prof = sol.profile_steps(t, dt, nprof)
     real = 8 if form == "fp64" else 4
-    sb = stage_bytes(pre, real, pair_state=(form == "mixed"), geo_bytes=4 if form == "mixed" else 8)
+    sb = stage_bytes(pre, real, pair_state=(form == "mixed"), geo_bytes=real)
     avg_ms = [prof["stage_ms"][s] / max(prof["stage_launches"][s], 1) for s in range(4)]
     achieved = sum(sb) / (sum(avg_ms) * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
@@ -726,18 +726,24 @@ def main():
                     help="run the curved-element section alone (profiling case) and print it as one JSON line")
     ap.add_argument("--parareal-only", action="store_true",
                     help="run the learned parareal section alone (profiling case) and print it as one JSON line")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="run the multi-source batch section alone (profiling case) and print it as one JSON line")
+    ap.add_argument("--uneven-only", action="store_true",
+                    help="run the uneven multi-mesh section alone (profiling case) and print it as one JSON line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least three untimed warm-up steps
     world, rank, local, pg = dist_init()
-    if args.curved_only or args.parareal_only:
+    only = [(flag, key, fn) for flag, key, fn in
+            ((args.curved_only, "curved", curved_section), (args.parareal_only, "learned_parareal", parareal_section),
+             (args.batched_only, "batched", batched_section), (args.uneven_only, "uneven_batch", uneven_section))
+            if flag]
+    if only:
         import dgcuda as D
 
         ensure_built()
         if rank == 0:
-            if args.curved_only:
-                print(json.dumps({"curved": curved_section(D, args, local)}), flush=True)
-            else:
-                print(json.dumps({"learned_parareal": parareal_section(D, args, local)}), flush=True)
+            for _, key, fn in only:
+                print(json.dumps({key: fn(D, args, local)}), flush=True)
     elif args.impl == "reference":
         reference_arm(args, world, rank, pg)
     else:

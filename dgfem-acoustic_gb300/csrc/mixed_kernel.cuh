@@ -1,4 +1,4 @@
-// Mixed-precision stage kernel: FP32 state tiles, FP64 geometry factors, and
+// Mixed-precision stage kernel: FP32 state tiles and geometry factors, and
 // the volume + lift contraction on the tensor cores with exact accumulation.
 //
 // For a tile of ELEMS elements the right-hand side of every (field, element)

@@ -299,7 +299,7 @@ int upload_mesh_args(dg_multi *c, const std::vector<double> &dt) {
             }
             a.fstride = g.ndof;
             a.bstride = 0;
-            a.geo = (const double *)g.geo;
+            a.geo = (const Real *)g.geo;
             a.fgeo = (const Real *)g.fgeo;
             a.conn = (const int2 *)g.conn;
             a.ops = (const Real *)c->d_ops[g.order];
@@ -574,8 +574,7 @@ int dg_multi_create(int nmesh, const dg_mesh_desc *meshes, const dg_phys_desc *p
             g.c0 = phys[i].c0;
             g.rho0 = phys[i].rho0;
             for (int k = 0; k < 3; ++k) g.v0[k] = phys[i].v0[k];
-            if (!fin(cudaMalloc(&g.geo, lay.geo.size() * 8), "cudaMalloc(geo)")) break;
-            if (!fin(cudaMemcpy(g.geo, lay.geo.data(), lay.geo.size() * 8, cudaMemcpyHostToDevice), "copy geo")) break;
+            if (!upload_real(lay.geo, &g.geo)) break;
             if (!upload_real(lay.fgeo, &g.fgeo)) break;
             if (!fin(cudaMalloc(&g.conn, lay.conn.size() * 4), "cudaMalloc(conn)")) break;
             if (!fin(cudaMemcpy(g.conn, lay.conn.data(), lay.conn.size() * 4, cudaMemcpyHostToDevice), "copy conn"))

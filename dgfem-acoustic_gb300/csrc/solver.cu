@@ -167,7 +167,8 @@ template <typename Real>
 void fill_args(dg_ctx *c, dgk::StageArgs<Real> &a, int stage, double dt) {
     a.fstride = c->ndof;
     a.bstride = c->bstride;
-    a.geo = c->d_geo;
+    if constexpr (sizeof(Real) == 8) a.geo = reinterpret_cast<const Real *>(c->d_geo);
+    else a.geo = reinterpret_cast<const Real *>(c->d_geo32);
     a.fgeo = reinterpret_cast<const Real *>(c->d_fgeo);
     a.conn = c->d_conn;
     a.ops = reinterpret_cast<const Real *>(c->d_ops);
@@ -431,9 +432,18 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
         c->d_wa = c->d_state + 2 * state_bytes;
         c->d_wb = c->d_state + 3 * state_bytes;
         if (!fin(cudaMemsetAsync(c->d_state, 0, 4 * state_bytes, c->stream), "cudaMemset")) break;
-        if (!fin(cudaMalloc(&c->d_geo, lay.geo.size() * 8), "cudaMalloc(geo)")) break;
-        if (!fin(cudaMemcpy(c->d_geo, lay.geo.data(), lay.geo.size() * 8, cudaMemcpyHostToDevice), "copy geo"))
-            break;
+        // inverse Jacobians in the stage precision (FP32 contexts round them
+        // once here instead of converting them in every stage)
+        if (c->prec == DG_PREC_FP64) {
+            if (!fin(cudaMalloc(&c->d_geo, lay.geo.size() * 8), "cudaMalloc(geo)")) break;
+            if (!fin(cudaMemcpy(c->d_geo, lay.geo.data(), lay.geo.size() * 8, cudaMemcpyHostToDevice), "copy geo"))
+                break;
+        } else {
+            std::vector<float> g32(lay.geo.begin(), lay.geo.end());
+            if (!fin(cudaMalloc(&c->d_geo32, std::max<size_t>(g32.size(), 1) * 4), "cudaMalloc(geo32)")) break;
+            if (!fin(cudaMemcpy(c->d_geo32, g32.data(), g32.size() * 4, cudaMemcpyHostToDevice), "copy geo32"))
+                break;
+        }
         auto upload_real = [&](const std::vector<double> &v, void **dst) -> bool {
             if (!fin(cudaMalloc(dst, v.size() * c->rsize), "cudaMalloc")) return false;
             if (c->prec == DG_PREC_FP64)
@@ -479,12 +489,6 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
         c->grid = std::max(1, std::min(ntiles, (resident + nbatch - 1) / nbatch));
         if (c->mixed) {
             if (!fin(cudaMalloc(&c->d_ulo, state_bytes), "cudaMalloc(ulo)")) break;
-            {
-                std::vector<float> g32(lay.geo.begin(), lay.geo.end());
-                if (!fin(cudaMalloc(&c->d_geo32, g32.size() * 4), "cudaMalloc(geo32)")) break;
-                if (!fin(cudaMemcpy(c->d_geo32, g32.data(), g32.size() * 4, cudaMemcpyHostToDevice), "copy geo32"))
-                    break;
-            }
             if (!fin(cudaMemsetAsync(c->d_ulo, 0, state_bytes, c->stream), "cudaMemset")) break;
             std::vector<uint8_t> img;
             std::vector<int> eb;

@@ -57,7 +57,7 @@ struct StageArgs {
     Real *wout;            // next stage input (stage 4: the new state, == u)
     long long fstride;     // elements * NP (distance between fields)
     long long bstride;     // distance between batch members (sources)
-    const double *geo;     // [K][DIM*DIM]  B[x][u] at x*DIM+u
+    const Real *geo;       // [K][DIM*DIM]  B[x][u] at x*DIM+u (rounded once to Real)
     const Real *fgeo;      // [K][NF][4]    outward normal (DIM) and detJf/detJe
     const int2 *conn;      // [K][NF]       neighbour element, connectivity word
     const Real *ops;       // NOPS reference operators
@@ -155,7 +155,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<Real> &a, long long b
         for (int x = 0; x < DIM; ++x)
 #pragma unroll
             for (int u = 0; u < DIM; ++u)
-                B[x][u] = valid ? Real(a.geo[(long long)e * DIM * DIM + x * DIM + u]) : Real(0);
+                B[x][u] = valid ? a.geo[(long long)e * DIM * DIM + x * DIM + u] : Real(0);
         Real g[NQ][DIM];
 #pragma unroll
         for (int f = 0; f < NQ; ++f)

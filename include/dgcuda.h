@@ -45,7 +45,7 @@ extern "C" {
 #define DG_ERR_CONFIG (-8)
 
 #define DG_PREC_FP64 0 /* FP64 throughout */
-#define DG_PREC_FP32 1 /* FP32 state and flux, FP64 geometry factors */
+#define DG_PREC_FP32 1 /* FP32 state, flux and geometry factors */
 #define DG_PREC_MIXED 2 /* FP32 stage data, state kept as an FP32 pair, volume + lift
                          * contraction on the tensor cores (BF16 fixed-point slices,
                          * exact FP32 accumulation); orders 1-4 in 3D, 1-5 in 2D */
