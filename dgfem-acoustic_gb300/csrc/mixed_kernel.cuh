@@ -85,22 +85,28 @@ struct MixedShape {
     static constexpr int r16(int x) { return (x + 15) / 16 * 16; }
     static constexpr int OFF_B = 0;                                   // sliced operator image
     static constexpr int OFF_Q = OFF_B + BBYTES;                      // state tile [f][le][QS]
-    static constexpr int OFF_A = r16(OFF_Q + NQ * ELEMS * QS * 4);    // FP32 A rows [128][KSTR]
-    static constexpr int OFF_NBR = r16(OFF_A + 128 * KSTR * 4);       // neighbour traces [task][4]
-    static constexpr int OFF_GEO = OFF_NBR + ELEMS * NSLOT * 16;      // [le][DIM*DIM] floats
+    static constexpr int OFF_NBR = r16(OFF_Q + NQ * ELEMS * QS * 4);  // neighbour traces [task][4]
+    static constexpr int OFF_A = r16(OFF_NBR + ELEMS * NSLOT * 16);   // FP32 A rows [128][KSTR]
+    static constexpr int OFF_GEO = OFF_A + 128 * KSTR * 4;            // [le][DIM*DIM] floats
     static constexpr int OFF_CONN = r16(OFF_GEO + ELEMS * DIM * DIM * 4);  // 2 x [le][NF] int2
     static constexpr int CONN_BYTES = r16(ELEMS * NF * 8);
     static constexpr int OFF_FGEO = OFF_CONN + 2 * CONN_BYTES;         // [le][NF] float4
     static constexpr int OFF_MAX = OFF_FGEO + ELEMS * NF * 16;
     static constexpr int OFF_TAB = OFF_MAX + MAX_WG * 128 * 4;
     static constexpr int OFF_EB = r16(OFF_TAB + S::NTAB);
-    // Overlap (where shared memory allows): the epilogue stages its outputs
-    // in their own region, so that the next tile's A rows can be built while
-    // this tile's MMAs run.
+    // Overlap: the next tile's A rows are built while this tile's MMAs run,
+    // so the epilogue stages its outputs outside the A-row region: in a
+    // region of their own where shared memory allows, else in the state-tile
+    // and neighbour-trace regions (adjacent; the next tile's rows, built
+    // from them, are complete before the epilogue starts, and its copies
+    // into them start after it).
     static constexpr int OUT_FLOATS = 2 * NQ * ELEMS * NP;
-    static constexpr int OFF_OUT = r16(OFF_EB + NPAD * 4);
-    static constexpr bool OVERLAP = OFF_OUT + OUT_FLOATS * 4 + 16 <= 227 * 1024;
-    static constexpr int OFF_BAR = OVERLAP ? r16(OFF_OUT + OUT_FLOATS * 4) : OFF_EB + NPAD * 4;
+    static constexpr int OFF_OUT_OWN = r16(OFF_EB + NPAD * 4);
+    static constexpr bool OUT_OWN = OFF_OUT_OWN + OUT_FLOATS * 4 + 16 <= 227 * 1024;
+    static constexpr bool OUT_ALIAS = !OUT_OWN && OUT_FLOATS * 4 <= OFF_A - OFF_Q;
+    static constexpr bool OVERLAP = OUT_OWN || OUT_ALIAS;
+    static constexpr int OFF_OUT = OUT_OWN ? OFF_OUT_OWN : OFF_Q;
+    static constexpr int OFF_BAR = OUT_OWN ? r16(OFF_OUT + OUT_FLOATS * 4) : OFF_EB + NPAD * 4;
     static constexpr int SMEM = OFF_BAR + 16;
     // the epilogue stages the tile's two output arrays in the A-row region
     static_assert(2 * NQ * ELEMS * NP <= 128 * KSTR, "output staging fits in the A-row region");
