@@ -111,6 +111,10 @@ struct MixedShape {
     // the epilogue stages the tile's two output arrays in the A-row region
     static_assert(2 * NQ * ELEMS * NP <= 128 * KSTR, "output staging fits in the A-row region");
     static_assert(SMEM <= 227 * 1024, "tile does not fit in shared memory");
+    static_assert(NPASS * KPASS >= KSTEPS && (NPASS == 1 || LEVELS), "the passes cover every K-step");
+    static_assert(!LEVELS || (ACC + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256), "level accumulators fit");
+    static_assert(!OUT_ALIAS || (OFF_Q + OUT_FLOATS * 4 <= OFF_A && OFF_NBR > OFF_Q && OFF_A > OFF_NBR),
+                  "aliased output staging stays inside the state-tile and neighbour-trace regions");
     // at least half of the SM's shared memory, so one CTA (the tensor-memory
     // owner) runs per SM
     static constexpr int SMEM_LAUNCH = SMEM < 118 * 1024 ? 118 * 1024 : SMEM;
