@@ -255,11 +255,12 @@ def reference_arm(args, world, rank, pg):
         return
     threads = os.cpu_count() or 1
     total = args.steps + args.warmup
-    # per-step sample sized so the whole run stays within about two minutes
+    # per-step sample sized so the whole run stays within --reference-seconds
+    # (two minutes by default)
     _, sec4, _ = oracle_sample_rate(4, 1, threads)
     n = 2
     for cand in (3, 4, 6, 8, 10, 12, 16):
-        if sec4 * (cand / 4) ** 3 * total <= 120.0:
+        if sec4 * (cand / 4) ** 3 * total <= args.reference_seconds:
             n = cand
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle_py as O
@@ -287,9 +288,9 @@ def reference_arm(args, world, rank, pg):
 # ------------------------------------------------------------------ GPU arm
 FORMS = {
     "mixed": ("FP32 stage data, state kept as an FP32 pair, volume + lift contraction on the tcgen05 tensor "
-              "cores with BF16 fixed-point slices and exact FP32 accumulation, FP64 geometry factors",
+              "cores with BF16 fixed-point slices and exact FP32 accumulation, FP32 geometry factors",
               "f32+bf16x4 (exact accumulation)", "mixed_stage_kernel<3,3> (tcgen05 kind::f16, A in TMEM)"),
-    "fp32": ("FP32 state and flux, FP64 geometry factors, fused stage kernel on CUDA cores", "f32",
+    "fp32": ("FP32 state, flux and geometry factors, fused stage kernel on CUDA cores", "f32",
              "stage_kernel<3,3,float>"),
     "fp64": ("FP64 throughout, fused stage kernel on CUDA cores", "f64", "stage_kernel<3,3,double>"),
 }
@@ -699,6 +700,8 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=2000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--reference-seconds", type=float, default=120.0,
+                    help="time budget of the --impl reference run (sizes its per-step sample)")
     ap.add_argument("--cells", type=int, default=NCELL, help="cube cells per side (profiling cases)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
