@@ -1,0 +1,109 @@
+"""dg_create rejects bad arguments and inconsistent meshes on the host,
+before any device call, with the documented error code and a message.  The
+kernels index device memory through the caller's face ids, neighbour ids and
+face node maps, so every such array is range-checked here.  (No GPU: a check
+that were missing would reach the device calls and return DG_ERR_CUDA.)"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+import dgcuda as D
+
+DG_ERR_ARG, DG_ERR_UNSUPPORTED, DG_ERR_MESH = -1, -3, -6
+
+
+class Desc:
+    """A mesh descriptor whose arrays are private copies that a test may
+    corrupt."""
+
+    def __init__(self, dim: int, order: int):
+        m = D.Mesh.box_tri(2, 2, order=order) if dim == 2 else D.Mesh.box_tet(2, 2, 2, order=order)
+        self.pre = D.Precomp(m)
+        self.d = self.pre.desc()
+        a = self.pre.arrays()
+        self.a = {k: np.ascontiguousarray(v) for k, v in a.items() if isinstance(v, np.ndarray)}
+        self._point()
+
+    def _point(self):
+        d, a = self.d, self.a
+        d.el_jacobians = a["el_jacobians"].ctypes.data_as(D.P_d)
+        d.el_jacobian_dets = a["el_jacobian_dets"].ctypes.data_as(D.P_d)
+        d.f_normals = a["f_normals"].ctypes.data_as(D.P_d)
+        d.f_jacobian_dets = a["f_jacobian_dets"].ctypes.data_as(D.P_d)
+        d.el_f_ids = a["el_f_ids"].ctypes.data_as(D.P_i)
+        d.el_f_orientation = a["el_f_orientation"].ctypes.data_as(D.P_i)
+        d.f_nbr_el_ids = a["f_nbr_el_ids"].ctypes.data_as(D.P_i)
+        d.f_n_to_el_n_ids = a["f_n_to_el_n_ids"].ctypes.data_as(D.P_i)
+        d.f_bc = a["f_bc"].ctypes.data_as(D.P_i)
+        d.f_is_boundary = a["f_is_boundary"].ctypes.data_as(D.P_u8)
+
+    def interior_face(self) -> int:
+        return int(np.flatnonzero(self.a["f_is_boundary"] == 0)[0])
+
+
+def create(d, c0=340.0, rho0=1.225, precision=0, flux=0, nbatch=1, null_mesh=False):
+    ph = D.PhysDesc()
+    ph.c0, ph.rho0 = c0, rho0
+    o = D.Opts()
+    D.lib().dg_default_opts(C.byref(o))
+    o.precision, o.flux_sign = precision, flux
+    h = C.c_void_p()
+    code = D.lib().dg_create_batch(None if null_mesh else C.byref(d), C.byref(ph), C.byref(o), nbatch, C.byref(h))
+    msg = (D.lib().dg_last_error() or b"").decode()
+    return code, msg, h
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_arguments(dim):
+    x = Desc(dim, 2)
+    assert create(x.d, null_mesh=True)[0] == DG_ERR_ARG
+    for nb in (0, 65536):
+        code, msg, h = create(x.d, nbatch=nb)
+        assert code == DG_ERR_ARG and "batch" in msg and not h.value
+    code, msg, _ = create(x.d, precision=7)
+    assert code == DG_ERR_ARG and "precision" in msg
+    code, msg, _ = create(x.d, flux=9)
+    assert code == DG_ERR_ARG and "flux" in msg
+    for c0, rho0 in ((0.0, 1.2), (340.0, -1.0), (math.nan, 1.2)):
+        code, msg, _ = create(x.d, c0=c0, rho0=rho0)
+        assert code == DG_ERR_ARG and "positive" in msg
+
+
+def test_unsupported_dimension_and_order():
+    x = Desc(3, 2)
+    x.d.dim = 4
+    assert create(x.d)[0] == DG_ERR_UNSUPPORTED
+    x.d.dim = 3
+    x.d.order = 6
+    code, msg, _ = create(x.d)
+    assert code == DG_ERR_UNSUPPORTED and "order" in msg
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_inconsistent_meshes(dim):
+    cases = []
+
+    def case(name, fn, words):
+        cases.append((name, fn, words))
+
+    case("empty", lambda x: setattr(x.d, "num_el", 0), "empty")
+    case("node count", lambda x: setattr(x.d, "el_num_nodes", x.d.el_num_nodes + 1), "node counts")
+    case("null array", lambda x: setattr(x.d, "f_normals", D.P_d()), "null")
+    case("face id high", lambda x: x.a["el_f_ids"].__setitem__((0, 0), x.d.f_num), "face id out of range")
+    case("face id negative", lambda x: x.a["el_f_ids"].__setitem__((1, 1), -1), "face id out of range")
+    case("neighbour out of range",
+         lambda x: x.a["f_nbr_el_ids"].__setitem__((x.interior_face(), 1), x.d.num_el + 5), "neighbour")
+    case("face node map", lambda x: x.a["f_n_to_el_n_ids"].__setitem__((x.interior_face(), 0, 0), 10 ** 6),
+         "face node map")
+    case("singular Jacobian", lambda x: x.a["el_jacobians"].__setitem__(0, 0.0), "Jacobian")
+    for name, fn, words in cases:
+        x = Desc(dim, 2)
+        fn(x)
+        code, msg, h = create(x.d)
+        assert code == DG_ERR_MESH, (name, code, msg)
+        assert words in msg, (name, msg)
+        assert not h.value
