@@ -574,10 +574,14 @@ int dg_multi_create(int nmesh, const dg_mesh_desc *meshes, const dg_phys_desc *p
             g.c0 = phys[i].c0;
             g.rho0 = phys[i].rho0;
             for (int k = 0; k < 3; ++k) g.v0[k] = phys[i].v0[k];
-            if (!upload_real(lay.geo, &g.geo)) break;
-            if (!upload_real(lay.fgeo, &g.fgeo)) break;
-            if (!fin(cudaMalloc(&g.conn, lay.conn.size() * 4), "cudaMalloc(conn)")) break;
-            if (!fin(cudaMemcpy(g.conn, lay.conn.data(), lay.conn.size() * 4, cudaMemcpyHostToDevice), "copy conn"))
+            // registered before its uploads, so that a failed upload's
+            // buffers are released with the context
+            c->m.push_back(g);
+            dg_multi::Mesh &gm = c->m.back();
+            if (!upload_real(lay.geo, &gm.geo)) break;
+            if (!upload_real(lay.fgeo, &gm.fgeo)) break;
+            if (!fin(cudaMalloc(&gm.conn, lay.conn.size() * 4), "cudaMalloc(conn)")) break;
+            if (!fin(cudaMemcpy(gm.conn, lay.conn.data(), lay.conn.size() * 4, cudaMemcpyHostToDevice), "copy conn"))
                 break;
             if (!c->d_ops[g.order]) {
                 if (!upload_real(lay.ops, &c->d_ops[g.order])) break;
@@ -586,7 +590,6 @@ int dg_multi_create(int nmesh, const dg_mesh_desc *meshes, const dg_phys_desc *p
                          "copy tabs"))
                     break;
             }
-            c->m.push_back(g);
         }
         if (rc != DG_OK) break;
         c->total = off;
