@@ -35,6 +35,33 @@ def bump3(x, a=0.15):
     return y
 
 
+def boundary_fixed_mesh(D, dim, order, n=3, a=0.04):
+    """Unit square / cube of n^dim cells (reflecting walls) whose nodes move
+    by a map that vanishes on the boundary: every element is curved, yet the
+    discrete domain is still exactly the unit square / cube."""
+    if dim == 3:
+        m = D.Mesh.box_tet(n, n, n, (0, 0, 0), (1, 1, 1), order=order, side_names=("Reflecting",) * 6)
+
+        def fn(x):
+            b = a * np.sin(np.pi * x[:, 0]) * np.sin(np.pi * x[:, 1]) * np.sin(np.pi * x[:, 2])
+            y = x.copy()
+            y[:, 0] += b
+            y[:, 1] += 0.5 * b
+            y[:, 2] -= 0.7 * b
+            return y
+    else:
+        m = D.Mesh.box_tri(n, n, (0, 0), (1, 1), order=order, side_names=("Reflecting",) * 4)
+
+        def fn(x):
+            b = a * np.sin(np.pi * x[:, 0]) * np.sin(np.pi * x[:, 1])
+            y = x.copy()
+            y[:, 0] += b
+            y[:, 1] -= 0.6 * b
+            return y
+    m.warp(fn)
+    return m
+
+
 def curved_mesh(D, dim, order, warp=None):
     if dim == 3:
         m = D.Mesh.box_tet(2, 2, 2, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), order=order,

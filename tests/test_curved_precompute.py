@@ -14,7 +14,7 @@ import pytest
 
 import dgcuda as D
 import oracle_py as O
-from curved_model import bump3, curved_mesh, model_rhs
+from curved_model import boundary_fixed_mesh, bump3, curved_mesh, model_rhs
 
 ROOT = Path(__file__).resolve().parent.parent
 
@@ -112,38 +112,12 @@ def test_per_point_algebra_matches_the_oracle_rhs(dim, order, v0, upwind):
         assert np.linalg.norm(got[q] - ref[q]) <= 1e-12 * np.linalg.norm(ref[q])
 
 
-def _boundary_fixed_warp(dim, order, n, a=0.04):
-    """A unit square / cube of n^dim cells whose nodes move by a map that
-    vanishes on the boundary: every element is curved, yet the discrete
-    domain is still exactly the unit square / cube."""
-    if dim == 3:
-        m = D.Mesh.box_tet(n, n, n, (0, 0, 0), (1, 1, 1), order=order)
-
-        def fn(x):
-            b = a * np.sin(np.pi * x[:, 0]) * np.sin(np.pi * x[:, 1]) * np.sin(np.pi * x[:, 2])
-            y = x.copy()
-            y[:, 0] += b
-            y[:, 1] += 0.5 * b
-            y[:, 2] -= 0.7 * b
-            return y
-    else:
-        m = D.Mesh.box_tri(n, n, (0, 0), (1, 1), order=order)
-
-        def fn(x):
-            b = a * np.sin(np.pi * x[:, 0]) * np.sin(np.pi * x[:, 1])
-            y = x.copy()
-            y[:, 0] += b
-            y[:, 1] -= 0.6 * b
-            return y
-    m.warp(fn)
-    return D.Precomp(m)
-
 
 @pytest.mark.parametrize("dim,order", [(2, 2), (2, 3), (2, 5), (3, 2), (3, 3), (3, 4)])
 def test_per_point_geometry_keeps_volume_surface_and_normals(dim, order):
     # detJ of a degree-p map has degree dim*(p-1) <= 2p: the Gauss(2p) rules
     # integrate it exactly, so the curved elements fill the unit domain exactly
-    pre = _boundary_fixed_warp(dim, order, 3)
+    pre = D.Precomp(boundary_fixed_mesh(D, dim, order))
     c = pre.curved_arrays()
     a = pre.arrays()
     assert c["curved"].all()

@@ -114,6 +114,25 @@ def test_standing_mode_converges_at_high_order_3d(order):
     assert rate > order + 0.5, (e1, e2, rate)
 
 
+@pytest.mark.parametrize("dim,order", [(2, 2), (2, 3), (2, 4), (3, 2), (3, 3)])
+def test_constant_state_is_steady_on_curved_elements(dim, order):
+    # every element curved (per-point form), reflecting walls: the Gauss(2p)
+    # volume and face integrals of a constant flux cancel to rounding
+    from curved_model import boundary_fixed_mesh
+
+    m = boundary_fixed_mesh(D, dim, order)
+    pre = D.Precomp(m)
+    assert pre.num_curved == pre.num_el
+    orc = oracle_for(m, 1e-5, upwind=True)
+    u = np.zeros((4, pre.ndof))
+    u[0] = 1.0
+    orc.set_state(u)
+    orc.run(0.0, 5)
+    got = orc.get_state()
+    assert np.abs(got[0] - 1.0).max() < 1e-12
+    assert np.abs(got[1:]).max() < 1e-14
+
+
 def test_upwind_energy_decays_and_reference_sign_3d_p3_grows():
     m = D.Mesh.box_tet(2, 2, 2, order=3, side_names=("Reflecting",) * 6)
     pre = D.Precomp(m)
