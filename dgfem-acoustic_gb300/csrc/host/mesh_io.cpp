@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -11,6 +12,7 @@
 #include <map>
 #include <set>
 #include <sstream>
+#include <stdexcept>
 #include <unordered_map>
 
 #include "refel.h"
@@ -95,6 +97,48 @@ struct Tok {
         size_t e = buf.find(end_marker, pos);
         pos = (e == std::string::npos) ? buf.size() : e + end_marker.size();
     }
+
+    // Binary files (MSH 4.1 and 2.2, file-type 1): section names, counts of
+    // MSH 2.2 and $PhysicalNames stay ASCII; the section data that follows
+    // the line end is raw: int = 4 bytes, size_t = data-size bytes, double =
+    // 8 bytes, in the byte order of the file's endianness marker.
+    bool bin = false, swap = false;
+    int dsize = 8;
+    void line_end() {  // the end of the ASCII line before raw data
+        while (pos < buf.size() && (buf[pos] == ' ' || buf[pos] == '\t' || buf[pos] == '\r')) ++pos;
+        if (pos < buf.size() && buf[pos] == '\n') ++pos;
+    }
+    template <typename T>
+    T raw() {
+        if (pos + sizeof(T) > buf.size()) throw std::runtime_error("truncated binary data");
+        T v;
+        std::memcpy(&v, buf.data() + pos, sizeof(T));
+        pos += sizeof(T);
+        return v;
+    }
+    uint32_t raw32() {
+        uint32_t v = raw<uint32_t>();
+        return swap ? __builtin_bswap32(v) : v;
+    }
+    uint64_t raw64() {
+        uint64_t v = raw<uint64_t>();
+        return swap ? __builtin_bswap64(v) : v;
+    }
+    // fields by their type in the format: ASCII tokens or raw values
+    long I() { return bin ? (long)(int32_t)raw32() : integer(); }
+    long S() {
+        if (!bin) return integer();
+        const uint64_t v = dsize == 8 ? raw64() : (uint64_t)raw32();
+        if (v > (uint64_t)INT32_MAX) throw std::runtime_error("count or tag too large");
+        return (long)v;
+    }
+    double R() {
+        if (!bin) return real();
+        const uint64_t v = raw64();
+        double d;
+        std::memcpy(&d, &v, 8);
+        return d;
+    }
 };
 
 struct ElemBlock {
@@ -122,8 +166,20 @@ std::string read_msh(const std::string &path, RawMesh &out) {
             if (sec == "$MeshFormat") {
                 version = t.real();
                 int ft = (int)t.integer();
-                t.integer();
-                if (ft != 0) return "binary .msh files are not supported";
+                int ds = (int)t.integer();
+                if (ft == 1) {
+                    if (version >= 4.0 && version < 4.1) return "binary MSH 4.0 files are not supported";
+                    if (ds != 4 && ds != 8) return "unsupported data size " + std::to_string(ds);
+                    t.bin = true;
+                    t.dsize = ds;
+                    t.line_end();
+                    const uint32_t one = t.raw<uint32_t>();
+                    if (one == 1u) t.swap = false;
+                    else if (__builtin_bswap32(one) == 1u) t.swap = true;
+                    else return "bad endianness marker in " + path;
+                } else if (ft != 0) {
+                    return "unknown file type " + std::to_string(ft);
+                }
                 t.skip_to("$EndMeshFormat");
             } else if (sec == "$PhysicalNames") {
                 long n = t.integer();
@@ -134,42 +190,44 @@ std::string read_msh(const std::string &path, RawMesh &out) {
                 }
                 t.skip_to("$EndPhysicalNames");
             } else if (sec == "$Entities" && version >= 4.0) {
+                if (t.bin) t.line_end();
                 long cnt[4];
-                for (int d = 0; d < 4; ++d) cnt[d] = t.integer();
+                for (int d = 0; d < 4; ++d) cnt[d] = t.S();
                 for (int d = 0; d < 4; ++d)
                     for (long e = 0; e < cnt[d]; ++e) {
-                        int tag = (int)t.integer();
+                        int tag = (int)t.I();
                         int ncoord = (d == 0 && version >= 4.1) ? 3 : 6;
-                        for (int k = 0; k < ncoord; ++k) t.real();
-                        long nph = t.integer();
+                        for (int k = 0; k < ncoord; ++k) t.R();
+                        long nph = t.S();
                         std::vector<int> ph;
-                        for (long k = 0; k < nph; ++k) ph.push_back((int)t.integer());
+                        for (long k = 0; k < nph; ++k) ph.push_back((int)t.I());
                         ent_phys[{d, tag}] = ph;
                         if (d > 0) {
-                            long nb = t.integer();
-                            for (long k = 0; k < nb; ++k) t.integer();
+                            long nb = t.S();
+                            for (long k = 0; k < nb; ++k) t.I();
                         }
                         if (cnt[d] > 0) max_ent_dim = std::max(max_ent_dim, d);
                     }
                 t.skip_to("$EndEntities");
             } else if (sec == "$Nodes") {
                 if (version >= 4.0) {
-                    long nblk = t.integer();
-                    long nn = t.integer();
-                    if (version >= 4.1) { t.integer(); t.integer(); }
+                    if (t.bin) t.line_end();
+                    long nblk = t.S();
+                    long nn = t.S();
+                    if (version >= 4.1) { t.S(); t.S(); }
                     nodes.reserve(nn);
                     for (long b = 0; b < nblk; ++b) {
-                        long a0 = t.integer(), a1 = t.integer();
+                        long a0 = t.I(), a1 = t.I();
                         (void)a0; (void)a1;
-                        int param = (int)t.integer();
-                        long n = t.integer();
+                        int param = (int)t.I();
+                        long n = t.S();
                         if (param) return "parametric nodes are not supported";
                         if (version >= 4.1) {
                             std::vector<int> tags(n);
-                            for (long i = 0; i < n; ++i) tags[i] = (int)t.integer();
+                            for (long i = 0; i < n; ++i) tags[i] = (int)t.S();
                             for (long i = 0; i < n; ++i) {
-                                std::array<double, 3> x{t.real(), t.real(), t.real()};
-                                nodes.push_back({tags[i], x});
+                                const double x0 = t.R(), x1 = t.R(), x2 = t.R();
+                                nodes.push_back({tags[i], {x0, x1, x2}});
                             }
                         } else {
                             for (long i = 0; i < n; ++i) {
@@ -180,49 +238,70 @@ std::string read_msh(const std::string &path, RawMesh &out) {
                         }
                     }
                 } else {
-                    long nn = t.integer();
+                    long nn = t.integer();  // ASCII in binary files too
+                    if (t.bin) t.line_end();
                     nodes.reserve(nn);
                     for (long i = 0; i < nn; ++i) {
-                        int tag = (int)t.integer();
-                        std::array<double, 3> x{t.real(), t.real(), t.real()};
-                        nodes.push_back({tag, x});
+                        int tag = (int)t.I();
+                        const double x0 = t.R(), x1 = t.R(), x2 = t.R();
+                        nodes.push_back({tag, {x0, x1, x2}});
                     }
                 }
                 t.skip_to("$EndNodes");
             } else if (sec == "$Elements") {
                 if (version >= 4.0) {
-                    long nblk = t.integer();
-                    t.integer();
-                    if (version >= 4.1) { t.integer(); t.integer(); }
+                    if (t.bin) t.line_end();
+                    long nblk = t.S();
+                    t.S();
+                    if (version >= 4.1) { t.S(); t.S(); }
                     for (long b = 0; b < nblk; ++b) {
                         ElemBlock eb;
-                        long a0 = t.integer(), a1 = t.integer();
+                        long a0 = t.I(), a1 = t.I();
                         if (version >= 4.1) { eb.ent_dim = (int)a0; eb.ent_tag = (int)a1; }
                         else { eb.ent_tag = (int)a0; eb.ent_dim = (int)a1; }
-                        eb.type = (int)t.integer();
-                        long n = t.integer();
+                        eb.type = (int)t.I();
+                        long n = t.S();
                         int d, p, np;
                         if (!gmsh_type_info(eb.type, &d, &p, &np))
                             return "unsupported element type " + std::to_string(eb.type);
                         eb.tags.resize(n);
                         eb.nodes.resize(n * np);
                         for (long i = 0; i < n; ++i) {
-                            eb.tags[i] = (int)t.integer();
-                            for (int k = 0; k < np; ++k) eb.nodes[i * np + k] = (int)t.integer();
+                            eb.tags[i] = (int)t.S();
+                            for (int k = 0; k < np; ++k) eb.nodes[i * np + k] = (int)t.S();
                         }
                         blocks.push_back(std::move(eb));
                     }
                 } else {
-                    long ne = t.integer();
-                    // MSH2: group per (type, physical, elementary)
+                    long ne = t.integer();  // ASCII in binary files too
+                    if (t.bin) t.line_end();
+                    // MSH2: group per (type, physical, elementary); binary
+                    // files give the elements in runs of one type and tag
+                    // count (header: type, run length, tag count)
                     std::map<std::array<int, 3>, size_t> idx;
+                    long run = 0;
+                    int run_type = 0, run_ntags = 0;
                     for (long i = 0; i < ne; ++i) {
-                        int tag = (int)t.integer();
-                        int type = (int)t.integer();
-                        int ntags = (int)t.integer();
+                        int tag, type, ntags;
+                        if (t.bin) {
+                            if (run == 0) {
+                                run_type = (int)t.I();
+                                run = t.I();
+                                run_ntags = (int)t.I();
+                                if (run < 1 || run_ntags < 0) return "bad element run header in " + path;
+                            }
+                            --run;
+                            tag = (int)t.I();
+                            type = run_type;
+                            ntags = run_ntags;
+                        } else {
+                            tag = (int)t.integer();
+                            type = (int)t.integer();
+                            ntags = (int)t.integer();
+                        }
                         int phys = 0, elem = 0;
                         for (int k = 0; k < ntags; ++k) {
-                            int v = (int)t.integer();
+                            int v = (int)t.I();
                             if (k == 0) phys = v;
                             if (k == 1) elem = v;
                         }
@@ -245,7 +324,7 @@ std::string read_msh(const std::string &path, RawMesh &out) {
                         }
                         ElemBlock &eb = blocks[it->second];
                         eb.tags.push_back(tag);
-                        for (int k = 0; k < np; ++k) eb.nodes.push_back((int)t.integer());
+                        for (int k = 0; k < np; ++k) eb.nodes.push_back((int)t.I());
                         max_ent_dim = std::max(max_ent_dim, d);
                     }
                 }

@@ -3,7 +3,8 @@
 // getPhysicalGroups / getPhysicalName; dgalerkin.cpp:24-26, Mesh.cpp:25-38,
 // 371, configParser.cpp:117-132).
 //
-// Readers: MSH 2.2, 4.0 and 4.1 ASCII.  Writer: MSH 4.1 ASCII.
+// Readers: MSH 2.2, 4.0 and 4.1 ASCII; MSH 2.2 and 4.1 binary (either byte
+// order, data size 4 or 8).  Writer: MSH 4.1 ASCII.
 // Generators: structured boxes of straight-sided simplices of any order 1..5,
 // with high-order nodes shared between neighbours (as gmsh meshes have them),
 // boundary facets grouped per side into physical groups, and optional removed

@@ -159,3 +159,61 @@ def test_reference_meshes(path):
     # every interior face has two neighbours, every boundary face one
     nbr = a["f_nbr_el_ids"]
     assert np.all((nbr[:, 1] >= 0) == (a["f_is_boundary"] == 0))
+
+
+def _same_mesh(m1, m2):
+    r1, r2 = m1.raw(), m2.raw()
+    assert np.array_equal(r1["el_nodes"], r2["el_nodes"])
+    assert np.array_equal(r1["xyz"], r2["xyz"])
+    assert r1["phys_name"] == r2["phys_name"]
+    for g in range(len(r1["phys_name"])):
+        a = r1["phys_nodes"][r1["phys_offsets"][g]:r1["phys_offsets"][g + 1]]
+        b = r2["phys_nodes"][r2["phys_offsets"][g]:r2["phys_offsets"][g + 1]]
+        assert np.array_equal(a, b)
+    p1, p2 = D.Precomp(m1).arrays(), D.Precomp(m2).arrays()
+    for k in ("el_f_ids", "f_bc", "el_f_orientation", "f_nbr_el_ids", "f_n_to_el_n_ids"):
+        assert np.array_equal(p1[k], p2[k]), k
+
+
+@pytest.mark.parametrize("dim,order", [(2, 1), (2, 3), (3, 2), (3, 4)])
+@pytest.mark.parametrize("fmt", ["41-le", "41-be", "41-le-size4", "22-le", "22-be"])
+def test_binary_msh_reads_like_ascii(tmp_path, dim, order, fmt):
+    from msh_binary import parse_msh41, write_msh22_binary, write_msh41_binary
+
+    if dim == 2:
+        m = D.Mesh.box_tri(3, 2, order=order, side_names=("Absorbing", "Reflecting") * 2)
+    else:
+        m = D.Mesh.box_tet(2, 1, 2, order=order, side_names=("Absorbing", "Reflecting") * 3)
+    src = tmp_path / "ascii.msh"
+    m.write_msh(src)
+    parsed = parse_msh41(src)
+    dst = tmp_path / "binary.msh"
+    endian = ">" if fmt.endswith("be") else "<"
+    if fmt.startswith("41"):
+        write_msh41_binary(parsed, dst, endian=endian, dsize=4 if fmt.endswith("size4") else 8)
+    else:
+        write_msh22_binary(parsed, dst, endian=endian)
+    _same_mesh(D.Mesh.read_msh(src), D.Mesh.read_msh(dst))
+
+
+def test_binary_msh_errors(tmp_path):
+    from msh_binary import parse_msh41, write_msh41_binary
+
+    m = D.Mesh.box_tri(2, 2, order=2)
+    src = tmp_path / "ascii.msh"
+    m.write_msh(src)
+    good = tmp_path / "good.msh"
+    write_msh41_binary(parse_msh41(src), good)
+    data = good.read_bytes()
+    cases = {
+        # binary MSH 4.0 uses other field types: refused rather than misread
+        "v40.msh": (data.replace(b"4.1 1 8", b"4.0 1 8", 1), "4.0"),
+        "marker.msh": (data.replace(b"4.1 1 8\n\x01\x00\x00\x00", b"4.1 1 8\n\x02\x00\x00\x00", 1), "endianness"),
+        "cut.msh": (data[:data.index(b"$Nodes") + 40], "truncated"),
+        "size.msh": (data.replace(b"4.1 1 8", b"4.1 1 2", 1), "data size"),
+    }
+    for name, (blob, words) in cases.items():
+        p = tmp_path / name
+        p.write_bytes(blob)
+        with pytest.raises(RuntimeError, match=words):
+            D.Mesh.read_msh(p)
