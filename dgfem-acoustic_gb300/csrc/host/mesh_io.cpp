@@ -218,21 +218,25 @@ std::string read_msh(const std::string &path, RawMesh &out) {
                     nodes.reserve(nn);
                     for (long b = 0; b < nblk; ++b) {
                         long a0 = t.I(), a1 = t.I();
-                        (void)a0; (void)a1;
+                        const int edim = (int)(version >= 4.1 ? a0 : a1);
                         int param = (int)t.I();
                         long n = t.S();
-                        if (param) return "parametric nodes are not supported";
+                        // parametric blocks add the node's entityDim
+                        // parametric coordinates after x y z (skipped)
+                        const int npar = param ? std::max(0, std::min(edim, 3)) : 0;
                         if (version >= 4.1) {
                             std::vector<int> tags(n);
                             for (long i = 0; i < n; ++i) tags[i] = (int)t.S();
                             for (long i = 0; i < n; ++i) {
                                 const double x0 = t.R(), x1 = t.R(), x2 = t.R();
+                                for (int k = 0; k < npar; ++k) t.R();
                                 nodes.push_back({tags[i], {x0, x1, x2}});
                             }
                         } else {
                             for (long i = 0; i < n; ++i) {
                                 int tag = (int)t.integer();
                                 std::array<double, 3> x{t.real(), t.real(), t.real()};
+                                for (int k = 0; k < npar; ++k) t.real();
                                 nodes.push_back({tag, x});
                             }
                         }

@@ -83,7 +83,8 @@ def write_msh41_binary(m: dict, path: str | Path, endian: str = "<", dsize: int 
     out += b"$Nodes\n" + p("4" + S, len(m["nodes"]), len(tags), min(tags), max(tags))
     for ed, et, par, tg, xyz in m["nodes"]:
         out += p("3i", ed, et, par) + p(S, len(tg)) + p("%d%s" % (len(tg), S), *tg)
-        out += p("%dd" % (3 * len(xyz)), *[c for x in xyz for c in x])
+        flat = [c for x in xyz for c in x]  # x y z and any parametric coordinates
+        out += p("%dd" % len(flat), *flat)
     out += b"\n$EndNodes\n"
     etags = [e[0] for b in m["elements"] for e in b[3]]
     out += b"$Elements\n" + p("4" + S, len(m["elements"]), len(etags), min(etags), max(etags))
@@ -115,3 +116,75 @@ def write_msh22_binary(m: dict, path: str | Path, endian: str = "<") -> None:
             out += p("3i", e[0], ent_phys[(ed, et)], et) + p("%di" % (len(e) - 1), *e[1:])
     out += b"\n$EndElements\n"
     Path(path).write_bytes(out)
+
+
+def _fmt(v) -> str:
+    return repr(float(v))
+
+
+def write_msh41_ascii(m: dict, path: str | Path) -> None:
+    out = ["$MeshFormat", "4.1 0 8", "$EndMeshFormat"]
+    txt = _phys_section(m).decode()
+    if txt:
+        out += txt.strip("\n").split("\n")
+    out += ["$Entities", " ".join(map(str, m["counts"]))]
+    for d, tag, box, ph, bnd in m["ents"]:
+        row = [str(tag)] + [_fmt(v) for v in box] + [str(len(ph))] + [str(v) for v in ph]
+        if d > 0:
+            row += [str(len(bnd))] + [str(v) for v in bnd]
+        out.append(" ".join(row))
+    out.append("$EndEntities")
+    tags = [t for b in m["nodes"] for t in b[3]]
+    out += ["$Nodes", f"{len(m['nodes'])} {len(tags)} {min(tags)} {max(tags)}"]
+    for ed, et, par, tg, xyz in m["nodes"]:
+        out.append(f"{ed} {et} {par} {len(tg)}")
+        out += [str(t) for t in tg]
+        out += [" ".join(_fmt(c) for c in x) for x in xyz]
+    out.append("$EndNodes")
+    etags = [e[0] for b in m["elements"] for e in b[3]]
+    out += ["$Elements", f"{len(m['elements'])} {len(etags)} {min(etags)} {max(etags)}"]
+    for ed, et, typ, els in m["elements"]:
+        out.append(f"{ed} {et} {typ} {len(els)}")
+        out += [" ".join(map(str, e)) for e in els]
+    out.append("$EndElements")
+    Path(path).write_text("\n".join(out) + "\n")
+
+
+def write_msh40_ascii(m: dict, path: str | Path) -> None:
+    """MSH 4.0: points carry a 6-value box, block headers give the entity tag
+    before its dimension, nodes are "tag x y z [params]" lines, and the
+    section headers have no tag ranges."""
+    out = ["$MeshFormat", "4 0 8", "$EndMeshFormat"]
+    txt = _phys_section(m).decode()
+    if txt:
+        out += txt.strip("\n").split("\n")
+    out += ["$Entities", " ".join(map(str, m["counts"]))]
+    for d, tag, box, ph, bnd in m["ents"]:
+        b6 = box if d > 0 else box + box
+        row = [str(tag)] + [_fmt(v) for v in b6] + [str(len(ph))] + [str(v) for v in ph]
+        if d > 0:
+            row += [str(len(bnd))] + [str(v) for v in bnd]
+        out.append(" ".join(row))
+    out.append("$EndEntities")
+    nn = sum(len(b[3]) for b in m["nodes"])
+    out += ["$Nodes", f"{len(m['nodes'])} {nn}"]
+    for ed, et, par, tg, xyz in m["nodes"]:
+        out.append(f"{et} {ed} {par} {len(tg)}")
+        out += [f"{t} " + " ".join(_fmt(c) for c in x) for t, x in zip(tg, xyz)]
+    out.append("$EndNodes")
+    ne = sum(len(b[3]) for b in m["elements"])
+    out += ["$Elements", f"{len(m['elements'])} {ne}"]
+    for ed, et, typ, els in m["elements"]:
+        out.append(f"{et} {ed} {typ} {len(els)}")
+        out += [" ".join(map(str, e)) for e in els]
+    out.append("$EndElements")
+    Path(path).write_text("\n".join(out) + "\n")
+
+
+def with_parametric_nodes(m: dict) -> dict:
+    """The same mesh with every node block marked parametric: each node gains
+    entityDim parametric coordinates after x y z."""
+    m = dict(m)
+    m["nodes"] = [(ed, et, 1, tg, [list(x) + [0.125 * (k + 1) for k in range(ed)] for x in xyz])
+                  for ed, et, par, tg, xyz in m["nodes"]]
+    return m

@@ -217,3 +217,20 @@ def test_binary_msh_errors(tmp_path):
         p.write_bytes(blob)
         with pytest.raises(RuntimeError, match=words):
             D.Mesh.read_msh(p)
+
+
+@pytest.mark.parametrize("fmt", ["40-ascii", "41-ascii", "41-binary"])
+@pytest.mark.parametrize("parametric", [False, True])
+def test_msh4_encodings_and_parametric_nodes(tmp_path, fmt, parametric):
+    from msh_binary import (parse_msh41, with_parametric_nodes, write_msh40_ascii, write_msh41_ascii,
+                            write_msh41_binary)
+
+    m = D.Mesh.box_tet(2, 2, 1, order=3, side_names=("Absorbing", "Reflecting") * 3)
+    src = tmp_path / "ascii.msh"
+    m.write_msh(src)
+    parsed = parse_msh41(src)
+    if parametric:
+        parsed = with_parametric_nodes(parsed)
+    dst = tmp_path / "other.msh"
+    {"40-ascii": write_msh40_ascii, "41-ascii": write_msh41_ascii, "41-binary": write_msh41_binary}[fmt](parsed, dst)
+    _same_mesh(D.Mesh.read_msh(src), D.Mesh.read_msh(dst))
