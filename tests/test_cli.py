@@ -110,12 +110,6 @@ def test_cli_curved_mesh_matches_oracle(tmp_path):
     assert np.linalg.norm(p - ref) <= 1e-10 * np.linalg.norm(ref)
 
 
-def test_cli_argument_count():
-    exe = D.PKG / "lib" / "dgalerkin"
-    r = subprocess.run([str(exe), "only-one"], capture_output=True)
-    assert r.returncode != 0
-
-
 def test_cli_forward_euler_and_unknown_method(tmp_path):
     """timeIntMethod = Euler1 runs forward Euler (dgalerkin.cpp:55-56); a name
     the reference does not know runs nothing and writes no views."""
