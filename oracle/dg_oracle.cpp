@@ -953,7 +953,12 @@ void *oracle_create(const oracle_input *in, char *err, int errlen) {
         }
         Config c;
         c.timeStep = in->time_step;
-        c.numThreads = in->num_threads;
+        // the reference's numThreads key: 1 is read as 0, the OpenMP default
+        // team (configParser.cpp:57-58).  With a one-thread outer team the
+        // nested face loop's inner `parallel for` would become the active
+        // level and share the outer region's scratch vectors across threads;
+        // the reference never reaches that state, and neither does the oracle.
+        c.numThreads = in->num_threads == 1 ? 0 : in->num_threads;
         c.v0 = {in->v0[0], in->v0[1], in->v0[2]};
         c.rho0 = in->rho0;
         c.c0 = in->c0;

@@ -71,7 +71,11 @@ def _arr(ptr, n, dtype):
 
 
 class Oracle:
-    """Faithful CPU restatement of the reference solver on a raw mesh."""
+    """Faithful CPU restatement of the reference solver on a raw mesh.
+
+    num_threads is the reference's numThreads configuration key: the OpenMP
+    team of its element and face loops, with 0 (and 1, which the reference
+    reads as 0) meaning the OpenMP default team."""
 
     def __init__(self, raw: dict, time_step: float, c0: float, rho0: float, v0=(0.0, 0.0, 0.0),
                  bcs=(), sources=None, num_threads: int = 0, upwind: bool = False):

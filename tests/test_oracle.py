@@ -133,6 +133,19 @@ def test_constant_state_is_steady_on_curved_elements(dim, order):
     assert np.abs(got[1:]).max() < 1e-14
 
 
+def test_right_hand_side_is_the_same_for_every_thread_count():
+    # numThreads = 1 is read as 0 (configParser.cpp:57-58): with a one-thread
+    # outer team the nested face loop would share its scratch vectors
+    m = D.Mesh.box_tet(2, 2, 2, order=2, side_names=("Reflecting", "Absorbing") * 3)
+    pre = D.Precomp(m)
+    u0 = pre.initial_state([(0, 0.4, 0.5, 0.6, 0.02, 1.0)])
+    ref = oracle_for(m, 1e-5, upwind=True, num_threads=0).rhs(u0)
+    for nt in (1, 2, 3):
+        o = oracle_for(m, 1e-5, upwind=True, num_threads=nt)
+        for _ in range(3):
+            assert np.array_equal(o.rhs(u0), ref), nt
+
+
 def test_upwind_energy_decays_and_reference_sign_3d_p3_grows():
     m = D.Mesh.box_tet(2, 2, 2, order=3, side_names=("Reflecting",) * 6)
     pre = D.Precomp(m)
