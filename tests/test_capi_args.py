@@ -107,3 +107,30 @@ def test_inconsistent_meshes(dim):
         assert code == DG_ERR_MESH, (name, code, msg)
         assert words in msg, (name, msg)
         assert not h.value
+
+
+def test_last_error_is_per_thread():
+    import threading
+
+    x, y = Desc(2, 2), Desc(3, 2)
+    x.d.order = 9          # -> "order must be in 1..5"
+    y.d.num_el = 0         # -> "empty mesh"
+    got = {}
+    barrier = threading.Barrier(2)
+
+    def work(name, d):
+        barrier.wait()
+        for _ in range(200):
+            code, msg, _ = create(d)
+            got.setdefault(name, set()).add((code, msg))
+
+    ts = [threading.Thread(target=work, args=("order", x.d)), threading.Thread(target=work, args=("empty", y.d))]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert len(got["order"]) == 1 and len(got["empty"]) == 1
+    (c1, m1), = got["order"]
+    (c2, m2), = got["empty"]
+    assert c1 == DG_ERR_UNSUPPORTED and "order" in m1
+    assert c2 == DG_ERR_MESH and "empty" in m2
