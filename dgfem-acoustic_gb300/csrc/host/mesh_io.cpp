@@ -87,6 +87,7 @@ struct Tok {
         skip_ws();
         if (pos < buf.size() && buf[pos] == '"') {
             size_t e = buf.find('"', pos + 1);
+            if (e == std::string::npos) throw std::runtime_error("unterminated quoted string");
             std::string s = buf.substr(pos + 1, e - pos - 1);
             pos = e + 1;
             return s;
@@ -123,6 +124,13 @@ struct Tok {
     uint64_t raw64() {
         uint64_t v = raw<uint64_t>();
         return swap ? __builtin_bswap64(v) : v;
+    }
+    // a count read from the file: each item takes at least min_bytes of what
+    // is left, so larger counts are corrupt (and must not size an allocation)
+    long count(long n, long min_bytes) {
+        const long left = (long)(buf.size() - std::min(pos, buf.size()));
+        if (n < 0 || n > left / std::max(1L, min_bytes)) throw std::runtime_error("count exceeds the file");
+        return n;
     }
     // fields by their type in the format: ASCII tokens or raw values
     long I() { return bin ? (long)(int32_t)raw32() : integer(); }
@@ -182,28 +190,29 @@ std::string read_msh(const std::string &path, RawMesh &out) {
                 }
                 t.skip_to("$EndMeshFormat");
             } else if (sec == "$PhysicalNames") {
-                long n = t.integer();
+                long n = t.count(t.integer(), 6);
                 for (long i = 0; i < n; ++i) {
                     int d = (int)t.integer();
                     int tag = (int)t.integer();
+                    if (d < 0 || d > 3) return "invalid physical group dimension " + std::to_string(d) + " in " + path;
                     names_by_tag[d][tag] = t.quoted();
                 }
                 t.skip_to("$EndPhysicalNames");
             } else if (sec == "$Entities" && version >= 4.0) {
                 if (t.bin) t.line_end();
                 long cnt[4];
-                for (int d = 0; d < 4; ++d) cnt[d] = t.S();
+                for (int d = 0; d < 4; ++d) cnt[d] = t.count(t.S(), 4);
                 for (int d = 0; d < 4; ++d)
                     for (long e = 0; e < cnt[d]; ++e) {
                         int tag = (int)t.I();
                         int ncoord = (d == 0 && version >= 4.1) ? 3 : 6;
                         for (int k = 0; k < ncoord; ++k) t.R();
-                        long nph = t.S();
+                        long nph = t.count(t.S(), 1);
                         std::vector<int> ph;
                         for (long k = 0; k < nph; ++k) ph.push_back((int)t.I());
                         ent_phys[{d, tag}] = ph;
                         if (d > 0) {
-                            long nb = t.S();
+                            long nb = t.count(t.S(), 1);
                             for (long k = 0; k < nb; ++k) t.I();
                         }
                         if (cnt[d] > 0) max_ent_dim = std::max(max_ent_dim, d);
@@ -212,15 +221,15 @@ std::string read_msh(const std::string &path, RawMesh &out) {
             } else if (sec == "$Nodes") {
                 if (version >= 4.0) {
                     if (t.bin) t.line_end();
-                    long nblk = t.S();
-                    long nn = t.S();
+                    long nblk = t.count(t.S(), 4);
+                    long nn = t.count(t.S(), 4);
                     if (version >= 4.1) { t.S(); t.S(); }
                     nodes.reserve(nn);
                     for (long b = 0; b < nblk; ++b) {
                         long a0 = t.I(), a1 = t.I();
                         const int edim = (int)(version >= 4.1 ? a0 : a1);
                         int param = (int)t.I();
-                        long n = t.S();
+                        long n = t.count(t.S(), 4);
                         // parametric blocks add the node's entityDim
                         // parametric coordinates after x y z (skipped)
                         const int npar = param ? std::max(0, std::min(edim, 3)) : 0;
@@ -242,7 +251,7 @@ std::string read_msh(const std::string &path, RawMesh &out) {
                         }
                     }
                 } else {
-                    long nn = t.integer();  // ASCII in binary files too
+                    long nn = t.count(t.integer(), 4);  // ASCII in binary files too
                     if (t.bin) t.line_end();
                     nodes.reserve(nn);
                     for (long i = 0; i < nn; ++i) {
@@ -255,7 +264,7 @@ std::string read_msh(const std::string &path, RawMesh &out) {
             } else if (sec == "$Elements") {
                 if (version >= 4.0) {
                     if (t.bin) t.line_end();
-                    long nblk = t.S();
+                    long nblk = t.count(t.S(), 4);
                     t.S();
                     if (version >= 4.1) { t.S(); t.S(); }
                     for (long b = 0; b < nblk; ++b) {
@@ -268,6 +277,10 @@ std::string read_msh(const std::string &path, RawMesh &out) {
                         int d, p, np;
                         if (!gmsh_type_info(eb.type, &d, &p, &np))
                             return "unsupported element type " + std::to_string(eb.type);
+                        if (eb.ent_dim != d)
+                            return "element block of dimension " + std::to_string(eb.ent_dim) + " holds type " +
+                                   std::to_string(eb.type) + " in " + path;
+                        t.count(n, 2L * (np + 1));
                         eb.tags.resize(n);
                         eb.nodes.resize(n * np);
                         for (long i = 0; i < n; ++i) {
@@ -277,7 +290,7 @@ std::string read_msh(const std::string &path, RawMesh &out) {
                         blocks.push_back(std::move(eb));
                     }
                 } else {
-                    long ne = t.integer();  // ASCII in binary files too
+                    long ne = t.count(t.integer(), 4);  // ASCII in binary files too
                     if (t.bin) t.line_end();
                     // MSH2: group per (type, physical, elementary); binary
                     // files give the elements in runs of one type and tag
@@ -337,7 +350,11 @@ std::string read_msh(const std::string &path, RawMesh &out) {
                 std::string end = "$End" + sec.substr(1);
                 t.skip_to(end);
             } else {
-                return "unexpected token '" + sec + "' in " + path;
+                // quote at most 32 bytes of the token, non-printable ones as '?'
+                std::string shown;
+                for (size_t k = 0; k < sec.size() && k < 32; ++k)
+                    shown += (sec[k] >= 0x20 && sec[k] < 0x7f) ? sec[k] : '?';
+                return "unexpected token '" + shown + (sec.size() > 32 ? "...'" : "'") + " in " + path;
             }
         }
     } catch (std::exception &e) {
@@ -352,6 +369,15 @@ std::string read_msh(const std::string &path, RawMesh &out) {
               [](const std::pair<int, std::array<double, 3>> &a, const std::pair<int, std::array<double, 3>> &b) {
                   return a.first < b.first;
               });
+    // gmsh tags start at 1; a node tag may appear once
+    for (size_t i = 0; i < nodes.size(); ++i) {
+        if (nodes[i].first < 1) return "invalid node tag " + std::to_string(nodes[i].first) + " in " + path;
+        if (i > 0 && nodes[i].first == nodes[i - 1].first)
+            return "duplicate node tag " + std::to_string(nodes[i].first) + " in " + path;
+    }
+    for (auto &b : blocks)
+        for (int t : b.nodes)
+            if (t < 1) return "invalid element node tag " + std::to_string(t) + " in " + path;
     out.node_tags.resize(nodes.size());
     out.xyz.resize(nodes.size() * 3);
     for (size_t i = 0; i < nodes.size(); ++i) {

@@ -218,14 +218,34 @@ std::string precompute(const RawMesh &m, const std::vector<std::pair<int, bool>>
     P.fc = (dim == 3 && m.order != 1) ? -1 : 1;
     P.el_node_tags = m.el_nodes;
 
-    // node tag -> coordinates
+    // node tag -> coordinates: a dense table, or a hash map when the tags
+    // are sparse (tags are positive and unique)
+    if (m.xyz.size() != m.node_tags.size() * 3) return "node coordinate count mismatch";
     int maxtag = 0;
-    for (int t : m.node_tags) maxtag = std::max(maxtag, t);
-    std::vector<int> idx(maxtag + 1, -1);
-    for (size_t i = 0; i < m.node_tags.size(); ++i) idx[m.node_tags[i]] = (int)i;
+    for (int t : m.node_tags) {
+        if (t < 1) return "invalid node tag " + std::to_string(t);
+        maxtag = std::max(maxtag, t);
+    }
+    const bool dense = (size_t)maxtag <= 8 * m.node_tags.size() + 1024;
+    std::vector<int> idx(dense ? (size_t)maxtag + 1 : 0, -1);
+    std::unordered_map<int, int> sparse;
+    for (size_t i = 0; i < m.node_tags.size(); ++i) {
+        const int t = m.node_tags[i];
+        const bool fresh = dense ? idx[t] < 0 : sparse.find(t) == sparse.end();
+        if (!fresh) return "duplicate node tag " + std::to_string(t);
+        if (dense) idx[t] = (int)i;
+        else sparse[t] = (int)i;
+    }
     auto X = [&](int tag) -> const double * {
-        if (tag < 0 || tag > maxtag || idx[tag] < 0) return nullptr;
-        return &m.xyz[idx[tag] * 3];
+        if (tag < 1 || tag > maxtag) return nullptr;
+        int i = -1;
+        if (dense) {
+            i = idx[tag];
+        } else {
+            auto it = sparse.find(tag);
+            if (it != sparse.end()) i = it->second;
+        }
+        return i < 0 ? nullptr : &m.xyz[(size_t)i * 3];
     };
     for (int t : m.el_nodes)
         if (!X(t)) return "element references an unknown node tag " + std::to_string(t);

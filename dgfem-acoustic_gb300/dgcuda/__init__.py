@@ -54,7 +54,7 @@ def lib() -> C.CDLL:
 
 def _check(code: int) -> None:
     if code != 0:
-        raise DGError(code, lib().dg_last_error().decode())
+        raise DGError(code, lib().dg_last_error().decode(errors="replace"))
 
 
 P_d, P_i, P_u8 = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_ubyte)
@@ -288,7 +288,7 @@ class Mesh:
             "el_nodes": _arr(v.el_nodes, v.num_el * v.np, np.int32).reshape(-1, v.np),
             "phys_dim": _arr(v.phys_dim, v.num_phys, np.int32),
             "phys_tag": _arr(v.phys_tag, v.num_phys, np.int32),
-            "phys_name": [v.phys_name[i].decode() for i in range(v.num_phys)],
+            "phys_name": [v.phys_name[i].decode(errors="replace") for i in range(v.num_phys)],
             "phys_offsets": off,
             "phys_nodes": _arr(v.phys_nodes, int(off[-1]) if off.size else 0, np.int32),
         }
@@ -328,11 +328,11 @@ class Config:
         tags = _arr(v.bc_phys_tags, v.num_bcs, np.int32)
         refl = _arr(v.bc_reflecting, v.num_bcs, np.int32)
         self.bcs = [(int(a), bool(b)) for a, b in zip(tags, refl)]
-        self.element_type = v.element_type.decode()
-        self.time_int_method = v.time_int_method.decode()
-        self.save_file = v.save_file.decode()
-        self.precision = v.precision.decode()
-        self.flux_sign = v.flux_sign.decode()
+        self.element_type = v.element_type.decode(errors="replace")
+        self.time_int_method = v.time_int_method.decode(errors="replace")
+        self.save_file = v.save_file.decode(errors="replace")
+        self.precision = v.precision.decode(errors="replace")
+        self.flux_sign = v.flux_sign.decode(errors="replace")
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
