@@ -52,6 +52,17 @@ def lib() -> C.CDLL:
     return _lib
 
 
+def _check_out(out, shape) -> None:
+    """An output buffer the library writes into: float64, the given shape,
+    every row contiguous (it is filled in place, never copied)."""
+    if not isinstance(out, np.ndarray) or out.dtype != np.float64 or out.shape != shape:
+        raise ValueError(f"output must be a float64 array of shape {shape}")
+    if not all(out[q].flags["C_CONTIGUOUS"] for q in range(shape[0])):
+        raise ValueError("output rows must be contiguous")
+    if not out.flags["WRITEABLE"]:
+        raise ValueError("output must be writeable")
+
+
 def _check(code: int) -> None:
     if code != 0:
         raise DGError(code, lib().dg_last_error().decode(errors="replace"))
@@ -506,7 +517,8 @@ class Solver:
     def set_state(self, u: np.ndarray, member: int | None = None) -> None:
         """Sets every batch member (member=None) or one member to u [4][ndof]."""
         u = np.ascontiguousarray(u, dtype=np.float64)
-        assert u.shape == (4, self.ndof)
+        if u.shape != (4, self.ndof):
+            raise ValueError(f"state must have shape (4, {self.ndof}), got {u.shape}")
         ptrs = (P_d * 4)(*[_dptr(u[q]) for q in range(4)])
         if member is None:
             _check(lib().dg_set_state(self._h, ptrs))
@@ -516,6 +528,8 @@ class Solver:
     def get_state(self, out: np.ndarray | None = None, member: int = 0) -> np.ndarray:
         if out is None:
             out = np.empty((4, self.ndof))
+        else:
+            _check_out(out, (4, self.ndof))
         ptrs = (P_d * 4)(*[_dptr(out[q]) for q in range(4)])
         _check(lib().dg_get_state_member(self._h, member, ptrs))
         return out
@@ -542,7 +556,9 @@ class Solver:
         for s, (m, dofs, w, amp, freq, phase, dur) in enumerate(sources):
             mem[s] = m
             idx.append(np.asarray(dofs, dtype=np.int32))
-            wts.append(np.ones(len(dofs)) if w is None else np.asarray(w, dtype=np.float64))
+            wts.append(np.ones(len(dofs)) if w is None else np.asarray(w, dtype=np.float64).reshape(-1))
+            if len(wts[-1]) != len(idx[-1]):
+                raise ValueError(f"source {s}: {len(idx[-1])} node indices but {len(wts[-1])} weights")
             off[s + 1] = off[s] + len(dofs)
             par += [amp, freq, phase, dur]
         idx_a = np.concatenate(idx) if idx else np.zeros(1, dtype=np.int32)
@@ -664,11 +680,17 @@ class MultiSolver:
     __del__ = close
 
     def set_state(self, mesh: int, u: np.ndarray) -> None:
+        if not 0 <= mesh < len(self.pres):
+            raise ValueError(f"mesh index {mesh} out of range")
         u = np.ascontiguousarray(u, dtype=np.float64)
+        if u.shape != (4, self.pres[mesh].ndof):
+            raise ValueError(f"state must have shape (4, {self.pres[mesh].ndof}), got {u.shape}")
         ptrs = (P_d * 4)(*[_dptr(u[q]) for q in range(4)])
         _check(lib().dg_multi_set_state(self._h, mesh, ptrs))
 
     def get_state(self, mesh: int) -> np.ndarray:
+        if not 0 <= mesh < len(self.pres):
+            raise ValueError(f"mesh index {mesh} out of range")
         out = np.empty((4, self.pres[mesh].ndof))
         ptrs = (P_d * 4)(*[_dptr(out[q]) for q in range(4)])
         _check(lib().dg_multi_get_state(self._h, mesh, ptrs))
@@ -683,7 +705,9 @@ class MultiSolver:
         for s, (m, dofs, w, amp, freq, phase, dur) in enumerate(sources):
             mesh[s] = m
             idx.append(np.asarray(dofs, dtype=np.int32))
-            wts.append(np.ones(len(dofs)) if w is None else np.asarray(w, dtype=np.float64))
+            wts.append(np.ones(len(dofs)) if w is None else np.asarray(w, dtype=np.float64).reshape(-1))
+            if len(wts[-1]) != len(idx[-1]):
+                raise ValueError(f"source {s}: {len(idx[-1])} node indices but {len(wts[-1])} weights")
             off[s + 1] = off[s] + len(dofs)
             par += [amp, freq, phase, dur]
         idx_a = np.concatenate(idx) if idx else np.zeros(1, dtype=np.int32)
@@ -692,15 +716,21 @@ class MultiSolver:
         _check(lib().dg_multi_set_sources(self._h, n, _iptr(mesh), _iptr(off), _iptr(idx_a), _dptr(w_a),
                                           _dptr(par_a)))
 
+    def _per_mesh(self, a, name: str) -> np.ndarray:
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+        if a.size != len(self.pres):
+            raise ValueError(f"{name} needs one value per mesh ({len(self.pres)}), got {a.size}")
+        return a
+
     def rk4_steps(self, t, dt, nsteps: int) -> np.ndarray:
-        tt = np.ascontiguousarray(t, dtype=np.float64).copy()
-        d = np.ascontiguousarray(dt, dtype=np.float64)
+        tt = self._per_mesh(t, "t").copy()
+        d = self._per_mesh(dt, "dt")
         _check(lib().dg_multi_rk4_steps(self._h, _dptr(tt), _dptr(d), nsteps))
         return tt
 
     def rk4_steps_timed(self, t, dt, nsteps: int) -> tuple[np.ndarray, float]:
-        tt = np.ascontiguousarray(t, dtype=np.float64).copy()
-        d = np.ascontiguousarray(dt, dtype=np.float64)
+        tt = self._per_mesh(t, "t").copy()
+        d = self._per_mesh(dt, "dt")
         ms = C.c_double()
         _check(lib().dg_multi_rk4_steps_timed(self._h, _dptr(tt), _dptr(d), nsteps, C.byref(ms)))
         return tt, ms.value
@@ -709,7 +739,7 @@ class MultiSolver:
         _check(lib().dg_multi_set_config(self._h, cfg))
 
     def autotune(self, dt, trial_steps: int = 4) -> tuple[int, list]:
-        d = np.ascontiguousarray(dt, dtype=np.float64)
+        d = self._per_mesh(dt, "dt")
         info = self.info()
         ms = np.zeros(info["ncfg"])
         ch = C.c_int()
