@@ -64,6 +64,10 @@ std::string parse_config(const std::string &path, const RawMesh &mesh, Config &c
     if (!(err = need_d("timeEnd", c.timeEnd)).empty()) return err;
     if (!(err = need_d("timeStep", c.timeStep)).empty()) return err;
     if (!(err = need_d("timeRate", c.timeRate)).empty()) return err;
+    // a step that does not advance time would make the time loop
+    // (solver.cpp:216, t <= timeEnd; t += timeStep) run forever: refused
+    if (!(c.timeStep > 0) || !std::isfinite(c.timeStep))
+        return "configuration key 'timeStep' must be a positive number";
     c.elementType = cm["elementType"];
     c.timeIntMethod = cm["timeIntMethod"];
     c.saveFile = cm["saveFile"];

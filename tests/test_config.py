@@ -80,3 +80,13 @@ def test_unknown_boundary_names_are_skipped(tmp_path):
     p.write_text(CONF.replace("Absorbing = Absorbing\n", ""))
     c = D.Config.parse(p, mesh())
     assert len(c.bcs) == 1 and c.bcs[0][1] is True
+
+
+@pytest.mark.parametrize("step", ["0", "-1e-5", "nan", "inf"])
+def test_time_step_must_advance_time(tmp_path, step):
+    # the reference's loop (solver.cpp:216) would never end: refused instead
+    p = tmp_path / "c.conf"
+    p.write_text(CONF.replace("timeStep=1e-5\n", f"timeStep={step}\n"))
+    with pytest.raises(D.DGError) as e:
+        D.Config.parse(p, mesh())
+    assert "timeStep" in str(e.value)
