@@ -3,6 +3,8 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <memory>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -24,6 +26,20 @@ int fail(int code, const std::string &msg) {
 }  // namespace dg
 
 using namespace dg;
+
+namespace {
+// Runs an entry point's body so that no exception crosses the C ABI.
+template <typename F>
+int guarded(F &&body) {
+    try {
+        return body();
+    } catch (const std::bad_alloc &) {
+        return fail(DG_ERR_NOMEM, "out of host memory");
+    } catch (const std::exception &e) {
+        return fail(DG_ERR_ARG, e.what());
+    }
+}
+}  // namespace
 
 struct dgm_mesh {
     RawMesh m;
@@ -58,12 +74,14 @@ const char *dg_last_error(void) { return g_last_error.c_str(); }
 
 int dgm_read_msh(const char *path, dgm_mesh **out) {
     if (!path || !out) return fail(DG_ERR_ARG, "null argument");
-    auto *h = new dgm_mesh();
-    std::string err = read_msh(path, h->m);
-    if (!err.empty()) { delete h; return fail(DG_ERR_IO, err); }
-    h->flatten();
-    *out = h;
-    return DG_OK;
+    return guarded([&]() {
+        std::unique_ptr<dgm_mesh> h(new dgm_mesh());
+        std::string err = read_msh(path, h->m);
+        if (!err.empty()) return fail(DG_ERR_IO, err);
+        h->flatten();
+        *out = h.release();
+        return DG_OK;
+    });
 }
 
 int dgm_write_msh(const dgm_mesh *m, const char *path) {
@@ -81,26 +99,31 @@ static std::vector<std::string> names(const char *const *n, int cnt) {
 int dgm_box_tri(int nx, int ny, const double lo[2], const double hi[2], int order, const char *const side_names[4],
                 dgm_mesh **out) {
     if (!lo || !hi || !out) return fail(DG_ERR_ARG, "null argument");
-    auto *h = new dgm_mesh();
-    std::string err = box_tri(nx, ny, lo, hi, order, names(side_names, 4), h->m);
-    if (!err.empty()) { delete h; return fail(DG_ERR_ARG, err); }
-    h->flatten();
-    *out = h;
-    return DG_OK;
+    return guarded([&]() {
+        std::unique_ptr<dgm_mesh> h(new dgm_mesh());
+        std::string err = box_tri(nx, ny, lo, hi, order, names(side_names, 4), h->m);
+        if (!err.empty()) return fail(DG_ERR_ARG, err);
+        h->flatten();
+        *out = h.release();
+        return DG_OK;
+    });
 }
 
 int dgm_box_tet(int nx, int ny, int nz, const double lo[3], const double hi[3], int order,
                 const char *const side_names[6], const int *removed, int nremoved, const char *obstacle_name,
                 dgm_mesh **out) {
     if (!lo || !hi || !out) return fail(DG_ERR_ARG, "null argument");
-    auto *h = new dgm_mesh();
-    std::vector<int> rem(removed, removed + (removed ? nremoved : 0));
-    std::string err = box_tet(nx, ny, nz, lo, hi, order, names(side_names, 6), rem,
-                              obstacle_name ? obstacle_name : "", h->m);
-    if (!err.empty()) { delete h; return fail(DG_ERR_ARG, err); }
-    h->flatten();
-    *out = h;
-    return DG_OK;
+    if (removed && nremoved < 0) return fail(DG_ERR_ARG, "negative count of removed cells");
+    return guarded([&]() {
+        std::unique_ptr<dgm_mesh> h(new dgm_mesh());
+        std::vector<int> rem(removed, removed + (removed ? nremoved : 0));
+        std::string err = box_tet(nx, ny, nz, lo, hi, order, names(side_names, 6), rem,
+                                  obstacle_name ? obstacle_name : "", h->m);
+        if (!err.empty()) return fail(DG_ERR_ARG, err);
+        h->flatten();
+        *out = h.release();
+        return DG_OK;
+    });
 }
 
 int dgm_get_raw(const dgm_mesh *h, dgm_raw *o) {
@@ -215,14 +238,16 @@ int dgm_source_dofs(const dgm_precomp *h, double x, double y, double z, double s
 
 int dgm_parse_config(const char *path, const dgm_mesh *m, dgm_config **out) {
     if (!path || !m || !out) return fail(DG_ERR_ARG, "null argument");
-    auto *h = new dgm_config();
-    std::string err = parse_config(path, m->m, h->c);
-    if (!err.empty()) { delete h; return fail(DG_ERR_CONFIG, err); }
-    for (auto &s : h->c.sources) h->src.insert(h->src.end(), s.begin(), s.end());
-    for (auto &s : h->c.initConditions) h->ic.insert(h->ic.end(), s.begin(), s.end());
-    for (auto &kv : h->c.physBCs) { h->bc_tag.push_back(kv.first); h->bc_refl.push_back(kv.second ? 1 : 0); }
-    *out = h;
-    return DG_OK;
+    return guarded([&]() {
+        std::unique_ptr<dgm_config> h(new dgm_config());
+        std::string err = parse_config(path, m->m, h->c);
+        if (!err.empty()) return fail(DG_ERR_CONFIG, err);
+        for (auto &s : h->c.sources) h->src.insert(h->src.end(), s.begin(), s.end());
+        for (auto &s : h->c.initConditions) h->ic.insert(h->ic.end(), s.begin(), s.end());
+        for (auto &kv : h->c.physBCs) { h->bc_tag.push_back(kv.first); h->bc_refl.push_back(kv.second ? 1 : 0); }
+        *out = h.release();
+        return DG_OK;
+    });
 }
 
 int dgm_get_config(const dgm_config *h, dgm_config_view *v) {

@@ -694,6 +694,8 @@ std::string finish(LatticeBuilder &lb, const double *lo, const double *hi, long 
 std::string box_tri(int nx, int ny, const double lo[2], const double hi[2], int order,
                     const std::vector<std::string> &side_names, RawMesh &out) {
     if (nx < 1 || ny < 1 || order < 1 || order > 5) return "bad box parameters";
+    // element nodes are indexed with 32-bit integers
+    if ((long long)nx * ny * 2 * ((order + 1) * (order + 2) / 2) > INT32_MAX) return "box too large";
     LatticeBuilder lb(2, order, nx, ny, 1);
     lb.el_lat.reserve((size_t)nx * ny * 2 * lb.np);
     for (long j = 0; j < ny; ++j)
@@ -710,6 +712,8 @@ std::string box_tet(int nx, int ny, int nz, const double lo[3], const double hi[
                     const std::vector<std::string> &side_names, const std::vector<int> &removed,
                     const std::string &obstacle_name, RawMesh &out) {
     if (nx < 1 || ny < 1 || nz < 1 || order < 1 || order > 5) return "bad box parameters";
+    // element nodes are indexed with 32-bit integers
+    if ((long long)nx * ny * nz * 6 * ((order + 1) * (order + 2) * (order + 3) / 6) > INT32_MAX) return "box too large";
     std::vector<char> gone((size_t)nx * ny * nz, 0);
     for (int c : removed)
         if (c >= 0 && (size_t)c < gone.size()) gone[c] = 1;

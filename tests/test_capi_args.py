@@ -134,3 +134,17 @@ def test_last_error_is_per_thread():
     (c2, m2), = got["empty"]
     assert c1 == DG_ERR_UNSUPPORTED and "order" in m1
     assert c2 == DG_ERR_MESH and "empty" in m2
+
+
+def test_mesh_generators_refuse_oversized_and_negative_inputs():
+    with pytest.raises(D.DGError, match="too large"):
+        D.Mesh.box_tri(100000, 100000, order=5)
+    with pytest.raises(D.DGError, match="too large"):
+        D.Mesh.box_tet(2000, 2000, 2000, order=3)
+    with pytest.raises(D.DGError):
+        D.Mesh.box_tri(0, 3, order=2)
+    lo, hi = (C.c_double * 3)(0, 0, 0), (C.c_double * 3)(1, 1, 1)
+    removed = (C.c_int * 1)(0)
+    h = C.c_void_p()
+    code = D.lib().dgm_box_tet(2, 2, 2, lo, hi, 2, None, removed, -5, None, C.byref(h))
+    assert code == DG_ERR_ARG and not h.value
