@@ -27,20 +27,6 @@ int fail(int code, const std::string &msg) {
 
 using namespace dg;
 
-namespace {
-// Runs an entry point's body so that no exception crosses the C ABI.
-template <typename F>
-int guarded(F &&body) {
-    try {
-        return body();
-    } catch (const std::bad_alloc &) {
-        return fail(DG_ERR_NOMEM, "out of host memory");
-    } catch (const std::exception &e) {
-        return fail(DG_ERR_ARG, e.what());
-    }
-}
-}  // namespace
-
 struct dgm_mesh {
     RawMesh m;
     // flattened views

@@ -844,7 +844,7 @@ int coarse_apply(dg_learned *L, double *u) {
 
 extern "C" {
 
-int dg_learned_create(const dg_mesh_desc *mesh, const dg_phys_desc *phys, int flux_sign, int width,
+static int dg_learned_create_impl(const dg_mesh_desc *mesh, const dg_phys_desc *phys, int flux_sign, int width,
                       int hidden_layers, int coarse_steps, double dt, unsigned seed, int device, dg_learned **out) {
     if (!mesh || !phys || !out || coarse_steps < 1 || !(dt > 0)) return fail(DG_ERR_ARG, "bad arguments");
     *out = nullptr;
@@ -904,6 +904,11 @@ int dg_learned_create(const dg_mesh_desc *mesh, const dg_phys_desc *phys, int fl
     if (rc != DG_OK) return bail(rc);
     *out = L;
     return DG_OK;
+}
+
+int dg_learned_create(const dg_mesh_desc *mesh, const dg_phys_desc *phys, int flux_sign, int width,
+                      int hidden_layers, int coarse_steps, double dt, unsigned seed, int device, dg_learned **out) {
+    return dg::guarded([&]() { return dg_learned_create_impl(mesh, phys, flux_sign, width, hidden_layers, coarse_steps, dt, seed, device, out); });
 }
 
 void dg_learned_destroy(dg_learned *L) {

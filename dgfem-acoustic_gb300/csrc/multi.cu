@@ -510,7 +510,7 @@ int enqueue_multi(dg_multi *c, double *t, const double *dt, int nsteps) {
 
 extern "C" {
 
-int dg_multi_create(int nmesh, const dg_mesh_desc *meshes, const dg_phys_desc *phys, const dg_opts *opts_in,
+static int dg_multi_create_impl(int nmesh, const dg_mesh_desc *meshes, const dg_phys_desc *phys, const dg_opts *opts_in,
                     dg_multi **out) {
     if (!out || nmesh < 1 || !meshes || !phys) return fail(DG_ERR_ARG, "null argument or empty batch");
     *out = nullptr;
@@ -619,6 +619,11 @@ int dg_multi_create(int nmesh, const dg_mesh_desc *meshes, const dg_phys_desc *p
     return DG_OK;
 }
 
+int dg_multi_create(int nmesh, const dg_mesh_desc *meshes, const dg_phys_desc *phys, const dg_opts *opts_in,
+                    dg_multi **out) {
+    return dg::guarded([&]() { return dg_multi_create_impl(nmesh, meshes, phys, opts_in, out); });
+}
+
 void dg_multi_destroy(dg_multi *c) { free_multi(c); }
 
 int dg_multi_set_state(dg_multi *c, int mesh, const double *const u[4]) {
@@ -660,7 +665,7 @@ int dg_multi_get_state(dg_multi *c, int mesh, double *const u[4]) {
     return DG_OK;
 }
 
-int dg_multi_set_sources(dg_multi *c, int nsrc, const int *mesh, const int *offsets, const int *dof_idx,
+static int dg_multi_set_sources_impl(dg_multi *c, int nsrc, const int *mesh, const int *offsets, const int *dof_idx,
                          const double *weights, const double *params) {
     if (!c || nsrc < 0 || (nsrc > 0 && (!mesh || !offsets || !params))) return fail(DG_ERR_ARG, "bad source arguments");
     CK(cudaSetDevice(c->device));
@@ -717,6 +722,11 @@ int dg_multi_set_sources(dg_multi *c, int nsrc, const int *mesh, const int *offs
     CK(cudaMemcpy(c->d_src_w, w.data(), w.size() * 8, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->d_src_params, params, (size_t)nsrc * 32, cudaMemcpyHostToDevice));
     return DG_OK;
+}
+
+int dg_multi_set_sources(dg_multi *c, int nsrc, const int *mesh, const int *offsets, const int *dof_idx,
+                         const double *weights, const double *params) {
+    return dg::guarded([&]() { return dg_multi_set_sources_impl(c, nsrc, mesh, offsets, dof_idx, weights, params); });
 }
 
 int dg_multi_rk4_steps(dg_multi *c, double *t, const double *dt, int nsteps) {

@@ -368,7 +368,7 @@ int dg_create(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts
     return dg_create_batch(m, ph, opts_in, 1, out);
 }
 
-int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts_in, int nbatch,
+static int dg_create_batch_impl(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts_in, int nbatch,
                     dg_ctx **out) {
     if (!m || !ph || !out) return fail(DG_ERR_ARG, "null argument");
     if (nbatch < 1 || nbatch > 65535) return fail(DG_ERR_ARG, "batch size must be in 1..65535");
@@ -621,6 +621,11 @@ int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts
     return DG_OK;
 }
 
+int dg_create_batch(const dg_mesh_desc *m, const dg_phys_desc *ph, const dg_opts *opts_in, int nbatch,
+                    dg_ctx **out) {
+    return dg::guarded([&]() { return dg_create_batch_impl(m, ph, opts_in, nbatch, out); });
+}
+
 void dg_destroy(dg_ctx *c) { free_ctx(c); }
 
 }  // extern "C"
@@ -764,7 +769,7 @@ int dg_set_state_member(dg_ctx *c, int member, const double *const u[4]) { retur
 
 int dg_get_state_member(dg_ctx *c, int member, double *const u[4]) { return get_member(c, member, u); }
 
-int dg_set_sources(dg_ctx *c, int nsrc, const int *offsets, const int *dof_idx, const double *params) {
+static int dg_set_sources_impl(dg_ctx *c, int nsrc, const int *offsets, const int *dof_idx, const double *params) {
     if (!c || nsrc < 0 || (nsrc > 0 && (!offsets || !params))) return fail(DG_ERR_ARG, "bad source arguments");
     std::vector<long long> at;
     std::vector<int> src;
@@ -783,7 +788,11 @@ int dg_set_sources(dg_ctx *c, int nsrc, const int *offsets, const int *dof_idx, 
     return upload_sources(c, nsrc, params, at, src, w);
 }
 
-int dg_set_batch_sources(dg_ctx *c, int nsrc, const int *member, const int *offsets, const int *dof_idx,
+int dg_set_sources(dg_ctx *c, int nsrc, const int *offsets, const int *dof_idx, const double *params) {
+    return dg::guarded([&]() { return dg_set_sources_impl(c, nsrc, offsets, dof_idx, params); });
+}
+
+static int dg_set_batch_sources_impl(dg_ctx *c, int nsrc, const int *member, const int *offsets, const int *dof_idx,
                          const double *weights, const double *params) {
     if (!c || nsrc < 0 || (nsrc > 0 && (!member || !offsets || !params)))
         return fail(DG_ERR_ARG, "bad source arguments");
@@ -802,6 +811,11 @@ int dg_set_batch_sources(dg_ctx *c, int nsrc, const int *member, const int *offs
         }
     }
     return upload_sources(c, nsrc, params, at, src, w);
+}
+
+int dg_set_batch_sources(dg_ctx *c, int nsrc, const int *member, const int *offsets, const int *dof_idx,
+                         const double *weights, const double *params) {
+    return dg::guarded([&]() { return dg_set_batch_sources_impl(c, nsrc, member, offsets, dof_idx, weights, params); });
 }
 
 int dg_set_receivers(dg_ctx *c, int nrec, const int *dof_idx, int max_steps) {
