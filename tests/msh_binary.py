@@ -188,3 +188,21 @@ def with_parametric_nodes(m: dict) -> dict:
     m["nodes"] = [(ed, et, 1, tg, [list(x) + [0.125 * (k + 1) for k in range(ed)] for x in xyz])
                   for ed, et, par, tg, xyz in m["nodes"]]
     return m
+
+
+def write_msh22_ascii(m: dict, path: str | Path) -> None:
+    """MSH 2.2 ASCII: "tag x y z" node lines and "tag type 2 physical
+    elementary nodes..." element lines."""
+    ent_phys = {(d, tag): (ph[0] if ph else 0) for d, tag, _, ph, _ in m["ents"]}
+    out = ["$MeshFormat", "2.2 0 8", "$EndMeshFormat"]
+    txt = _phys_section(m).decode()
+    if txt:
+        out += txt.strip("\n").split("\n")
+    nodes = [(t, x) for b in m["nodes"] for t, x in zip(b[3], b[4])]
+    out += ["$Nodes", str(len(nodes))] + [f"{t} " + " ".join(_fmt(c) for c in x[:3]) for t, x in nodes]
+    out.append("$EndNodes")
+    els = [(e, typ, ent_phys[(ed, et)], et) for ed, et, typ, es in m["elements"] for e in es]
+    out += ["$Elements", str(len(els))]
+    out += [f"{e[0]} {typ} 2 {ph} {et} " + " ".join(map(str, e[1:])) for e, typ, ph, et in els]
+    out.append("$EndElements")
+    Path(path).write_text("\n".join(out) + "\n")

@@ -234,3 +234,14 @@ def test_msh4_encodings_and_parametric_nodes(tmp_path, fmt, parametric):
     dst = tmp_path / "other.msh"
     {"40-ascii": write_msh40_ascii, "41-ascii": write_msh41_ascii, "41-binary": write_msh41_binary}[fmt](parsed, dst)
     _same_mesh(D.Mesh.read_msh(src), D.Mesh.read_msh(dst))
+
+
+def test_msh22_ascii_encoding_reads_like_41(tmp_path):
+    from msh_binary import parse_msh41, write_msh22_ascii
+
+    m = D.Mesh.box_tet(2, 1, 2, order=2, side_names=("Absorbing", "Reflecting") * 3)
+    src = tmp_path / "ascii.msh"
+    m.write_msh(src)
+    dst = tmp_path / "v22.msh"
+    write_msh22_ascii(parse_msh41(src), dst)
+    _same_mesh(D.Mesh.read_msh(src), D.Mesh.read_msh(dst))

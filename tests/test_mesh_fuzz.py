@@ -1,7 +1,7 @@
 """Malformed .msh files fail with an error, never a crash: specific cases
 (tags, group dimensions, quotes, counts, block dimensions) and a seeded
-fuzz of truncated and byte-corrupted ASCII 4.1, binary 4.1 and binary 2.2
-files, run in a child process so that a crash fails the test instead of
+fuzz of truncated and byte-corrupted ASCII 4.1, 4.0 (parametric) and 2.2
+and binary 4.1 and 2.2 files, run in a child process so that a crash fails the test instead of
 ending the session."""
 from __future__ import annotations
 
@@ -83,16 +83,19 @@ FUZZ = textwrap.dedent("""
     import os, random, sys
     sys.path.insert(0, {pkg!r}); sys.path.insert(0, {tests!r})
     import dgcuda as D
-    from msh_binary import parse_msh41, write_msh22_binary, write_msh41_binary
+    from msh_binary import (parse_msh41, with_parametric_nodes, write_msh22_ascii, write_msh22_binary,
+                            write_msh40_ascii, write_msh41_binary)
     d = {tmp!r}
     m = D.Mesh.box_tet(2, 1, 1, order=2, side_names=("Absorbing", "Reflecting") * 3)
     src = os.path.join(d, "a.msh"); m.write_msh(src)
     p = parse_msh41(src)
     b41 = os.path.join(d, "b41.msh"); write_msh41_binary(p, b41)
     b22 = os.path.join(d, "b22.msh"); write_msh22_binary(p, b22)
+    a40 = os.path.join(d, "a40.msh"); write_msh40_ascii(with_parametric_nodes(p), a40)
+    a22 = os.path.join(d, "a22.msh"); write_msh22_ascii(p, a22)
     rng = random.Random(2026)
     counts = [0, 0]
-    for path in (src, b41, b22):
+    for path in (src, b41, b22, a40, a22):
         data = open(path, "rb").read()
         cases = [data[:k] for k in range(0, len(data), max(1, len(data) // 60))]
         for _ in range(140):
