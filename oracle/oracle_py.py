@@ -130,6 +130,8 @@ class Oracle:
 
     def set_state(self, u: np.ndarray) -> None:
         u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        if u.size != 4 * self.ndof:
+            raise ValueError(f"state must hold 4 x {self.ndof} values, got {u.size}")
         lib().oracle_set_state(self._h, u.ctypes.data_as(P_d))
 
     def get_state(self) -> np.ndarray:
@@ -155,6 +157,8 @@ class Oracle:
 
     def rhs(self, u: np.ndarray) -> np.ndarray:
         u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        if u.size != 4 * self.ndof:
+            raise ValueError(f"state must hold 4 x {self.ndof} values, got {u.size}")
         out = np.empty_like(u)
         lib().oracle_rhs(self._h, u.ctypes.data_as(P_d), out.ctypes.data_as(P_d))
         return out.reshape(4, self.ndof)
