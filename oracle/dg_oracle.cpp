@@ -135,24 +135,36 @@ void cross(const double *A, const double *B, double *O) {
 // gmsh restatement: reference elements, Lagrange bases, rules
 // ---------------------------------------------------------------------------
 typedef std::array<double, 3> P3;
+// The reference-element lattice and the Lagrange basis are built in long
+// double (x86-64: 64-bit significand; aarch64: IEEE binary128) and rounded to
+// double once.  gmsh's monomial Vandermonde at equispaced nodes is badly
+// conditioned at orders 4-5 (3D order 5: 56 x 56), so a double inverse and a
+// double evaluation of sum_m c_m x^m lose several digits in cancellation;
+// extended precision keeps the basis values and gradients at the rule points
+// correct to double rounding, with the same monomial representation.
+typedef long double LD;
+typedef std::array<LD, 3> PL;
 
 // Nodes of the order-p element on the given vertices (reference coordinates),
 // gmsh order: vertices, edges (in edge direction), faces, interior.
-static void push_edge(std::vector<P3> &out, const P3 &a, const P3 &b, int p) {
+template <class PT>
+static void push_edge(std::vector<PT> &out, const PT &a, const PT &b, int p) {
     for (int k = 1; k < p; ++k) {
-        double t = double(k) / p;
+        typename PT::value_type t = typename PT::value_type(k) / p;
         out.push_back({a[0] + t * (b[0] - a[0]), a[1] + t * (b[1] - a[1]), a[2] + t * (b[2] - a[2])});
     }
 }
-static P3 shrink(const P3 *v, int nv, int which, int p) {
+template <class PT>
+static PT shrink(const PT *v, int nv, int which, int p) {
     // vertex of the inner simplex: v_w + sum_{o != w} (v_o - v_w)/p
-    P3 r = v[which];
+    PT r = v[which];
     for (int o = 0; o < nv; ++o)
         if (o != which)
             for (int k = 0; k < 3; ++k) r[k] += (v[o][k] - v[which][k]) / p;
     return r;
 }
-static void tri_points(std::vector<P3> &out, P3 a, P3 b, P3 c, int p) {
+template <class PT>
+static void tri_points(std::vector<PT> &out, PT a, PT b, PT c, int p) {
     while (true) {
         if (p == 0) {
             out.push_back(a);
@@ -165,8 +177,8 @@ static void tri_points(std::vector<P3> &out, P3 a, P3 b, P3 c, int p) {
         push_edge(out, b, c, p);
         push_edge(out, c, a, p);
         if (p < 3) return;
-        P3 v[3] = {a, b, c};
-        P3 na = shrink(v, 3, 0, p), nb = shrink(v, 3, 1, p), nc = shrink(v, 3, 2, p);
+        PT v[3] = {a, b, c};
+        PT na = shrink(v, 3, 0, p), nb = shrink(v, 3, 1, p), nc = shrink(v, 3, 2, p);
         a = na; b = nb; c = nc;
         p -= 3;
     }
@@ -174,9 +186,10 @@ static void tri_points(std::vector<P3> &out, P3 a, P3 b, P3 c, int p) {
 static const int kTetEdge[6][2] = {{0, 1}, {1, 2}, {2, 0}, {3, 0}, {3, 2}, {3, 1}};
 static const int kTetFace[4][3] = {{0, 2, 1}, {0, 1, 3}, {0, 3, 2}, {3, 1, 2}};
 static const int kTriEdge[3][2] = {{0, 1}, {1, 2}, {2, 0}};
-static void tet_points(std::vector<P3> &out, P3 v0, P3 v1, P3 v2, P3 v3, int p) {
+template <class PT>
+static void tet_points(std::vector<PT> &out, PT v0, PT v1, PT v2, PT v3, int p) {
     while (true) {
-        P3 v[4] = {v0, v1, v2, v3};
+        PT v[4] = {v0, v1, v2, v3};
         if (p == 0) {
             out.push_back(v0);
             return;
@@ -185,69 +198,110 @@ static void tet_points(std::vector<P3> &out, P3 v0, P3 v1, P3 v2, P3 v3, int p) 
         for (auto &e : kTetEdge) push_edge(out, v[e[0]], v[e[1]], p);
         if (p >= 3)
             for (auto &f : kTetFace) {
-                P3 fv[3] = {v[f[0]], v[f[1]], v[f[2]]};
+                PT fv[3] = {v[f[0]], v[f[1]], v[f[2]]};
                 tri_points(out, shrink(fv, 3, 0, p), shrink(fv, 3, 1, p), shrink(fv, 3, 2, p), p - 3);
             }
         if (p < 4) return;
-        P3 n0 = shrink(v, 4, 0, p), n1 = shrink(v, 4, 1, p), n2 = shrink(v, 4, 2, p), n3 = shrink(v, 4, 3, p);
+        PT n0 = shrink(v, 4, 0, p), n1 = shrink(v, 4, 1, p), n2 = shrink(v, 4, 2, p), n3 = shrink(v, 4, 3, p);
         v0 = n0; v1 = n1; v2 = n2; v3 = n3;
         p -= 4;
     }
 }
 
+// In-place inverse (partial-pivot Gauss-Jordan) of a column-major n x n
+// long double matrix; the Vandermonde of distinct lattice nodes is regular.
+static void inverse_ld(std::vector<LD> &a, int n) {
+    std::vector<LD> inv(n * n, 0.0L);
+    for (int i = 0; i < n; ++i) inv[i * n + i] = 1.0L;
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        for (int r = k + 1; r < n; ++r)
+            if (std::fabs(a[k * n + r]) > std::fabs(a[k * n + p])) p = r;
+        if (p != k)
+            for (int c = 0; c < n; ++c) {
+                std::swap(a[c * n + k], a[c * n + p]);
+                std::swap(inv[c * n + k], inv[c * n + p]);
+            }
+        LD d = a[k * n + k];
+        for (int c = 0; c < n; ++c) {
+            a[c * n + k] /= d;
+            inv[c * n + k] /= d;
+        }
+        for (int r = 0; r < n; ++r) {
+            if (r == k) continue;
+            LD l = a[k * n + r];
+            if (l == 0.0L) continue;
+            for (int c = 0; c < n; ++c) {
+                a[c * n + r] -= l * a[c * n + k];
+                inv[c * n + r] -= l * inv[c * n + k];
+            }
+        }
+    }
+    a.swap(inv);
+}
+
 struct Basis {
     int dim = 0, order = 0, n = 0;
-    std::vector<P3> nodes;                 // reference coordinates
+    std::vector<P3> nodes;                 // reference coordinates (rounded)
     std::vector<std::array<int, 3>> mono;  // exponents
-    std::vector<double> coef;              // [m][k]: phi_k = sum_m coef[m][k] mono_m
+    std::vector<LD> coef;                  // [m][k]: phi_k = sum_m coef[m][k] mono_m
     void build(int d, int p) {
         dim = d;
         order = p;
-        nodes.clear();
+        std::vector<PL> ln;
         if (d == 1) {
-            nodes.push_back({-1, 0, 0});
-            nodes.push_back({1, 0, 0});
-            push_edge(nodes, {-1, 0, 0}, {1, 0, 0}, p);
+            ln.push_back({-1, 0, 0});
+            ln.push_back({1, 0, 0});
+            push_edge(ln, PL{-1, 0, 0}, PL{1, 0, 0}, p);
         } else if (d == 2) {
-            tri_points(nodes, {0, 0, 0}, {1, 0, 0}, {0, 1, 0}, p);
+            tri_points(ln, PL{0, 0, 0}, PL{1, 0, 0}, PL{0, 1, 0}, p);
         } else {
-            tet_points(nodes, {0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, p);
+            tet_points(ln, PL{0, 0, 0}, PL{1, 0, 0}, PL{0, 1, 0}, PL{0, 0, 1}, p);
         }
-        n = (int)nodes.size();
+        n = (int)ln.size();
+        nodes.resize(n);
+        for (int i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k) nodes[i][k] = (double)ln[i][k];
         mono.clear();
         for (int a = 0; a <= p; ++a)
             for (int b = 0; b <= (d >= 2 ? p - a : 0); ++b)
                 for (int c = 0; c <= (d == 3 ? p - a - b : 0); ++c) mono.push_back({a, b, c});
-        std::vector<double> V(n * n);  // column-major V(i,m) = mono_m(x_i)
+        std::vector<LD> V(n * n);  // column-major V(i,m) = mono_m(x_i)
         for (int i = 0; i < n; ++i)
-            for (int m = 0; m < n; ++m) V[m * n + i] = mono_val(m, nodes[i].data());
-        la::inverse(V.data(), n);  // V^-1 column-major: Vi(m,k) at [k*n + m]
-        coef.assign(n * n, 0.0);
+            for (int m = 0; m < n; ++m) V[m * n + i] = mono_val(m, ln[i].data());
+        inverse_ld(V, n);  // V^-1 column-major: Vi(m,k) at [k*n + m]
+        coef.assign(n * n, 0.0L);
         for (int m = 0; m < n; ++m)
             for (int k = 0; k < n; ++k) coef[m * n + k] = V[k * n + m];
     }
-    double mono_val(int m, const double *x) const {
-        return std::pow(x[0], mono[m][0]) * std::pow(x[1], mono[m][1]) * std::pow(x[2], mono[m][2]);
+    static LD ipow(LD x, int e) {
+        LD r = 1.0L;
+        for (int i = 0; i < e; ++i) r *= x;
+        return r;
     }
-    double mono_der(int m, int dir, const double *x) const {
+    LD mono_val(int m, const LD *x) const {
+        return ipow(x[0], mono[m][0]) * ipow(x[1], mono[m][1]) * ipow(x[2], mono[m][2]);
+    }
+    LD mono_der(int m, int dir, const LD *x) const {
         int e = mono[m][dir];
-        if (e == 0) return 0.0;
-        double v = e;
-        for (int k = 0; k < 3; ++k) v *= std::pow(x[k], k == dir ? e - 1 : mono[m][k]);
+        if (e == 0) return 0.0L;
+        LD v = e;
+        for (int k = 0; k < 3; ++k) v *= ipow(x[k], k == dir ? e - 1 : mono[m][k]);
         return v;
     }
-    void eval(const double *x, double *phi, double *grad /*[n][3]*/) const {
+    void eval(const double *xd, double *phi, double *grad /*[n][3]*/) const {
+        const LD x[3] = {xd[0], xd[1], xd[2]};
         for (int k = 0; k < n; ++k) {
-            double v = 0, g[3] = {0, 0, 0};
+            LD v = 0, g[3] = {0, 0, 0};
             for (int m = 0; m < n; ++m) {
-                double c = coef[m * n + k];
-                if (c == 0.0) continue;
+                LD c = coef[m * n + k];
+                if (c == 0.0L) continue;
                 v += c * mono_val(m, x);
                 for (int dd = 0; dd < dim; ++dd) g[dd] += c * mono_der(m, dd, x);
             }
-            if (phi) phi[k] = v;
+            if (phi) phi[k] = (double)v;
             if (grad)
-                for (int dd = 0; dd < 3; ++dd) grad[k * 3 + dd] = g[dd];
+                for (int dd = 0; dd < 3; ++dd) grad[k * 3 + dd] = (double)g[dd];
         }
     }
 };
@@ -988,6 +1042,54 @@ void *oracle_create(const oracle_input *in, char *err, int errlen) {
 }
 
 void oracle_destroy(void *p) { delete (Handle *)p; }
+
+// Reference-element data as the oracle builds it for elements of the given
+// dimension (1-3) and order: its node lattice (gmsh order), its Gauss(2p)
+// rule, and the matrices that rule gives with its Lagrange basis
+//   mass[i*n + j]          = sum_g w_g phi_i(g) phi_j(g)
+//   stiff[(u*n + i)*n + j] = sum_g w_g dphi_i/du(g) phi_j(g)   (u < dim)
+// and the basis at the rule points, phi[g*n + i] and grad[(g*n + i)*3 + u].
+// Any output pointer may be null.  Returns n (nodes), *ng the rule's point
+// count, or -1 when no rule exists.  Used by the tests that pin the
+// restated basis and rules against exact rational integrals.
+int oracle_reference_element(int dim, int order, double *nodes, double *mass, double *stiff, int *ng,
+                             double *rule, double *phi_out, double *grad_out) {
+    if (dim < 1 || dim > 3 || order < 1 || order > 5) return -1;
+    try {
+        Basis b;
+        b.build(dim, order);
+        Rule r = get_rule(dim, 2 * order);
+        int n = b.n;
+        if (ng) *ng = r.n;
+        if (rule) std::copy(r.uvwq.begin(), r.uvwq.end(), rule);
+        if (nodes)
+            for (int i = 0; i < n; ++i)
+                for (int k = 0; k < 3; ++k) nodes[i * 3 + k] = b.nodes[i][k];
+        std::vector<double> phi((size_t)r.n * n), grad((size_t)r.n * n * 3);
+        for (int g = 0; g < r.n; ++g) b.eval(&r.uvwq[g * 4], &phi[(size_t)g * n], &grad[(size_t)g * n * 3]);
+        if (phi_out) std::copy(phi.begin(), phi.end(), phi_out);
+        if (grad_out) std::copy(grad.begin(), grad.end(), grad_out);
+        if (mass)
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) {
+                    double s = 0;
+                    for (int g = 0; g < r.n; ++g) s += r.uvwq[g * 4 + 3] * phi[g * n + i] * phi[g * n + j];
+                    mass[i * n + j] = s;
+                }
+        if (stiff)
+            for (int u = 0; u < dim; ++u)
+                for (int i = 0; i < n; ++i)
+                    for (int j = 0; j < n; ++j) {
+                        double s = 0;
+                        for (int g = 0; g < r.n; ++g)
+                            s += r.uvwq[g * 4 + 3] * grad[(g * n + i) * 3 + u] * phi[g * n + j];
+                        stiff[(u * n + i) * n + j] = s;
+                    }
+        return n;
+    } catch (std::exception &) {
+        return -1;
+    }
+}
 
 // 0 = classical RK4 ("Runge-Kutta"), 1 = forward Euler ("Euler1").
 int oracle_set_method(void *p, int method) {

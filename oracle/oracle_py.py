@@ -62,8 +62,28 @@ def lib() -> C.CDLL:
         L.oracle_face_maps.argtypes = [C.c_void_p, P_i, P_i]
         L.oracle_rhs.argtypes = [C.c_void_p, P_d, P_d]
         L.oracle_set_method.argtypes = [C.c_void_p, C.c_int]
+        L.oracle_reference_element.argtypes = [C.c_int, C.c_int, P_d, P_d, P_d, P_i, P_d, P_d, P_d]
         _lib = L
     return _lib
+
+
+def reference_element(dim: int, order: int) -> dict:
+    """The oracle's reference element of the given dimension and order: node
+    lattice [n][3], Gauss(2p) rule [ng][4] (u, v, w, weight), the Lagrange
+    basis and its gradients at the rule points ([ng][n], [ng][n][3]), and
+    the mass and stiffness matrices that rule gives with that basis."""
+    L = lib()
+    ng = C.c_int()
+    n = L.oracle_reference_element(dim, order, None, None, None, C.byref(ng), None, None, None)
+    if n < 0:
+        raise ValueError(f"no reference element for dim {dim}, order {order}")
+    nodes, mass = np.empty((n, 3)), np.empty((n, n))
+    stiff, rule = np.empty((dim, n, n)), np.empty((ng.value, 4))
+    phi, grad = np.empty((ng.value, n)), np.empty((ng.value, n, 3))
+    L.oracle_reference_element(dim, order, nodes.ctypes.data_as(P_d), mass.ctypes.data_as(P_d),
+                               stiff.ctypes.data_as(P_d), C.byref(ng), rule.ctypes.data_as(P_d),
+                               phi.ctypes.data_as(P_d), grad.ctypes.data_as(P_d))
+    return {"nodes": nodes, "mass": mass, "stiff": stiff, "rule": rule, "phi": phi, "grad": grad}
 
 
 def _arr(ptr, n, dtype):

@@ -45,15 +45,15 @@ def _oracle_points(m):
             O._arr(v.f_normals, F * ngf * 3, np.float64).reshape(F, ngf, 3))
 
 
-@pytest.mark.parametrize("dim,order", [(2, 2), (2, 3), (2, 5), (3, 2), (3, 3), (3, 4)])
+@pytest.mark.parametrize("dim,order", [(2, 2), (2, 3), (2, 5), (3, 2), (3, 3), (3, 4), (3, 5)])
 def test_per_point_arrays_match_the_oracle(dim, order):
     m, pre = curved_mesh(D, dim, order)
     assert pre.num_curved == pre.num_el
     ca, ar = pre.curved_arrays(), pre.arrays()
     om, edet, fdet, fnrm = _oracle_points(m)
-    # the oracle's order-5 basis (monomials x inverse Vandermonde) carries
-    # about 1e-12 of rounding; lower orders agree to a few 1e-14
-    tol = 1e-11 if order == 5 else 1e-12
+    # the oracle builds its monomial basis in extended precision, so every
+    # order agrees to a few 1e-14
+    tol = 1e-12
     assert np.abs(ca["el_detj"] - edet).max() <= tol * np.abs(edet).max()
     assert np.abs(ca["f_detj"] - fdet).max() <= tol * np.abs(fdet).max()
     assert np.abs(ca["f_normal"] - fnrm).max() <= tol

@@ -2,8 +2,7 @@
 kernel together with the affine kernels must reproduce the oracle, which
 evaluates every element and face at the points of its Gauss(2p) rule as the
 reference does (Mesh.cpp:31-78, 135-194, 440-557).  FP64 is held to 1e-10
-relative L2 per field (order 5: 1e-9, the conditioning of its operators),
-FP32 to 1e-5."""
+relative L2 per field at every order 2-5, FP32 to 1e-5."""
 from __future__ import annotations
 
 import numpy as np
@@ -61,7 +60,7 @@ def test_fully_curved_mesh_matches_oracle(dim, order):
     info = s.info()
     assert info["curved"] == pre.num_el
     got = s.get_state()
-    tol = 1e-9 if order == 5 else 1e-10
+    tol = 1e-10
     for q in range(dim + 1):
         assert rel(got[q], ref[q]) <= tol, (q, rel(got[q], ref[q]))
 
