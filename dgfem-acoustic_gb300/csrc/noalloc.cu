@@ -9,7 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <mutex>
+#include <cstdint>
 #include <string>
 
 #include "../../include/dgcuda.h"
@@ -25,25 +25,21 @@ constexpr long long kNoAllocMaxValues = 1LL << 20;
 
 static __device__ __align__(256) double g_stage_scratch[3 * kNoAllocMaxValues];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double *g_scratch_addr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device; resolved once
-// per device (the host-side symbol is only a stand-in, never a device
-// address).
-int scratch_address(int dev, double **out) {
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_stage_scratch);
-        if (e != cudaSuccess)
-            return dg::fail(DG_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_scratch_addr[dev] = static_cast<double *>(p);
-    }
-    *out = g_scratch_addr[dev];
+// Device address of the scratch array in the current device's context.  The
+// host-side symbol is only a stand-in, never a device address, so the address
+// is looked up with cudaGetSymbolAddress, on every call: the lookup is cheap,
+// and a context that the application reset (cudaDeviceReset) and recreated
+// gets the array's new address instead of a stale one.
+int scratch_address(double **out) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_stage_scratch);
+    if (e != cudaSuccess)
+        return dg::fail(DG_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    *out = static_cast<double *>(p);
     return DG_OK;
 }
+
+bool aligned(const void *p, uintptr_t n) { return (reinterpret_cast<uintptr_t>(p) % n) == 0; }
 
 }  // namespace
 
@@ -55,6 +51,13 @@ extern "C" int dg_rk4_steps_noalloc(const dg_device_layout *lay, double *u, doub
     if (lay->num_el < 1) return dg::fail(DG_ERR_ARG, "empty mesh");
     if (!lay->geo || !lay->fgeo || !lay->conn || !lay->ops || !lay->tabs)
         return dg::fail(DG_ERR_ARG, "null layout array");
+    // the stage kernels read fgeo as 16-byte double2 vectors, conn as 8-byte
+    // int2 pairs and geo, ops and u as doubles: a misaligned pointer would
+    // fault on the device, so it is refused here, before any launch
+    if (!aligned(lay->fgeo, 16)) return dg::fail(DG_ERR_ARG, "fgeo must be 16-byte aligned");
+    if (!aligned(lay->conn, 8)) return dg::fail(DG_ERR_ARG, "conn must be 8-byte aligned");
+    if (!aligned(lay->geo, 8) || !aligned(lay->ops, 8) || !aligned(u, 8))
+        return dg::fail(DG_ERR_ARG, "geo, ops and u must be 8-byte aligned");
     dgk::KernelSet ks;
     if (!dgk::get_kernels(DG_PREC_FP64, lay->dim, lay->order, &ks))
         return dg::fail(DG_ERR_UNSUPPORTED, "order must be in 1..5");
@@ -69,9 +72,8 @@ extern "C" int dg_rk4_steps_noalloc(const dg_device_layout *lay, double *u, doub
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return dg::fail(DG_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return dg::fail(DG_ERR_UNSUPPORTED, "device ordinal too large");
     double *scratch = nullptr;
-    int rc = scratch_address(dev, &scratch);
+    int rc = scratch_address(&scratch);
     if (rc != DG_OK) return rc;
     for (int s = 0; s < 4; ++s) {
         e = cudaFuncSetAttribute(ks.stage[s], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ks.smem);

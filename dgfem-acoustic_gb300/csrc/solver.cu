@@ -79,14 +79,22 @@ const void *host_device_view(const void *p) {
 }
 const int kHostIoBlocks = 2048;  // grid of the host-link kernels: many loads in flight
 
+// Value i of a state kept in the context's precision, plus its low FP32 part
+// when the state is an FP32 pair (mixed form): the FP64 value the form holds.
+template <typename Real>
+__device__ __forceinline__ double state_value(const Real *q, const float *lo, long long i) {
+    return lo ? double(q[i]) + double(lo[i]) : double(q[i]);
+}
+
 // FP64 monitors: thread per element, u^T M u per field, non-finite count.
 // Curved elements (cslot[e] >= 0) use their own mass matrix, applied as the
-// rule it was summed on: u^T M u = sum_g w detJ(g) u(g)^2.
+// rule it was summed on: u^T M u = sum_g w detJ(g) u(g)^2.  `ulo` (mixed form
+// only, else null) is the low part of the state pair, same layout as u.
 template <typename Real>
-__global__ void monitor_kernel(const Real *u, long long fstride, int K, int np, int nq, const double *mass,
-                               const double *detj, double rho, double c0, double *out /*[2+nq]*/,
-                               unsigned long long *bad, const int *cslot, const double *cwdet, const double *cphi,
-                               int cng) {
+__global__ void monitor_kernel(const Real *u, const float *ulo, long long fstride, int K, int np, int nq,
+                               const double *mass, const double *detj, double rho, double c0,
+                               double *out /*[2+nq]*/, unsigned long long *bad, const int *cslot,
+                               const double *cwdet, const double *cphi, int cng) {
     __shared__ double red[256][5];
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     double loc[5] = {0, 0, 0, 0, 0};
@@ -94,23 +102,25 @@ __global__ void monitor_kernel(const Real *u, long long fstride, int K, int np, 
     if (e < K) {
         const int cs = cslot ? cslot[e] : -1;
         for (int f = 0; f < nq; ++f) {
-            const Real *q = u + f * fstride + (long long)e * np;
+            const long long base = f * fstride + (long long)e * np;
+            const Real *q = u + base;
+            const float *ql = ulo ? ulo + base : nullptr;
             double s = 0;
             for (int i = 0; i < np; ++i)
-                if (!isfinite(double(q[i]))) ++nbad;
+                if (!isfinite(state_value(q, ql, i))) ++nbad;
             if (cs >= 0) {
                 for (int g = 0; g < cng; ++g) {
                     double v = 0;
-                    for (int j = 0; j < np; ++j) v += cphi[g * np + j] * double(q[j]);
+                    for (int j = 0; j < np; ++j) v += cphi[g * np + j] * state_value(q, ql, j);
                     s += cwdet[(long long)cs * cng + g] * v * v;
                 }
                 loc[1 + f] = s;
                 continue;
             }
             for (int i = 0; i < np; ++i) {
-                double qi = double(q[i]);
+                double qi = state_value(q, ql, i);
                 double t = 0;
-                for (int j = 0; j < np; ++j) t += mass[i * np + j] * double(q[j]);
+                for (int j = 0; j < np; ++j) t += mass[i * np + j] * state_value(q, ql, j);
                 s += qi * t;
             }
             loc[1 + f] = s * detj[e];
@@ -129,6 +139,46 @@ __global__ void monitor_kernel(const Real *u, long long fstride, int K, int np, 
     if (threadIdx.x == 0)
         for (int k = 0; k < 1 + nq; ++k) atomicAdd(&out[k], red[0][k]);
     if (nbad) atomicAdd(bad, nbad);
+}
+
+// FP64 error monitor: per field, sum (u - r)^2 and sum r^2 over the nodal
+// values of two states of the same mesh (either precision, FP32 pairs joined),
+// grid-stride, block reduction in shared memory, one atomic per block and
+// quantity.  out[2f] = squared difference, out[2f+1] = squared reference;
+// `bad` counts non-finite values of u.
+template <typename RU, typename RR>
+__global__ void error_kernel(const RU *u, const float *ulo, const RR *r, const float *rlo, long long n, int nq,
+                             double *out /*[8]*/, unsigned long long *bad) {
+    __shared__ double red[8][256];
+    double loc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long nbad = 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (int f = 0; f < nq; ++f)
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const long long k = f * n + i;
+            const double a = state_value(u, ulo, k), b = state_value(r, rlo, k);
+            if (!isfinite(a)) ++nbad;
+            loc[2 * f] += (a - b) * (a - b);
+            loc[2 * f + 1] += b * b;
+        }
+    for (int k = 0; k < 8; ++k) red[k][threadIdx.x] = loc[k];
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int k = 0; k < 8; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 2 * nq; ++k) atomicAdd(&out[k], red[k][0]);
+    if (nbad) atomicAdd(bad, nbad);
+}
+
+template <typename RU, typename RR>
+void launch_error(const void *u, const float *ulo, const void *r, const float *rlo, long long n, int nq,
+                  double *out, unsigned long long *bad, cudaStream_t st) {
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 4 * 152);
+    error_kernel<RU, RR><<<std::max(blocks, 1), 256, 0, st>>>(static_cast<const RU *>(u), ulo,
+                                                             static_cast<const RR *>(r), rlo, n, nq, out, bad);
 }
 
 }  // namespace
@@ -1046,13 +1096,14 @@ int dg_monitors(dg_ctx *c, double *energy, double *l2, long long *status) {
     CK(cudaMemsetAsync(c->d_bad, 0, 8, c->stream));
     int blocks = (c->K + 255) / 256;
     if (c->prec == DG_PREC_FP64)
-        monitor_kernel<double><<<blocks, 256, 0, c->stream>>>((const double *)c->d_u, c->ndof, c->K, c->np, c->nq,
-                                                              c->d_mass, c->d_detj, c->rho0, c->c0, c->d_mon,
+        monitor_kernel<double><<<blocks, 256, 0, c->stream>>>((const double *)c->d_u, nullptr, c->ndof, c->K, c->np,
+                                                              c->nq, c->d_mass, c->d_detj, c->rho0, c->c0, c->d_mon,
                                                               c->d_bad, c->d_cslot, c->d_cwdet, c->d_cphi64, c->cng);
     else
-        monitor_kernel<float><<<blocks, 256, 0, c->stream>>>((const float *)c->d_u, c->ndof, c->K, c->np, c->nq,
-                                                             c->d_mass, c->d_detj, c->rho0, c->c0, c->d_mon,
-                                                             c->d_bad, c->d_cslot, c->d_cwdet, c->d_cphi64, c->cng);
+        monitor_kernel<float><<<blocks, 256, 0, c->stream>>>((const float *)c->d_u, c->mixed ? c->d_ulo : nullptr,
+                                                             c->ndof, c->K, c->np, c->nq, c->d_mass, c->d_detj,
+                                                             c->rho0, c->c0, c->d_mon, c->d_bad, c->d_cslot,
+                                                             c->d_cwdet, c->d_cphi64, c->cng);
     CK(cudaGetLastError());
     double h[8];
     unsigned long long bad = 0;
@@ -1062,6 +1113,42 @@ int dg_monitors(dg_ctx *c, double *energy, double *l2, long long *status) {
     if (energy) *energy = h[0];
     if (l2)
         for (int f = 0; f < 4; ++f) l2[f] = f < c->nq ? std::sqrt(std::max(h[1 + f], 0.0)) : 0.0;
+    if (status) *status = (long long)bad;
+    return bad ? DG_ERR_NONFINITE : DG_OK;
+}
+
+int dg_error_vs(dg_ctx *c, int member, dg_ctx *ref, int ref_member, double *rel_l2, long long *status) {
+    if (!c || !ref || !rel_l2) return fail(DG_ERR_ARG, "null argument");
+    if (member < 0 || member >= c->nbatch || ref_member < 0 || ref_member >= ref->nbatch)
+        return fail(DG_ERR_ARG, "member out of range");
+    if (c->ndof != ref->ndof || c->nq != ref->nq || c->np != ref->np)
+        return fail(DG_ERR_ARG, "the two contexts do not hold states of the same mesh");
+    if (c->device != ref->device) return fail(DG_ERR_ARG, "the two contexts live on different devices");
+    CK(cudaSetDevice(c->device));
+    if (ref != c) CK(cudaStreamSynchronize(ref->stream));
+    CK(cudaMemsetAsync(c->d_mon, 0, 8 * 8, c->stream));
+    CK(cudaMemsetAsync(c->d_bad, 0, 8, c->stream));
+    const long long ou = (long long)member * c->bstride, orf = (long long)ref_member * ref->bstride;
+    const char *u = static_cast<const char *>(c->d_u) + ou * (long long)c->rsize;
+    const char *r = static_cast<const char *>(ref->d_u) + orf * (long long)ref->rsize;
+    const float *ulo = c->mixed ? c->d_ulo + ou : nullptr;
+    const float *rlo = ref->mixed ? ref->d_ulo + orf : nullptr;
+    const bool u64 = c->prec == DG_PREC_FP64, r64 = ref->prec == DG_PREC_FP64;
+    if (u64 && r64) launch_error<double, double>(u, ulo, r, rlo, c->ndof, c->nq, c->d_mon, c->d_bad, c->stream);
+    else if (u64) launch_error<double, float>(u, ulo, r, rlo, c->ndof, c->nq, c->d_mon, c->d_bad, c->stream);
+    else if (r64) launch_error<float, double>(u, ulo, r, rlo, c->ndof, c->nq, c->d_mon, c->d_bad, c->stream);
+    else launch_error<float, float>(u, ulo, r, rlo, c->ndof, c->nq, c->d_mon, c->d_bad, c->stream);
+    CK(cudaGetLastError());
+    double h[8];
+    unsigned long long bad = 0;
+    CK(cudaMemcpyAsync(h, c->d_mon, 8 * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&bad, c->d_bad, 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int f = 0; f < 4; ++f) {
+        if (f >= c->nq) { rel_l2[f] = 0.0; continue; }
+        const double d = std::sqrt(std::max(h[2 * f], 0.0)), n = std::sqrt(std::max(h[2 * f + 1], 0.0));
+        rel_l2[f] = n > 0 ? d / n : d;
+    }
     if (status) *status = (long long)bad;
     return bad ? DG_ERR_NONFINITE : DG_OK;
 }

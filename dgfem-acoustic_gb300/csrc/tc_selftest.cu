@@ -27,9 +27,16 @@ __host__ __device__ inline uint32_t b_offset(int n, int k) {
     return (uint32_t)((k / 16) * 1024 + (n / 8) * 256 + ((k % 16) / 8) * 128 + (n % 8) * 16 + (k % 8) * 2);
 }
 
-__global__ void __launch_bounds__(128, 1) tc_selftest_kernel(float *out, int *err) {
+// mode 0: the GEMM, result in out.  mode 1: the same MMAs are issued and
+// committed, but the kernel first waits, with a 1 ms limit, on a second
+// mbarrier that nothing arrives on; the wait runs out, the kernel records
+// err bit 1, then drains its own MMAs with the normal bounded wait on the
+// commit barrier (err bit 2 if that too ran out) and frees its tensor
+// memory before returning -- the error path of the mixed stage kernel.
+__global__ void __launch_bounds__(128, 1) tc_selftest_kernel(float *out, int *err, int mode) {
     __shared__ __align__(1024) unsigned char sB[kSteps * 1024];
     __shared__ __align__(8) uint64_t bar;
+    __shared__ __align__(8) uint64_t bar_never;
     __shared__ uint32_t tbase;
     const int tid = threadIdx.x, warp = tid >> 5;
     if (warp == 0) {
@@ -38,6 +45,7 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(float *out, int *er
     }
     if (tid == 0) {
         dgtc::mbar_init(&bar, 1);
+        dgtc::mbar_init(&bar_never, 1);
         dgtc::fence_mbar_init();
     }
     for (int idx = tid; idx < kN * kK; idx += blockDim.x) {
@@ -73,6 +81,17 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(float *out, int *er
         dgtc::mma_commit(&bar);
     }
     __syncwarp();
+    if (mode == 1) {
+        const bool got = dgtc::mbar_wait_bounded(&bar_never, 0, 1u << 20, 1000000ull);
+        if (!__any_sync(0xffffffffu, got) && tid == 0) atomicOr(err, 1);
+        // drain the MMAs in flight before the tensor memory is freed
+        const bool drained = __all_sync(0xffffffffu, dgtc::mbar_wait_bounded(&bar, 0, 1u << 22));
+        if (!drained && (tid & 31) == 0) atomicOr(err, 2);
+        dgtc::fence_before_sync();
+        __syncthreads();
+        if (warp == 0) dgtc::tmem_dealloc(base, 256);
+        return;
+    }
     bool ok = dgtc::mbar_wait_bounded(&bar, 0, 1u << 22);
     ok = __all_sync(0xffffffffu, ok);
     if (!ok) {
@@ -111,7 +130,7 @@ extern "C" int dg_tc_selftest(int device, double *max_abs_err) {
     }
     cudaMemset(d_out, 0, kM * 64 * sizeof(float));
     cudaMemset(d_err, 0, sizeof(int));
-    tc_selftest_kernel<<<1, 128>>>(d_out, d_err);
+    tc_selftest_kernel<<<1, 128>>>(d_out, d_err, 0);
     cudaError_t e = cudaDeviceSynchronize();
     std::vector<float> h(kM * 64);
     int herr = 0;
@@ -134,4 +153,26 @@ extern "C" int dg_tc_selftest(int device, double *max_abs_err) {
         }
     *max_abs_err = worst;
     return worst == 0 ? DG_OK : dg::fail(DG_ERR_CUDA, "tensor-core self-test: wrong GEMM result");
+}
+
+extern "C" int dg_tc_wait_selftest(int device, int *flags) {
+    if (!flags) return dg::fail(DG_ERR_ARG, "null argument");
+    if (cudaSetDevice(device) != cudaSuccess) return dg::fail(DG_ERR_CUDA, "cudaSetDevice failed");
+    float *d_out = nullptr;
+    int *d_err = nullptr;
+    if (cudaMalloc(&d_out, kM * 64 * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&d_err, sizeof(int)) != cudaSuccess) {
+        cudaFree(d_out);
+        return dg::fail(DG_ERR_CUDA, "cudaMalloc failed");
+    }
+    cudaMemset(d_err, 0, sizeof(int));
+    tc_selftest_kernel<<<1, 128>>>(d_out, d_err, 1);
+    cudaError_t e = cudaDeviceSynchronize();
+    int herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d_out);
+    cudaFree(d_err);
+    if (e != cudaSuccess) return dg::fail(DG_ERR_CUDA, std::string("tensor-core wait self-test: ") + cudaGetErrorString(e));
+    *flags = herr;
+    return DG_OK;
 }

@@ -143,6 +143,7 @@ def _declare(L: C.CDLL) -> None:
         "dg_rk4_steps_timed": (C.c_int, [vp, P_d, C.c_double, C.c_int, P_d]),
         "dg_profile_steps": (C.c_int, [vp, P_d, C.c_double, C.c_int, C.POINTER(KernelTimes)]),
         "dg_monitors": (C.c_int, [vp, P_d, P_d, C.POINTER(C.c_longlong)]),
+        "dg_error_vs": (C.c_int, [vp, C.c_int, vp, C.c_int, P_d, C.POINTER(C.c_longlong)]),
         "dg_synchronize": (C.c_int, [vp]),
         "dg_info": (C.c_int, [vp, C.POINTER(C.c_longlong), P_i, C.POINTER(C.c_longlong)]),
         "dg_curved_info": (C.c_int, [vp, P_i, P_i, P_i]),
@@ -154,6 +155,7 @@ def _declare(L: C.CDLL) -> None:
         "dg_layout_get": (C.c_int, [vp, C.POINTER(LayoutView)]),
         "dg_layout_free": (None, [vp]),
         "dg_tc_selftest": (C.c_int, [C.c_int, P_d]),
+        "dg_tc_wait_selftest": (C.c_int, [C.c_int, P_i]),
         "dg_euler_steps": (C.c_int, [vp, P_d, C.c_double, C.c_int]),
         "dg_multi_create": (C.c_int, [C.c_int, vp, vp, C.POINTER(Opts), C.POINTER(vp)]),
         "dg_multi_destroy": (None, [vp]),
@@ -613,6 +615,17 @@ class Solver:
         if code not in (0, -4):
             _check(code)
         return e.value, list(l2), bad.value
+
+    def error_vs(self, ref: "Solver", member: int = 0, ref_member: int = 0) -> tuple[list[float], int]:
+        """FP64 relative L2 error per field of this context's state (batch
+        member `member`) against `ref`'s (member `ref_member`), computed on the
+        device (dg_error_vs); also the number of non-finite values."""
+        rel = (C.c_double * 4)()
+        bad = C.c_longlong()
+        code = lib().dg_error_vs(self._h, member, ref._h, ref_member, rel, C.byref(bad))
+        if code not in (0, -4):
+            _check(code)
+        return list(rel), bad.value
 
     def synchronize(self) -> None:
         _check(lib().dg_synchronize(self._h))

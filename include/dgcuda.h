@@ -19,6 +19,7 @@
  *                  combination (src/solver.cpp:261-285); t += dt.
  *   dg_get_state   the copy-out at save steps (src/solver.cpp:226-235).
  *   dg_monitors    no counterpart: FP64 discrete energy, L2 norms, NaN check.
+ *   dg_error_vs    no counterpart: FP64 relative L2 error between two states.
  *
  * Conventions: 0 = success, negative = error (DG_ERR_*); no exceptions cross
  * the ABI.  A context is not thread-safe; use one per host thread.  The host
@@ -176,8 +177,21 @@ int dg_rk4_steps_timed(dg_ctx *ctx, double *t, double dt, int nsteps, double *ms
 int dg_profile_steps(dg_ctx *ctx, double *t, double dt, int nsteps, dg_kernel_times *times);
 
 /* FP64 monitors: energy = 1/2 sum_e u_e^T M_e (p^2/(rho0 c0^2) + rho0 |v|^2);
- * l2[q] = sqrt(u_q^T M u_q); status = number of non-finite values. */
+ * l2[q] = sqrt(u_q^T M u_q); status = number of non-finite values (the call
+ * then returns DG_ERR_NONFINITE).  The mixed form's state is read as the FP64
+ * sum of its FP32 pair. */
 int dg_monitors(dg_ctx *ctx, double *energy, double *l2, long long *status);
+
+/* FP64 error monitor (no counterpart in the reference, whose only monitor is
+ * a progress line, solver.cpp:240-244): rel_l2[q] = ||u_q - r_q|| / ||r_q||
+ * over the nodal values of field q, for member `member` of ctx against member
+ * `ref_member` of ref, two contexts on the same mesh and device, of any
+ * precision (FP32 pairs joined in FP64).  Accumulated in FP64 on the device;
+ * only the 8 sums cross to the host.  Waits for ref's stream, then enqueues
+ * on ctx's and waits.  rel_l2[q] = 0 for fields the mesh does not evolve;
+ * *status (may be null) = non-finite values in ctx's state, DG_ERR_NONFINITE
+ * when nonzero. */
+int dg_error_vs(dg_ctx *ctx, int member, dg_ctx *ref, int ref_member, double *rel_l2, long long *status);
 
 /* Waits for all work of the context. */
 int dg_synchronize(dg_ctx *ctx);
@@ -233,10 +247,15 @@ void dg_layout_free(dg_layout *layout);
  * more than 1,048,576 values (fields x element nodes) are rejected with
  * DG_ERR_UNSUPPORTED.  Work is enqueued on `stream` (a cudaStream_t, 0 for
  * the default stream) and not waited for; *t advances by dt per step.
- * The first call on a device looks up the array's device address (done once
- * per device, with that device current); make that first call before any
- * stream capture.  All calls share the one array, which keeps the previous
- * call's contents (nothing in it needs to start at zero): calls whose work
+ * Every call looks up the array's device address in the current device's
+ * context (cudaGetSymbolAddress, which allocates nothing), so a device that
+ * the application reset is served at the array's new address; the first
+ * call on a device loads the library's kernels into that context, so make
+ * it before any stream capture.  Alignment: fgeo 16 bytes, conn, geo, ops
+ * and u 8 bytes (cudaMalloc and pool allocations of 256-byte granularity
+ * satisfy both); other pointers are refused with DG_ERR_ARG before any
+ * launch.  All calls share the one array, which keeps the previous call's
+ * contents (nothing in it needs to start at zero): calls whose work
  * overlaps on the GPU race on it. */
 typedef struct dg_device_layout {
     int dim, order, num_el;
@@ -337,14 +356,25 @@ int dg_parareal(dg_learned *learned, const dg_mesh_desc *mesh, const dg_phys_des
                 const double *const u0[4], int nslices, int slice_steps, double dt, double tol, int max_iter,
                 double *const uout[4], int *iters, double *hist);
 
-/* Self-test of the tensor-core primitives of the mixed form (no counterpart
- * in the reference): a 128x32x112 BF16 GEMM with A in tensor memory and B in
- * shared memory on the given device; *max_abs_err = 0 when the FP32 result
- * is exact. */
-int dg_tc_selftest(int device, double *max_abs_err);
-
 /* Message of the last error on this thread. */
 const char *dg_last_error(void);
+
+/* ---- Test hooks: not part of the drop-in surface. ----------------------
+ * Exported so the GPU tests can exercise the tensor-core primitives and the
+ * bounded-wait error path directly; an integration never calls them.
+ *
+ * dg_tc_selftest: a 128x32x112 BF16 GEMM with A in tensor memory and B in
+ * shared memory on the given device; *max_abs_err = 0 when the FP32 result
+ * is exact.
+ * dg_tc_wait_selftest: the same MMAs, then a 1 ms bounded wait on an
+ * mbarrier that nothing arrives on.  The wait runs out and the kernel takes
+ * the stage kernels' error path: it records the timeout (*flags bit 0),
+ * drains its own MMAs with a second bounded wait (bit 1 set only if that
+ * also runs out), frees its tensor memory and returns, leaving the context
+ * usable.  Returns DG_OK when the kernel ran; *flags = 1 is the expected
+ * outcome. */
+int dg_tc_selftest(int device, double *max_abs_err);
+int dg_tc_wait_selftest(int device, int *flags);
 
 #ifdef __cplusplus
 }

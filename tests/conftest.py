@@ -43,4 +43,7 @@ def built_libraries():
     yield
 
 
-REFERENCE = Path(os.environ.get("DG_REFERENCE_DIR", "/root/reference"))
+# Checkout of the reference project (read-only; only its shipped example
+# meshes are read): DG_REFERENCE_DIR, else a sibling checkout named
+# "reference" next to this repository.  Tests that need it skip without it.
+REFERENCE = Path(os.environ["DG_REFERENCE_DIR"]) if "DG_REFERENCE_DIR" in os.environ else ROOT.parent / "reference"

@@ -1,8 +1,8 @@
 """Writes tests/golden/reference_meshes.json: element, face and boundary-face
 counts of the reference's shipped gmsh meshes (doc/2d, doc/3d), read with this
 project's MSH 4.0 reader.  The count of holes comes from the Euler
-characteristic of the 2D meshes.  Run in a checkout that has the reference:
-    python tests/golden/make_reference_mesh_counts.py [/path/to/reference]
+characteristic of the 2D meshes.  Give it the reference checkout:
+    python tests/golden/make_reference_mesh_counts.py /path/to/reference
 """
 from __future__ import annotations
 
@@ -16,7 +16,9 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT / "dgfem-acoustic_gb300"))
 import dgcuda as D  # noqa: E402
 
-ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit("usage: make_reference_mesh_counts.py /path/to/reference")
+ref = Path(sys.argv[1])
 out = {}
 for n in ["doc/2d/square.msh", "doc/2d/disk.msh", "doc/2d/square_reflection.msh", "doc/2d/room.msh",
           "doc/3d/cube.msh", "doc/3d/sphere.msh"]:

@@ -82,3 +82,37 @@ def test_reference_arm_under_torchrun_prints_one_line_from_rank0():
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     for key in ("metric", "scaling", "vs_baseline", "dtype", "data", "config"):
         assert key in d
+    assert d["config"]["tets"] == 384000 and d["config"]["fields"] == 4
+    assert d["sample"] and d["sample_reason"]
+
+
+def test_reference_arm_inputs_match_the_product_workload():
+    """The reference arm builds its mesh, initial state and time step without
+    the product library (oracle_box / oracle_workload).  On a small case they
+    equal the product's box generator and precompute: same element node
+    coordinates in the same order, same initial state, same time step, and
+    the oracle's right-hand side is the same on either mesh."""
+    sys.path.insert(0, str(ROOT))
+    import numpy as np
+
+    import bench
+    import dgcuda as D
+    import oracle_py as O
+
+    n = 3
+    raw, u0, dt, v0 = bench.oracle_workload(n)
+    mesh, pre, v0p, dtp, ic = bench.workload(n)
+    X = raw["xyz"][raw["el_nodes"] - 1].reshape(-1, 3)
+    assert np.abs(X - pre.dof_coords()).max() <= 1e-15
+    assert abs(dt - dtp) <= 1e-14 * dtp and tuple(v0) == tuple(v0p)
+    up = pre.initial_state([ic])
+    assert np.abs(u0 - up).max() <= 1e-15
+    a = O.Oracle(raw, dt, 340.0, 1.225, v0=v0, upwind=True)
+    b = O.Oracle(mesh.raw(), dt, 340.0, 1.225, v0=v0, bcs=mesh.bcs(), upwind=True)
+    u = np.random.default_rng(1).standard_normal((4, pre.ndof))
+    ra, rb = a.rhs(u), b.rhs(u)
+    assert np.abs(ra - rb).max() <= 1e-12 * np.abs(rb).max()
+    # congruent cells: the time step scales with the cell size, which is how
+    # the reference arm states the full workload's dt from its sample
+    _, _, dt8 = bench.oracle_box(8)
+    assert abs(dt * n / 8 - dt8) <= 1e-15 * dt8

@@ -148,3 +148,39 @@ def test_mesh_generators_refuse_oversized_and_negative_inputs():
     h = C.c_void_p()
     code = D.lib().dgm_box_tet(2, 2, 2, lo, hi, 2, None, removed, -5, None, C.byref(h))
     assert code == DG_ERR_ARG and not h.value
+
+
+def _fake_device_layout(dim=2, order=3, num_el=8, ptr=4096):
+    dl = D.DeviceLayout()
+    dl.dim, dl.order, dl.num_el = dim, order, num_el
+    dl.c0, dl.rho0 = 340.0, 1.225
+    for k in ("geo", "fgeo", "conn", "ops", "tabs"):
+        setattr(dl, k, ptr)
+    return dl
+
+
+@pytest.mark.parametrize("field,value,msg", [("fgeo", 4096 + 8, b"fgeo must be 16-byte"),
+                                             ("conn", 4096 + 4, b"conn must be 8-byte"),
+                                             ("geo", 4096 + 4, b"8-byte"), ("ops", 4096 + 2, b"8-byte")])
+def test_noalloc_refuses_misaligned_layout_pointers_before_any_launch(field, value, msg):
+    """The stage kernels read fgeo as 16-byte vectors and conn as 8-byte
+    pairs: dg_rk4_steps_noalloc checks the caller's pointers on the host and
+    returns DG_ERR_ARG before touching the device (no GPU needed here)."""
+    dl = _fake_device_layout()
+    setattr(dl, field, value)
+    tt = C.c_double(0.0)
+    code = D.lib().dg_rk4_steps_noalloc(C.byref(dl), C.c_void_p(4096), C.byref(tt), 1e-6, 1, None)
+    assert code == -1
+    assert msg in D.lib().dg_last_error()
+    code = D.lib().dg_rk4_steps_noalloc(C.byref(_fake_device_layout()), C.c_void_p(4096 + 4), C.byref(tt),
+                                        1e-6, 1, None)
+    assert code == -1 and b"u must be 8-byte" in D.lib().dg_last_error()
+    assert tt.value == 0.0
+
+
+def test_noalloc_rejects_states_beyond_capacity():
+    dl = _fake_device_layout(dim=3, order=5, num_el=1 << 20)
+    tt = C.c_double(0.0)
+    code = D.lib().dg_rk4_steps_noalloc(C.byref(dl), C.c_void_p(4096), C.byref(tt), 1e-6, 1, None)
+    assert code == -3
+    assert b"capacity" in D.lib().dg_last_error()
