@@ -110,6 +110,43 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// Instruction descriptor of kind::tf32: D format F32 (bits 4-5 = 1), A and
+// B format TF32 (bits 7-9 = 2, 10-12 = 2), both K-major.  One MMA covers
+// K = 8 (32 bytes of each K-major row, as K = 16 does for BF16), so the
+// shared-memory core-matrix layout and the A columns per K-step (8, one
+// 32-bit value per column) are those of the BF16 path.
+__host__ __device__ constexpr uint32_t idesc_tf32_f32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// D[tmem] (+)= A[tmem] * B[smem desc]^T, kind::tf32 (TF32 inputs in 32-bit
+// containers, FP32 accumulate).
+__device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
+                                            uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.u32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// FP32 rounded to the nearest TF32 value (10 explicit mantissa bits, ties
+// away from zero), kept in a 32-bit container with the low 13 bits clear.
+__host__ __device__ __forceinline__ float tf32_round(float x) {
+#ifdef __CUDA_ARCH__
+    const uint32_t b = __float_as_uint(x);
+    return __uint_as_float((b + 0x1000u) & 0xFFFFE000u);
+#else
+    uint32_t b;
+    __builtin_memcpy(&b, &x, 4);
+    b = (b + 0x1000u) & 0xFFFFE000u;
+    float r;
+    __builtin_memcpy(&r, &b, 4);
+    return r;
+#endif
+}
+
 __device__ __forceinline__ uint64_t desc_kmajor(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr >> 4) & 0x3FFFu);

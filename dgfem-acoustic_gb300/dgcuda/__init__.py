@@ -156,6 +156,7 @@ def _declare(L: C.CDLL) -> None:
         "dg_layout_free": (None, [vp]),
         "dg_tc_selftest": (C.c_int, [C.c_int, P_d]),
         "dg_tc_wait_selftest": (C.c_int, [C.c_int, P_i]),
+        "dg_tc_selftest_tf32": (C.c_int, [C.c_int, P_d]),
         "dg_euler_steps": (C.c_int, [vp, P_d, C.c_double, C.c_int]),
         "dg_multi_create": (C.c_int, [C.c_int, vp, vp, C.POINTER(Opts), C.POINTER(vp)]),
         "dg_multi_destroy": (None, [vp]),

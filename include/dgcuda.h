@@ -366,6 +366,8 @@ const char *dg_last_error(void);
  * dg_tc_selftest: a 128x32x112 BF16 GEMM with A in tensor memory and B in
  * shared memory on the given device; *max_abs_err = 0 when the FP32 result
  * is exact.
+ * dg_tc_selftest_tf32: the same product with kind::tf32 MMAs (A as TF32
+ * values in tensor memory, one per column; B in shared memory), exact.
  * dg_tc_wait_selftest: the same MMAs, then a 1 ms bounded wait on an
  * mbarrier that nothing arrives on.  The wait runs out and the kernel takes
  * the stage kernels' error path: it records the timeout (*flags bit 0),
@@ -374,6 +376,7 @@ const char *dg_last_error(void);
  * usable.  Returns DG_OK when the kernel ran; *flags = 1 is the expected
  * outcome. */
 int dg_tc_selftest(int device, double *max_abs_err);
+int dg_tc_selftest_tf32(int device, double *max_abs_err);
 int dg_tc_wait_selftest(int device, int *flags);
 
 #ifdef __cplusplus
