@@ -388,13 +388,16 @@ FORMS = {
     "fp32": ("FP32 state, flux and geometry factors, fused stage kernel on CUDA cores", "f32",
              "stage_kernel<3,3,float>"),
     "fp64": ("FP64 throughout, fused stage kernel on CUDA cores", "f64", "stage_kernel<3,3,double>"),
+    "tf32x3": ("FP32 stage data, state kept as an FP32 pair, volume + lift contraction on the tcgen05 tensor "
+               "cores by 3xTF32 split products (a_hi b_hi + a_hi b_lo + a_lo b_hi) with FP32 accumulation",
+               "f32+tf32x3", "mixed_stage_kernel<3,3,...,kTcTf32x3> (tcgen05 kind::tf32, A in TMEM)"),
 }
 
 
 def roofline_for(sol, pre, form, t, dt, nprof):
     _, prof = sol.profile_steps(t, dt, nprof)
     real = 8 if form == "fp64" else 4
-    sb = stage_bytes(pre, real, pair_state=(form == "mixed"), geo_bytes=real)
+    sb = stage_bytes(pre, real, pair_state=(form in ("mixed", "tf32x3")), geo_bytes=real)
     avg_ms = [prof["stage_ms"][s] / max(prof["stage_launches"][s], 1) for s in range(4)]
     achieved = sum(sb) / (sum(avg_ms) * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
@@ -477,7 +480,7 @@ def ours_arm(args, world, rank, local, pg):
     # against the FP64 form after the configuration's steps
     others = {}
     if not args.no_plain:
-        for f2 in ("fp64", "fp32", "mixed"):
+        for f2 in ("fp64", "fp32", "mixed", "tf32x3"):
             if f2 == form:
                 continue
             nsteps = max(5, min(args.steps, 40 if f2 == "fp64" else 400))
@@ -543,7 +546,8 @@ def batched_section(D, args, local):
                        f"{args.batched_sources} Gaussian sources (sigma 0.03, f in [2,8], positions in [0.1,0.9]^3, "
                        f"one per batch member), 16 receivers, zero initial state, absorbing walls",
            "unit": UNIT, "dofs_per_field": pre.ndof, "members": args.batched_sources, "dt": dt}
-    for form, steps in (("mixed", args.batched_steps), ("fp64", max(2, args.batched_steps // 5))):
+    for form, steps in (("mixed", args.batched_steps), ("tf32x3", args.batched_steps),
+                        ("fp64", max(2, args.batched_steps // 5))):
         s = D.Solver(pre, C0, RHO0, (0.0, 0.0, 0.0), precision=form, flux=FLUX, device=local,
                      nbatch=args.batched_sources)
         s.set_state(zero)
@@ -556,24 +560,56 @@ def batched_section(D, args, local):
                      "clocks": clk.summary()}
         s.close()
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
-    # accuracy on the first members (same sources, same steps)
-    nacc = min(4, args.batched_sources)
-    states, traces = {}, {}
-    for form in ("fp64", "mixed"):
+    out["tf32x3_over_fp64"] = out["tf32x3"]["value"] / out["fp64"]["value"]
+    out["accuracy"] = batched_accuracy(D, pre, dt, srcs, recs, min(4, args.batched_sources),
+                                       args.batched_acc_steps, local)
+    return out
+
+
+def batched_accuracy_section(D, args, local):
+    """Accuracy of the multi-source batch as configured: every one of the 64
+    members after 1000 steps against the FP64 batch.  The FP64 batch of the
+    40^3 order-4 mesh would need ~1.8 h for 1000 steps (2.2 G DOF-stage/s),
+    so this case keeps the configuration's sources, receivers, order and step
+    count on a coarser cube (--batched-acc-cells, default 12^3 x 6 tets)."""
+    from dgcuda import workloads as W
+
+    t0 = time.time()
+    mesh, pre, dt, srcs, recs = W.multi_source(n=args.batched_acc_cells, order=4, nsrc=args.batched_sources,
+                                               seed=SEED)
+    log(f"[bench] batched accuracy: {pre.num_el} tets x {args.batched_sources} sources, setup {time.time() - t0:.1f}s")
+    t0 = time.time()
+    res = batched_accuracy(D, pre, dt, srcs, recs, args.batched_sources, args.batched_acc_all_steps, local)
+    res["workload"] = (f"unit cube {args.batched_acc_cells}^3 hexes x 6 tets ({pre.num_el} tets), order 4, "
+                       f"{args.batched_sources} Gaussian sources (sigma 0.03, f in [2,8], positions in [0.1,0.9]^3), "
+                       f"16 receivers, zero initial state, absorbing walls")
+    res["seconds"] = time.time() - t0
+    return res
+
+
+def batched_accuracy(D, pre, dt, srcs, recs, nacc, steps, local):
+    """Members 0..nacc-1 of the tensor-core batches against the FP64 batch
+    after `steps` steps (same sources): the largest relative L2 over members
+    and fields (FP64 error monitor on the device) and the receiver traces."""
+    zero = np.zeros((4, pre.ndof))
+    sols, traces = {}, {}
+    for form in ("fp64", "mixed", "tf32x3"):
         s = D.Solver(pre, C0, RHO0, (0.0, 0.0, 0.0), precision=form, flux=FLUX, device=local, nbatch=nacc)
         s.set_state(zero)
         s.set_batch_sources([x for x in srcs if x[0] < nacc])
-        s.set_receivers(recs, args.batched_acc_steps)
-        s.rk4_steps(0.0, dt, args.batched_acc_steps)
-        states[form] = [s.get_state(member=m) for m in range(nacc)]
+        s.set_receivers(recs, steps)
+        s.rk4_steps(0.0, dt, steps)
         traces[form] = s.traces()
+        sols[form] = s
+    res = {"members": nacc, "steps": steps}
+    for form in ("mixed", "tf32x3"):
+        err = max(max(sols[form].error_vs(sols["fp64"], member=m, ref_member=m)[0]) for m in range(nacc))
+        terr = float(np.linalg.norm(traces[form] - traces["fp64"]) / np.linalg.norm(traces["fp64"]))
+        res[form] = {"state_rel_l2_vs_fp64_max": float(err), "receiver_traces_rel_l2_vs_fp64": terr,
+                     "meets_1e-5": bool(err <= 1e-5)}
+    for s in sols.values():
         s.close()
-    err = max(float(np.linalg.norm(states["mixed"][m][q] - states["fp64"][m][q]) /
-                    np.linalg.norm(states["fp64"][m][q])) for m in range(nacc) for q in range(4))
-    terr = float(np.linalg.norm(traces["mixed"] - traces["fp64"]) / np.linalg.norm(traces["fp64"]))
-    out["accuracy"] = {"members": nacc, "steps": args.batched_acc_steps, "state_rel_l2_vs_fp64_max": err,
-                       "receiver_traces_rel_l2_vs_fp64": terr}
-    return out
+    return res
 
 
 def uneven_section(D, args, local):
@@ -762,21 +798,23 @@ def parareal_section(D, args, local):
 
 def accuracy_all(D, pre, u0, dt, v0, args, local, nq):
     """Every form after the configuration's steps, relative L2 per field
-    against the FP64 form (which the parity tests tie to the CPU oracle)."""
+    against the FP64 form (which the parity tests tie to the CPU oracle),
+    computed by the library's FP64 error monitor on the device."""
     res = {}
-    states = {}
-    for f2 in ("fp64", "mixed", "fp32"):
+    ref = D.Solver(pre, C0, RHO0, v0, precision="fp64", flux=FLUX, device=local)
+    ref.set_state(u0)
+    ref.rk4_steps(0.0, dt, args.accuracy_steps)
+    res["fp64_energy_final"] = ref.monitors()[0]
+    for f2 in ("mixed", "tf32x3", "fp32"):
         s = D.Solver(pre, C0, RHO0, v0, precision=f2, flux=FLUX, device=local)
         s.set_state(u0)
         s.rk4_steps(0.0, dt, args.accuracy_steps)
-        states[f2] = s.get_state()
-        if f2 == "fp64":
-            res["fp64_energy_final"] = s.monitors()[0]
+        rel, bad = s.error_vs(ref)
+        per = [float(x) for x in rel[:nq]]
+        res[f2] = {"rel_l2_vs_fp64": max(per), "per_field": per, "nonfinite": bad,
+                   "meets_1e-5": bool(bad == 0 and max(per) <= 1e-5)}
         s.close()
-    ref = states["fp64"]
-    for f2 in ("mixed", "fp32"):
-        per = [float(np.linalg.norm(states[f2][q] - ref[q]) / np.linalg.norm(ref[q])) for q in range(nq)]
-        res[f2] = {"rel_l2_vs_fp64": max(per), "per_field": per}
+    ref.close()
     res["steps"] = args.accuracy_steps
     res["rel_l2_vs_fp64"] = res[args.form]["rel_l2_vs_fp64"] if args.form != "fp64" else 0.0
     res["fp64_vs_oracle"] = "FP64 GPU form matches the CPU oracle to <=1e-10 relative L2 (tests/test_gpu_parity.py)"
@@ -799,12 +837,15 @@ def main():
     ap.add_argument("--cells", type=int, default=NCELL, help="cube cells per side (profiling cases)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--form", choices=["mixed", "fp32", "fp64"], default="mixed")
+    ap.add_argument("--form", choices=["mixed", "tf32x3", "fp32", "fp64"], default="mixed")
     ap.add_argument("--no-batched", action="store_true", help="skip the multi-source batch section")
     ap.add_argument("--batched-cells", type=int, default=NCELL)
     ap.add_argument("--batched-sources", type=int, default=64)
     ap.add_argument("--batched-steps", type=int, default=10)
     ap.add_argument("--batched-acc-steps", type=int, default=100)
+    ap.add_argument("--batched-acc-cells", type=int, default=12,
+                    help="cube cells per side of the all-members accuracy case (--batched-accuracy-only)")
+    ap.add_argument("--batched-acc-all-steps", type=int, default=1000)
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven multi-mesh section")
     ap.add_argument("--uneven-meshes", type=int, default=32)
     ap.add_argument("--uneven-steps", type=int, default=500)
@@ -823,6 +864,8 @@ def main():
                     help="run the curved-element section alone (profiling case) and print it as one JSON line")
     ap.add_argument("--parareal-only", action="store_true",
                     help="run the learned parareal section alone (profiling case) and print it as one JSON line")
+    ap.add_argument("--batched-accuracy-only", action="store_true",
+                    help="every member of the multi-source batch after 1000 steps against FP64 (coarser cube)")
     ap.add_argument("--batched-only", action="store_true",
                     help="run the multi-source batch section alone (profiling case) and print it as one JSON line")
     ap.add_argument("--uneven-only", action="store_true",
@@ -832,7 +875,8 @@ def main():
     world, rank, local, pg = dist_init()
     only = [(flag, key, fn) for flag, key, fn in
             ((args.curved_only, "curved", curved_section), (args.parareal_only, "learned_parareal", parareal_section),
-             (args.batched_only, "batched", batched_section), (args.uneven_only, "uneven_batch", uneven_section))
+             (args.batched_only, "batched", batched_section), (args.uneven_only, "uneven_batch", uneven_section),
+             (args.batched_accuracy_only, "batched_accuracy_all_members", batched_accuracy_section))
             if flag]
     if only:
         import dgcuda as D

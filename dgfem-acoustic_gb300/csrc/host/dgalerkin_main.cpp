@@ -9,7 +9,7 @@
 // (solver.cpp:185-191, 225-238, 289-291).  The right-hand side runs through
 // the C ABI of include/dgcuda.h; steps between two saves are one
 // dg_rk4_steps call.  Options the reference does not read: precision
-// (fp64 | fp32 | mixed) and fluxSign (reference | upwind) in the .conf.
+// (fp64 | fp32 | mixed | tf32x3) and fluxSign (reference | upwind) in the .conf.
 #include <cerrno>
 #include <chrono>
 #include <cmath>
@@ -130,7 +130,10 @@ int main(int argc, char **argv) {
     for (int k = 0; k < 3; ++k) phys.v0[k] = cfg.v0[k];
     dg_opts opts;
     dg_default_opts(&opts);
-    opts.precision = cfg.precision == "fp32" ? DG_PREC_FP32 : cfg.precision == "mixed" ? DG_PREC_MIXED : DG_PREC_FP64;
+    opts.precision = cfg.precision == "fp32"     ? DG_PREC_FP32
+                     : cfg.precision == "mixed"  ? DG_PREC_MIXED
+                     : cfg.precision == "tf32x3" ? DG_PREC_TF32X3
+                                                 : DG_PREC_FP64;
     opts.flux_sign = cfg.fluxSign == "upwind" ? DG_FLUX_UPWIND : DG_FLUX_REFERENCE;
     dg_ctx *ctx = nullptr;
     if (dg_create(&desc, &phys, &opts, &ctx) != DG_OK) {

@@ -48,8 +48,8 @@ struct MixedKernelSet {
 };
 
 // masked: the variant for meshes with curved elements (MixedArgs::blist and
-// cmask in use).
-bool get_mixed_kernels(int dim, int order, bool masked, MixedKernelSet *out);
+// cmask in use).  kind: 0 = exact fixed-point BF16 slices, 1 = 3xTF32.
+bool get_mixed_kernels(int dim, int order, bool masked, int kind, MixedKernelSet *out);
 
 // Arguments of the mixed-precision stage kernels.
 struct MixedArgs {

@@ -42,14 +42,23 @@
 
 namespace dgk {
 
-template <int DIM, int P>
+// Contraction kinds: the exact fixed-point form (four BF16 slices of each
+// operand, kind::f16 MMAs, exact accumulation) and 3xTF32 (each operand split
+// into a high and a low TF32 part, a_hi b_hi + a_hi b_lo + a_lo b_hi by
+// kind::tf32 MMAs, FP32 accumulation).
+constexpr int kTcBf16x4 = 0, kTcTf32x3 = 1;
+
+template <int DIM, int P, int KIND = kTcBf16x4>
 struct MixedShape {
     using S = Shape<DIM, P>;
+    static constexpr bool TF = KIND == kTcTf32x3;
     static constexpr int NP = S::NP, NF = S::NF, NFP = S::NFP, NQ = S::NQ, NSLOT = S::NSLOT;
     static constexpr int NPERM = S::NPERM;
     static constexpr int KTOT = DIM * NP + NSLOT;
-    static constexpr int KPAD = (KTOT + 15) / 16 * 16;
-    static constexpr int KSTEPS = KPAD / 16;
+    static constexpr int KSTEP = TF ? 8 : 16;       // K of one MMA (32 bytes of a K-major row)
+    static constexpr int KPAD = (KTOT + KSTEP - 1) / KSTEP * KSTEP;
+    static constexpr int KSTEPS = KPAD / KSTEP;
+    static constexpr int NSLICE = TF ? 2 : 4;       // parts of each operand
     static constexpr int NPAD = (NP + 15) / 16 * 16;
     static constexpr int ELEMS = 128 / NQ;          // elements per tile
     static constexpr int TMEM_COLS = 512;
@@ -60,24 +69,27 @@ struct MixedShape {
     // slices of all K-steps and the four levels do not fit in tensor memory
     // together (3D order 4), the K-steps go in two passes that reuse the A
     // columns (the second pass is sliced once the first pass's MMAs are done).
-    static constexpr bool LEVELS_ONE = 4 * (KPAD / 2) + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256;
+    // 3xTF32: the two A parts of every K-step (one 32-bit value per column)
+    // and two accumulators (a_hi b_hi + a_lo b_hi, a_hi b_lo), one pass.
+    static constexpr bool LEVELS_ONE = !TF && 4 * (KPAD / 2) + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256;
     static constexpr int KPASS_TWO = (KSTEPS + 1) / 2;
-    static constexpr bool LEVELS_TWO = !LEVELS_ONE && 4 * KPASS_TWO * 8 + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256;
+    static constexpr bool LEVELS_TWO =
+        !TF && !LEVELS_ONE && 4 * KPASS_TWO * 8 + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256;
     static constexpr int NPASS = LEVELS_TWO ? 2 : 1;
     static constexpr int KPASS = NPASS == 2 ? KPASS_TWO : KSTEPS;  // K-steps per pass
     static constexpr bool LEVELS = LEVELS_ONE || LEVELS_TWO;
     static constexpr int ACOLS = KPASS * 8;         // tensor-memory columns per A slice (one pass)
-    static constexpr int ACC = 4 * ACOLS;           // first accumulator column
-    static constexpr bool FITS = ACC + 3 * NPAD <= TMEM_COLS;
+    static constexpr int ACC = TF ? (2 * ACOLS + 31) / 32 * 32 : 4 * ACOLS;  // first accumulator column
+    static constexpr bool FITS = TF ? (ACC + 2 * NPAD <= TMEM_COLS && 2 * NPAD <= 256) : ACC + 3 * NPAD <= TMEM_COLS;
     // Pair scheme (otherwise): one MMA per slice pair; accumulator 0 for
     // i+j = 0, 1 for i+j = 1 (both exact), NX more for the seven pairs with
     // i+j = 2, 3 (spread so that the MMAs of consecutive pairs do not wait on
     // one another)
     static constexpr int NACC_FIT = (TMEM_COLS - ACC) / NPAD;
-    static constexpr int NACC = LEVELS ? 4 : NACC_FIT < 9 ? NACC_FIT : 9;
+    static constexpr int NACC = TF ? 2 : LEVELS ? 4 : NACC_FIT < 9 ? NACC_FIT : 9;
     static constexpr int NX = NACC - 2;
     static constexpr int BTILE = NPAD * 32;         // bytes of one (K-step, slice) B tile; image [K-step][slice]
-    static constexpr int BBYTES = 4 * KSTEPS * BTILE;
+    static constexpr int BBYTES = NSLICE * KSTEPS * BTILE;
     static constexpr int QS = NP;                   // element stride in the state tile
     static constexpr int KSTR = KPAD + 1;           // padded row stride of the staged A rows (odd)
     static constexpr int MAX_WG = 4;                // warp groups per CTA (4 warps each), at most
@@ -170,10 +182,10 @@ __device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
 
 // Issues the cp.async copies of a tile's connectivity words into buffer cb;
 // the calling threads take words first, first + stride, ...
-template <int DIM, int P>
+template <int DIM, int P, int KIND>
 __device__ __forceinline__ void issue_conn_copies(const MixedArgs &a, unsigned char *smem, long long ebase, int cb,
                                                   int first, int stride) {
-    using MS = MixedShape<DIM, P>;
+    using MS = MixedShape<DIM, P, KIND>;
     constexpr int NF = MS::NF, ELEMS = MS::ELEMS;
     int2 *sConn = reinterpret_cast<int2 *>(smem + MS::OFF_CONN + cb * MS::CONN_BYTES);
     for (int idx = first; idx < ELEMS * NF; idx += stride) {
@@ -184,10 +196,10 @@ __device__ __forceinline__ void issue_conn_copies(const MixedArgs &a, unsigned c
 
 // Issues the cp.async copies of a tile's element data: state, inverse
 // Jacobians and face geometry (zero-filled past K).
-template <int DIM, int P>
+template <int DIM, int P, int KIND>
 __device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned char *smem, long long ebase,
                                                   long long moff, bool vec, int first, int stride) {
-    using MS = MixedShape<DIM, P>;
+    using MS = MixedShape<DIM, P, KIND>;
     constexpr int NP = MS::NP, NF = MS::NF, NQ = MS::NQ, ELEMS = MS::ELEMS, QS = MS::QS;
     static_assert(QS == NP, "the state tile is stored unpadded, as in global memory");
     float *sQ = reinterpret_cast<float *>(smem + MS::OFF_Q);
@@ -221,10 +233,10 @@ __device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned c
 // Issues the cp.async gathers of the neighbour traces of a tile's interior
 // face slots (reads the tile's connectivity words from buffer cb); the
 // calling threads take tasks first, first + stride, ...
-template <int DIM, int P>
+template <int DIM, int P, int KIND>
 __device__ __forceinline__ void issue_neighbour_copies(const MixedArgs &a, unsigned char *smem, long long ebase,
                                                        long long moff, int cb, int first, int stride) {
-    using MS = MixedShape<DIM, P>;
+    using MS = MixedShape<DIM, P, KIND>;
     constexpr int NP = MS::NP, NF = MS::NF, NFP = MS::NFP, NQ = MS::NQ, NSLOT = MS::NSLOT, ELEMS = MS::ELEMS;
     float *sNbr = reinterpret_cast<float *>(smem + MS::OFF_NBR);
     const int2 *sConn = reinterpret_cast<const int2 *>(smem + MS::OFF_CONN + cb * MS::CONN_BYTES);
@@ -247,10 +259,10 @@ __device__ __forceinline__ void issue_neighbour_copies(const MixedArgs &a, unsig
 // fluxes (one task per element node) and the face values negated and scaled
 // by detJf/detJe (one task per face slot), from the tile's state, geometry,
 // connectivity words (buffer cb) and neighbour traces.
-template <int DIM, int P>
+template <int DIM, int P, int KIND>
 __device__ __forceinline__ void build_rows(const MixedArgs &a, unsigned char *smem, long long ebase, int cb, int first,
                                            int stride) {
-    using MS = MixedShape<DIM, P>;
+    using MS = MixedShape<DIM, P, KIND>;
     constexpr int NP = MS::NP, NF = MS::NF, NFP = MS::NFP, NQ = MS::NQ, NSLOT = MS::NSLOT;
     constexpr int ELEMS = MS::ELEMS, QS = MS::QS, KSTR = MS::KSTR;
     const float *sQ = reinterpret_cast<const float *>(smem + MS::OFF_Q);
@@ -355,9 +367,9 @@ __device__ __forceinline__ void build_rows(const MixedArgs &a, unsigned char *sm
 // Largest magnitude of each A row over the K-steps of each warp group's
 // slicing range: sMax[g*128 + r] for part g of row r (items (g, r) spread over
 // the threads first, first + stride, ...).
-template <int DIM, int P, int NWG>
+template <int DIM, int P, int NWG, int KIND>
 __device__ __forceinline__ void row_maxima(unsigned char *smem, int first, int stride) {
-    using MS = MixedShape<DIM, P>;
+    using MS = MixedShape<DIM, P, KIND>;
     constexpr int KSTEPS = MS::KSTEPS, KTOT = MS::KTOT, KSTR = MS::KSTR;
     constexpr int KSP = (KSTEPS + NWG - 1) / NWG;
     const float *sA = reinterpret_cast<const float *>(smem + MS::OFF_A);
@@ -372,9 +384,9 @@ __device__ __forceinline__ void row_maxima(unsigned char *smem, int first, int s
     }
 }
 
-template <int DIM, int P, int STAGE, int NWG, bool MASKED>
+template <int DIM, int P, int STAGE, int NWG, bool MASKED, int KIND>
 __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedArgs a) {
-    using MS = MixedShape<DIM, P>;
+    using MS = MixedShape<DIM, P, KIND>;
     constexpr int NP = MS::NP, NQ = MS::NQ;
     constexpr int ELEMS = MS::ELEMS, KTOT = MS::KTOT, KSTEPS = MS::KSTEPS, KSTR = MS::KSTR;
     constexpr int NPAD = MS::NPAD, ACOLS = MS::ACOLS;
@@ -386,7 +398,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     static_assert(NWG >= 1 && NWG <= MS::MAX_WG, "warp groups");
     constexpr int NX = MS::NX;
     constexpr bool OVERLAP = MS::OVERLAP;
-    static_assert(NX >= 1, "at least three accumulators");
+    static_assert(MS::TF || NX >= 1, "at least three accumulators");
     static_assert(MS::ACC + (MS::NACC - 1) * NPAD + (NWG - 1) * NPP + 8 * NCH <= MS::TMEM_COLS,
                   "epilogue loads stay inside the allocation");
     static_assert(ELEMS <= 64, "curved-element mask holds 64 elements per tile");
@@ -459,11 +471,11 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     if ((long long)blockIdx.x < ntiles) {
         long long eb, mo;
         tile_base(blockIdx.x, eb, mo);
-        issue_conn_copies<DIM, P>(a, smem, eb, 0, tid, NT);
-        issue_tile_copies<DIM, P>(a, smem, eb, mo, vec, tid, NT);
+        issue_conn_copies<DIM, P, KIND>(a, smem, eb, 0, tid, NT);
+        issue_tile_copies<DIM, P, KIND>(a, smem, eb, mo, vec, tid, NT);
         dgtc::cp_async_wait_all();
         __syncthreads();
-        issue_neighbour_copies<DIM, P>(a, smem, eb, mo, 0, tid, NT);
+        issue_neighbour_copies<DIM, P, KIND>(a, smem, eb, mo, 0, tid, NT);
         dgtc::cp_async_commit();
         if constexpr (OVERLAP) {
             // the first tile's rows now; every later tile's while its
@@ -474,14 +486,14 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             if (T1 < ntiles) {
                 long long e1, m1;
                 tile_base(T1, e1, m1);
-                issue_conn_copies<DIM, P>(a, smem, e1, 1, tid, NT);
+                issue_conn_copies<DIM, P, KIND>(a, smem, e1, 1, tid, NT);
             }
             dgtc::cp_async_commit();
-            build_rows<DIM, P>(a, smem, eb, 0, tid, NT);
+            build_rows<DIM, P, KIND>(a, smem, eb, 0, tid, NT);
             __syncthreads();
             // the row maxima of every later tile are taken right after its
-            // rows, while the previous tile's MMAs run
-            row_maxima<DIM, P, NWG>(smem, tid, NT);
+            // rows, while the previous tile's MMAs run (3xTF32 needs none)
+            if constexpr (!MS::TF) row_maxima<DIM, P, NWG, KIND>(smem, tid, NT);
         }
     }
     int cb = 0;  // connectivity buffer of the current tile
@@ -494,16 +506,16 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
         if constexpr (!OVERLAP) {
             dgtc::cp_async_wait_all();
             __syncthreads();
-            if (next < ntiles) issue_conn_copies<DIM, P>(a, smem, nebase, cb ^ 1, tid, NT);
+            if (next < ntiles) issue_conn_copies<DIM, P, KIND>(a, smem, nebase, cb ^ 1, tid, NT);
             dgtc::cp_async_commit();
-            build_rows<DIM, P>(a, smem, ebase, cb, tid, NT);
+            build_rows<DIM, P, KIND>(a, smem, ebase, cb, tid, NT);
             __syncthreads();
         }
         // the tile's element data are consumed: start copying the next tile's
         // (with the overlap, warp 0 copies nothing for the next tile: it only
         // issues the MMAs while the other warps consume these copies)
         if (next < ntiles && (!OVERLAP || warp > 0))
-            issue_tile_copies<DIM, P>(a, smem, nebase, nmoff, vec, OVERLAP ? tid - 32 : tid, OVERLAP ? NT - 32 : NT);
+            issue_tile_copies<DIM, P, KIND>(a, smem, nebase, nmoff, vec, OVERLAP ? tid - 32 : tid, OVERLAP ? NT - 32 : NT);
         dgtc::cp_async_commit();
         // this thread's connectivity copies of the next tile are complete (only
         // the group just committed may still be pending); the barrier after
@@ -530,7 +542,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             }
         }
         const float *arow = &sA[r * KSTR];
-        if constexpr (!OVERLAP) {
+        if constexpr (!OVERLAP && !MS::TF) {
             float m = 0.0f;
             if (row_ok)
                 for (int k = ks0 * 16; k < ks1 * 16 && k < KTOT; ++k) m = fmaxf(m, fabsf(arow[k]));
@@ -538,17 +550,22 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
         }
         __syncthreads();
         if (next < ntiles && (!OVERLAP || warp > 0))
-            issue_neighbour_copies<DIM, P>(a, smem, nebase, nmoff, cb ^ 1, OVERLAP ? tid - 32 : tid,
+            issue_neighbour_copies<DIM, P, KIND>(a, smem, nebase, nmoff, cb ^ 1, OVERLAP ? tid - 32 : tid,
                                            OVERLAP ? NT - 32 : NT);
         dgtc::cp_async_commit();
-        float rmax = sMax[r];
+        int ea = 0;
+        bool live = row_ok;
+        float sc = 0.0f;
+        if constexpr (!MS::TF) {
+            float rmax = sMax[r];
 #pragma unroll
-        for (int g = 1; g < NWG; ++g) rmax = fmaxf(rmax, sMax[g * 128 + r]);
-        const int ea = row_exponent(rmax);
-        // rows below 2^-110 are treated as zero (their contribution is far
-        // below the FP32 resolution of any non-negligible row)
-        const bool live = row_ok && ea > -110;
-        const float sc = live ? exp2i(8 - ea) : 0.0f;
+            for (int g = 1; g < NWG; ++g) rmax = fmaxf(rmax, sMax[g * 128 + r]);
+            ea = row_exponent(rmax);
+            // rows below 2^-110 are treated as zero (their contribution is far
+            // below the FP32 resolution of any non-negligible row)
+            live = row_ok && ea > -110;
+            sc = live ? exp2i(8 - ea) : 0.0f;
+        }
         // K-steps of each pass (one pass unless tensor memory is short); the
         // pass's K-steps are spread over the warp groups for the slicing
         constexpr int NPASS = MS::NPASS, KPASS = MS::KPASS;
@@ -565,7 +582,23 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
                 dgtc::fence_after_sync();
             }
 #pragma unroll 1
-            for (int c = c0; c < c1; ++c) {
+            for (int c = c0; c < c1 && MS::TF; ++c) {
+                // 3xTF32: high part and remainder of every value, one per column
+                uint32_t wh[8], wl[8];
+#pragma unroll
+                for (int h = 0; h < 8; ++h) {
+                    const int k = c * 8 + h;
+                    const float x = (live && k < KTOT) ? arow[k] : 0.0f;
+                    const float xh = dgtc::tf32_round(x);
+                    wh[h] = __float_as_uint(xh);
+                    wl[h] = __float_as_uint(dgtc::tf32_round(x - xh));
+                }
+                __syncwarp();
+                dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, c * 8), wh);
+                dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, ACOLS + c * 8), wl);
+            }
+#pragma unroll 1
+            for (int c = c0; c < c1 && !MS::TF; ++c) {
                 uint32_t w[4][8];
 #pragma unroll
                 for (int h = 0; h < 8; ++h) {
@@ -590,7 +623,18 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             // 4. tensor-core contraction, issued by thread 0 K-step by K-step
             if (tid == 0 && !*sFail) {
                 dgtc::fence_after_sync();
-                if constexpr (MS::LEVELS) {
+                if constexpr (MS::TF) {
+                    // per K-step: a_hi against [b_hi | b_lo] into both
+                    // accumulators, then a_lo against b_hi into the first
+#pragma unroll 1
+                    for (int t = 0; t < KSTEPS; ++t) {
+                        const uint64_t bd = dgtc::desc_kmajor(sB + t * 2 * MS::BTILE, 128, 256);
+                        dgtc::mma_tf32_ts(tbase + MS::ACC, tbase + t * 8, bd, dgtc::idesc_tf32_f32(128, 2 * NPAD),
+                                          t > 0 ? 1u : 0u);
+                        dgtc::mma_tf32_ts(tbase + MS::ACC, tbase + ACOLS + t * 8, bd, dgtc::idesc_tf32_f32(128, NPAD),
+                                          1u);
+                    }
+                } else if constexpr (MS::LEVELS) {
                     // A slice 0 at K-step 0 starts all four levels
 #pragma unroll 1
                     for (int t = kb; t < ke; ++t) {
@@ -630,11 +674,13 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
                 if (next2 < ntiles) {
                     long long e2, m2;
                     tile_base(next2, e2, m2);
-                    issue_conn_copies<DIM, P>(a, smem, e2, cb, tid - 32, NT - 32);
+                    issue_conn_copies<DIM, P, KIND>(a, smem, e2, cb, tid - 32, NT - 32);
                 }
-                build_rows<DIM, P>(a, smem, nebase, cb ^ 1, tid - 32, NT - 32);
-                asm volatile("bar.sync 1, %0;" ::"r"(NT - 32) : "memory");
-                row_maxima<DIM, P, NWG>(smem, tid - 32, NT - 32);
+                build_rows<DIM, P, KIND>(a, smem, nebase, cb ^ 1, tid - 32, NT - 32);
+                if constexpr (!MS::TF) {
+                    asm volatile("bar.sync 1, %0;" ::"r"(NT - 32) : "memory");
+                    row_maxima<DIM, P, NWG, KIND>(smem, tid - 32, NT - 32);
+                }
             }
             dgtc::cp_async_commit();
         }
@@ -657,6 +703,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             }
 #pragma unroll
             for (int k = 0; k < 8 * NCH; ++k) v2[k] = 0.0f;
+            if constexpr (NX == 0) dgtc::tmem_ld_wait();
             // the extra accumulators, four at a time
 #pragma unroll
             for (int x0 = 0; x0 < NX; x0 += 4) {
@@ -685,11 +732,16 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
                 for (int t = 0; t < NPP; ++t) {
                     const int i = i0 + t;
                     if (i >= NP) break;
-                    float hi, lo;
-                    two_sum(__uint_as_float(v0[t]), __uint_as_float(v1[t]), hi, lo);
-                    lo += v2[t];
-                    const float scl = sdt * exp2i(sEb[i]);
-                    const float rr = fmaf(scl, hi, scl * lo);
+                    float rr;
+                    if constexpr (MS::TF) {
+                        rr = a.dt * (__uint_as_float(v0[t]) + __uint_as_float(v1[t]));
+                    } else {
+                        float hi, lo;
+                        two_sum(__uint_as_float(v0[t]), __uint_as_float(v1[t]), hi, lo);
+                        lo += v2[t];
+                        const float scl = sdt * exp2i(sEb[i]);
+                        rr = fmaf(scl, hi, scl * lo);
+                    }
                     const int o = r * NP + i;  // row r = (field, element) of the tile
                     if (STAGE == 1) {
                         sO0[o] = rr;

@@ -428,7 +428,8 @@ static int dg_create_batch_impl(const dg_mesh_desc *m, const dg_phys_desc *ph, c
     else dg_default_opts(&opts);
     if (m->dim != 2 && m->dim != 3) return fail(DG_ERR_UNSUPPORTED, "dimension must be 2 or 3");
     if (m->order < 1 || m->order > 5) return fail(DG_ERR_UNSUPPORTED, "order must be in 1..5");
-    if (opts.precision != DG_PREC_FP64 && opts.precision != DG_PREC_FP32 && opts.precision != DG_PREC_MIXED)
+    if (opts.precision != DG_PREC_FP64 && opts.precision != DG_PREC_FP32 && opts.precision != DG_PREC_MIXED &&
+        opts.precision != DG_PREC_TF32X3)
         return fail(DG_ERR_ARG, "unknown precision");
     if (opts.flux_sign != DG_FLUX_REFERENCE && opts.flux_sign != DG_FLUX_UPWIND)
         return fail(DG_ERR_ARG, "unknown flux sign mode");
@@ -454,7 +455,9 @@ static int dg_create_batch_impl(const dg_mesh_desc *m, const dg_phys_desc *ph, c
     c->rsize = c->prec == DG_PREC_FP64 ? 8 : 4;
     c->c0 = ph->c0; c->rho0 = ph->rho0;
     for (int k = 0; k < 3; ++k) c->v0[k] = ph->v0[k];
-    c->mixed = c->prec == DG_PREC_MIXED;
+    // both tensor-core forms keep the state as an FP32 pair and share the
+    // mixed form's kernels and buffers; they differ in the contraction
+    c->mixed = c->prec == DG_PREC_MIXED || c->prec == DG_PREC_TF32X3;
     c->naff = lay.curved.C > 0 ? (int)lay.curved.affine.size() : K;
 
     // the mixed form keeps FP32 stage data and uses the FP32 helper kernels
@@ -462,9 +465,10 @@ static int dg_create_batch_impl(const dg_mesh_desc *m, const dg_phys_desc *ph, c
         free_ctx(c);
         return fail(DG_ERR_UNSUPPORTED, "no kernel compiled for this order");
     }
-    if (c->mixed && !dgk::get_mixed_kernels(dim, m->order, lay.curved.C > 0, &c->mks)) {
+    if (c->mixed && !dgk::get_mixed_kernels(dim, m->order, lay.curved.C > 0, c->prec == DG_PREC_TF32X3 ? 1 : 0,
+                                            &c->mks)) {
         free_ctx(c);
-        return fail(DG_ERR_UNSUPPORTED, "the mixed form supports orders 1-4 in 3D and 1-5 in 2D");
+        return fail(DG_ERR_UNSUPPORTED, "the tensor-core forms support orders 1-4 in 3D and 1-5 in 2D");
     }
     int rc = DG_OK;
     auto fin = [&](cudaError_t e, const char *what) {

@@ -26,7 +26,7 @@ import numpy as np
 PKG = Path(__file__).resolve().parent.parent
 LIB_PATH = PKG / "lib" / "libdgcuda.so"
 
-PREC_FP64, PREC_FP32, PREC_MIXED = 0, 1, 2
+PREC_FP64, PREC_FP32, PREC_MIXED, PREC_TF32X3 = 0, 1, 2, 3
 FLUX_REFERENCE, FLUX_UPWIND = 0, 1
 ERRORS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "unsupported", -4: "non-finite values",
           -5: "I/O error", -6: "mesh error", -7: "out of memory", -8: "configuration error"}
@@ -496,7 +496,7 @@ class Solver:
         ph = PhysDesc(c0, rho0, (C.c_double * 3)(*v0))
         o = Opts()
         lib().dg_default_opts(C.byref(o))
-        o.precision = {"fp64": PREC_FP64, "fp32": PREC_FP32, "mixed": PREC_MIXED}[precision]
+        o.precision = {"fp64": PREC_FP64, "fp32": PREC_FP32, "mixed": PREC_MIXED, "tf32x3": PREC_TF32X3}[precision]
         o.flux_sign = {"reference": FLUX_REFERENCE, "upwind": FLUX_UPWIND}[flux]
         o.use_graph = 1 if use_graph else 0
         o.device = device

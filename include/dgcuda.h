@@ -50,6 +50,9 @@ extern "C" {
 #define DG_PREC_MIXED 2 /* FP32 stage data, state kept as an FP32 pair, volume + lift
                          * contraction on the tensor cores (BF16 fixed-point slices,
                          * exact FP32 accumulation); orders 1-4 in 3D, 1-5 in 2D */
+#define DG_PREC_TF32X3 3 /* as DG_PREC_MIXED, the contraction by 3xTF32 split products
+                          * (a_hi b_hi + a_hi b_lo + a_lo b_hi, kind::tf32 MMAs, FP32
+                          * accumulation); orders 1-4 in 3D, 1-5 in 2D */
 
 #define DG_FLUX_REFERENCE 0 /* interior jump sign fc*orientation, as the reference (Mesh.cpp:524) */
 #define DG_FLUX_UPWIND 1    /* interior jump sign +1 on every face */
