@@ -75,4 +75,12 @@ struct dg_ctx {
     int graph_method = -1;
     // events for profiling
     std::vector<cudaEvent_t> events;
+    // asynchronous copy-out (dg_get_state_async): FP64 snapshots taken on the
+    // solver stream into a two-slot ring, device-to-host copies on a side
+    // stream; save_ticket[s] = last ticket issued on slot s (-1: none)
+    cudaStream_t save_stream = nullptr;
+    double *d_snap[2] = {nullptr, nullptr};
+    cudaEvent_t snap_ready[2] = {nullptr, nullptr}, snap_done[2] = {nullptr, nullptr};
+    long long save_ticket[2] = {-1, -1};
+    long long save_next = 0;
 };

@@ -25,10 +25,16 @@
 
 namespace {
 
+// A saved frame: the state [4][ndof] in pinned host memory (dg_host_alloc),
+// filled by dg_get_state_async while the next steps run; `ticket` is waited
+// for before the views are written.  `own` is the pageable fallback when no
+// pinned memory can be had.
 struct Frame {
     double t;
     int step;
-    std::vector<double> u;  // [4][ndof]
+    double *u = nullptr;
+    long long ticket = -1;
+    std::vector<double> own;
 };
 
 void log(const std::string &s) { std::printf("Info    : %s\n", s.c_str()); }
@@ -141,7 +147,6 @@ int main(int argc, char **argv) {
         return EXIT_FAILURE;
     }
     const double *uq[4] = {&u[0], &u[ndof], &u[2 * ndof], &u[3 * ndof]};
-    double *uo[4] = {&u[0], &u[ndof], &u[2 * ndof], &u[3 * ndof]};
     int rc = dg_set_state(ctx, uq);
     // sources (solver.cpp:197-210)
     if (rc == DG_OK && !cfg.sources.empty()) {
@@ -174,9 +179,19 @@ int main(int argc, char **argv) {
                 pending = 0;
                 if (rc != DG_OK) break;
             }
-            rc = dg_get_state(ctx, uo);
+            // the copy-out overlaps the steps that follow (the reference
+            // copies the state into its views here, solver.cpp:226-235)
+            frames.emplace_back();
+            Frame &fr = frames.back();
+            fr.t = t;
+            fr.step = (int)step;
+            fr.u = static_cast<double *>(dg_host_alloc(4 * ndof * sizeof(double)));
+            if (!fr.u) {
+                fr.own.resize(4 * ndof);
+                fr.u = fr.own.data();
+            }
+            rc = dg_get_state_async(ctx, fr.u, &fr.ticket);
             if (rc != DG_OK) break;
-            frames.push_back({t, (int)step, u});
             auto el = std::chrono::duration_cast<std::chrono::seconds>(std::chrono::system_clock::now() - start);
             log("[" + std::to_string(t) + "/" + std::to_string(cfg.timeEnd) + "s] Step number : " +
                 std::to_string((int)step) + ", Elapsed time: " + std::to_string(el.count()) + "s");
@@ -185,13 +200,22 @@ int main(int argc, char **argv) {
         ++pending;
     }
     if (rc == DG_OK && pending) rc = run_steps(ctx, &t_run, cfg.timeStep, pending);
+    for (Frame &fr : frames)
+        if (rc == DG_OK && fr.ticket >= 0) rc = dg_wait_state(ctx, fr.ticket);
+    auto release = [&]() {
+        for (Frame &fr : frames)
+            if (fr.own.empty()) dg_host_free(fr.u);
+    };
     if (rc != DG_OK) {
         std::fprintf(stderr, "Error   : %s\n", dg_last_error());
-        dg_destroy(ctx);
+        dg_destroy(ctx);  // waits for copies still in flight
+        release();
         return EXIT_FAILURE;
     }
     dg_destroy(ctx);
-    if (!write_views(cfg.saveFile, mesh, pre, cfg, frames)) return EXIT_FAILURE;
+    const bool ok = write_views(cfg.saveFile, mesh, pre, cfg, frames);
+    release();
+    if (!ok) return EXIT_FAILURE;
     log("Views written to " + cfg.saveFile);
     return EXIT_SUCCESS;
 }

@@ -198,6 +198,16 @@ int cuda_fail(cudaError_t e, const char *what) {
 void free_ctx(dg_ctx *c) {
     if (!c) return;
     if (c->device >= 0) cudaSetDevice(c->device);
+    if (c->save_stream) {
+        // copies to the caller's buffers may still be in flight
+        cudaStreamSynchronize(c->save_stream);
+        cudaStreamDestroy(c->save_stream);
+    }
+    for (int k = 0; k < 2; ++k) {
+        if (c->snap_ready[k]) cudaEventDestroy(c->snap_ready[k]);
+        if (c->snap_done[k]) cudaEventDestroy(c->snap_done[k]);
+        if (c->d_snap[k]) cudaFree(c->d_snap[k]);
+    }
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     for (auto ev : c->events) cudaEventDestroy(ev);
     void *ptrs[] = {c->d_state, c->d_geo,     c->d_fgeo,    c->d_conn,    c->d_ops,     c->d_tabs,
@@ -759,6 +769,62 @@ int get_member(dg_ctx *c, int member, double *const u[4]) {
     return DG_OK;
 }
 
+// Asynchronous copy-out of member 0: an FP64 snapshot of the state on the
+// solver stream (after the work already enqueued there), then its copy to
+// `host` on the side stream while the solver stream goes on.
+int get_state_async(dg_ctx *c, double *host, long long *ticket) {
+    if (!c || !host || !ticket) return fail(DG_ERR_ARG, "null argument");
+    CK(cudaSetDevice(c->device));
+    if (!c->save_stream) {
+        CK(cudaStreamCreateWithFlags(&c->save_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            CK(cudaEventCreateWithFlags(&c->snap_ready[k], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&c->snap_done[k], cudaEventDisableTiming));
+        }
+    }
+    const int slot = (int)(c->save_next % 2);
+    // the slot's previous frame must have left the device buffer
+    if (c->save_ticket[slot] >= 0) CK(cudaEventSynchronize(c->snap_done[slot]));
+    const size_t bytes = (size_t)4 * c->ndof * 8;
+    if (!c->d_snap[slot]) {
+        cudaError_t e = cudaMalloc(&c->d_snap[slot], bytes);
+        if (e != cudaSuccess) {
+            c->d_snap[slot] = nullptr;
+            return fail(DG_ERR_CUDA, std::string("cudaMalloc(snapshot): ") + cudaGetErrorString(e));
+        }
+    }
+    double *snap = c->d_snap[slot];
+    for (int f = 0; f < c->nq; ++f) {
+        const long long off = f * c->ndof;
+        const char *src = (const char *)c->d_u + off * c->rsize;
+        if (c->prec == DG_PREC_FP64)
+            CK(cudaMemcpyAsync(snap + off, src, (size_t)c->ndof * 8, cudaMemcpyDeviceToDevice, c->stream));
+        else if (c->mixed)
+            join_kernel<<<1024, 256, 0, c->stream>>>((const float *)src, c->d_ulo + off, snap + off, c->ndof);
+        else
+            uncast_kernel<float><<<1024, 256, 0, c->stream>>>((const float *)src, snap + off, c->ndof);
+        CK(cudaGetLastError());
+    }
+    if (c->nq < 4) CK(cudaMemsetAsync(snap + 3 * c->ndof, 0, (size_t)c->ndof * 8, c->stream));
+    CK(cudaEventRecord(c->snap_ready[slot], c->stream));
+    CK(cudaStreamWaitEvent(c->save_stream, c->snap_ready[slot], 0));
+    CK(cudaMemcpyAsync(host, snap, bytes, cudaMemcpyDeviceToHost, c->save_stream));
+    CK(cudaEventRecord(c->snap_done[slot], c->save_stream));
+    c->save_ticket[slot] = c->save_next;
+    *ticket = c->save_next++;
+    return DG_OK;
+}
+
+int wait_state(dg_ctx *c, long long ticket) {
+    if (!c) return fail(DG_ERR_ARG, "null context");
+    if (ticket < 0 || ticket >= c->save_next) return fail(DG_ERR_ARG, "unknown ticket");
+    CK(cudaSetDevice(c->device));
+    const int slot = (int)(ticket % 2);
+    // a later ticket on the same slot waited for this one before reusing it
+    if (c->save_ticket[slot] == ticket) CK(cudaEventSynchronize(c->snap_done[slot]));
+    return DG_OK;
+}
+
 // Uploads a source set: entries (member, node, source, weight) grouped by
 // state value, sources of a value kept in order.
 int upload_sources(dg_ctx *c, int nsrc, const double *params, const std::vector<long long> &at_of_entry,
@@ -818,6 +884,10 @@ int dg_set_state(dg_ctx *c, const double *const u[4]) {
 }
 
 int dg_get_state(dg_ctx *c, double *const u[4]) { return get_member(c, 0, u); }
+
+int dg_get_state_async(dg_ctx *c, double *host, long long *ticket) { return get_state_async(c, host, ticket); }
+
+int dg_wait_state(dg_ctx *c, long long ticket) { return wait_state(c, ticket); }
 
 int dg_set_state_member(dg_ctx *c, int member, const double *const u[4]) { return set_member(c, member, u); }
 

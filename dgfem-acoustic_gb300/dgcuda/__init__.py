@@ -144,6 +144,8 @@ def _declare(L: C.CDLL) -> None:
         "dg_profile_steps": (C.c_int, [vp, P_d, C.c_double, C.c_int, C.POINTER(KernelTimes)]),
         "dg_monitors": (C.c_int, [vp, P_d, P_d, C.POINTER(C.c_longlong)]),
         "dg_error_vs": (C.c_int, [vp, C.c_int, vp, C.c_int, P_d, C.POINTER(C.c_longlong)]),
+        "dg_get_state_async": (C.c_int, [vp, P_d, C.POINTER(C.c_longlong)]),
+        "dg_wait_state": (C.c_int, [vp, C.c_longlong]),
         "dg_synchronize": (C.c_int, [vp]),
         "dg_info": (C.c_int, [vp, C.POINTER(C.c_longlong), P_i, C.POINTER(C.c_longlong)]),
         "dg_curved_info": (C.c_int, [vp, P_i, P_i, P_i]),
@@ -221,6 +223,21 @@ def _declare(L: C.CDLL) -> None:
         fn = getattr(L, name)
         fn.restype = res
         fn.argtypes = args
+
+
+def pinned_array(shape) -> np.ndarray:
+    """A float64 array in pinned host memory (dg_host_alloc), released with
+    dg_host_free when the array is garbage collected: the buffer to give
+    Solver.get_state_async for the copy to overlap the next steps."""
+    import weakref
+
+    n = int(np.prod(shape))
+    p = lib().dg_host_alloc(n * 8)
+    if not p:
+        raise DGError(-7, lib().dg_last_error().decode(errors="replace"))
+    buf = (C.c_double * n).from_address(p)
+    weakref.finalize(buf, lib().dg_host_free, C.c_void_p(p))
+    return np.ctypeslib.as_array(buf).reshape(shape)
 
 
 def _dptr(a: np.ndarray):
@@ -616,6 +633,20 @@ class Solver:
         if code not in (0, -4):
             _check(code)
         return e.value, list(l2), bad.value
+
+    def get_state_async(self, out: np.ndarray) -> int:
+        """Starts the copy-out of member 0 into out ([4][ndof] float64,
+        contiguous, ideally in pinned memory: see pinned_array) and returns
+        a ticket for wait_state; out must stay alive until then."""
+        if not (isinstance(out, np.ndarray) and out.dtype == np.float64 and out.shape == (4, self.ndof)
+                and out.flags["C_CONTIGUOUS"] and out.flags["WRITEABLE"]):
+            raise ValueError(f"output must be a writeable contiguous float64 array of shape (4, {self.ndof})")
+        t = C.c_longlong()
+        _check(lib().dg_get_state_async(self._h, _dptr(out), C.byref(t)))
+        return t.value
+
+    def wait_state(self, ticket: int) -> None:
+        _check(lib().dg_wait_state(self._h, ticket))
 
     def error_vs(self, ref: "Solver", member: int = 0, ref_member: int = 0) -> tuple[list[float], int]:
         """FP64 relative L2 error per field of this context's state (batch

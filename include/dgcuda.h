@@ -17,7 +17,9 @@
  *                  (src/Mesh.cpp:500-539), Mesh::getElFlux (src/Mesh.cpp:548-557),
  *                  Mesh::getElStiffVector (src/Mesh.cpp:476-489), and the RK
  *                  combination (src/solver.cpp:261-285); t += dt.
- *   dg_get_state   the copy-out at save steps (src/solver.cpp:226-235).
+ *   dg_get_state   the copy-out at save steps (src/solver.cpp:226-235);
+ *                  dg_get_state_async / dg_wait_state overlap it with the
+ *                  next steps.
  *   dg_monitors    no counterpart: FP64 discrete energy, L2 norms, NaN check.
  *   dg_error_vs    no counterpart: FP64 relative L2 error between two states.
  *
@@ -132,6 +134,19 @@ void dg_destroy(dg_ctx *ctx);
  * element-major (u[q][el*el_num_nodes + n]).  In 2D vz must be zero. */
 int dg_set_state(dg_ctx *ctx, const double *const u[4]);
 int dg_get_state(dg_ctx *ctx, double *const u[4]);
+
+/* Asynchronous copy-out for save steps (replaces the blocking copy of
+ * src/solver.cpp:226-235 at each timeRate): the state of member 0, as it is
+ * after the work already enqueued, is snapshotted in FP64 on the solver
+ * stream and copied to host[4*num_el*el_num_nodes] (fields p, vx, vy, vz one
+ * after the other; vz = 0 in 2D) on a side stream, so the following steps
+ * run while the frame crosses the host link.  Returns at once with a ticket;
+ * dg_wait_state(ticket) blocks until that frame is in host.  host must stay
+ * valid until then, and should be pinned (dg_host_alloc) for the copy to
+ * overlap: a pageable buffer makes the call wait for the copy.  Two frames
+ * can be in flight; a third call first waits for the oldest. */
+int dg_get_state_async(dg_ctx *ctx, double *host, long long *ticket);
+int dg_wait_state(dg_ctx *ctx, long long ticket);
 
 /* Hard sources: for source s, nodes dof_idx[offsets[s] .. offsets[s+1]) get
  * p = amp*sin(2*pi*freq*t + phase) while t < duration, at the start of each

@@ -64,3 +64,36 @@ def test_pinned_and_pageable_transfers_agree(precision):
     finally:
         for b in bufs:
             b.free()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "mixed"])
+def test_async_copy_out_frames_equal_blocking_copies(prec):
+    """dg_get_state_async snapshots the state after the work already
+    enqueued and copies it out on a side stream while later steps run: three
+    frames (two in pinned memory, one pageable; the third call reuses the
+    first slot) equal the blocking dg_get_state of a second context taken at
+    the same steps, bit for bit."""
+    mesh = D.Mesh.box_tet(3, 2, 2, order=3, side_names=("Absorbing", "Reflecting") * 3)
+    pre = D.Precomp(mesh)
+    v0 = (50.0, 0.0, 0.0)
+    dt = D.cfl_dt(pre, 340.0, v0)
+    u0 = pre.initial_state([(0, 0.5, 0.5, 0.5, 0.02, 1.0)])
+    a = D.Solver(pre, 340.0, 1.225, v0, precision=prec, flux="upwind")
+    b = D.Solver(pre, 340.0, 1.225, v0, precision=prec, flux="upwind")
+    a.set_state(u0)
+    b.set_state(u0)
+    outs = [D.pinned_array((4, pre.ndof)), D.pinned_array((4, pre.ndof)), np.empty((4, pre.ndof))]
+    tickets, want = [], []
+    t = tb = 0.0
+    for k in range(3):
+        t = a.rk4_steps(t, dt, 5)
+        tickets.append(a.get_state_async(outs[k]))
+        tb = b.rk4_steps(tb, dt, 5)
+        want.append(b.get_state().copy())
+    a.rk4_steps(t, dt, 7)  # more work after the last save
+    for tk in reversed(tickets):
+        a.wait_state(tk)
+    for k in range(3):
+        assert np.array_equal(outs[k], want[k]), k
+    with pytest.raises(D.DGError):
+        a.wait_state(99)
