@@ -232,9 +232,7 @@ __device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned c
 
 // Issues the cp.async gathers of the neighbour traces of a tile's interior
 // face slots (reads the tile's connectivity words from buffer cb); the
-// calling threads take tasks first, first + stride, ...  Neighbours inside
-// the tile are skipped: their traces are read from the tile's own state in
-// shared memory (about half of the interior faces of a hex-split mesh).
+// calling threads take tasks first, first + stride, ...
 template <int DIM, int P, int KIND>
 __device__ __forceinline__ void issue_neighbour_copies(const MixedArgs &a, unsigned char *smem, long long ebase,
                                                        long long moff, int cb, int first, int stride) {
@@ -250,7 +248,6 @@ __device__ __forceinline__ void issue_neighbour_copies(const MixedArgs &a, unsig
         if (ebase + le >= a.K) continue;
         const int2 cn = sConn[le * NF + lf];
         if (((cn.y >> 5) & 3) != kKindInterior) continue;
-        if ((unsigned long long)((long long)cn.x - ebase) < (unsigned long long)ELEMS) continue;
         const int nlf = cn.y & 3, pm = (cn.y >> 2) & 7;
         const long long nb = (long long)cn.x * NP + sFmask[nlf * NFP + sPerm[pm * NFP + k]];
 #pragma unroll
@@ -275,7 +272,6 @@ __device__ __forceinline__ void build_rows(const MixedArgs &a, unsigned char *sm
     const int2 *sConn = reinterpret_cast<const int2 *>(smem + MS::OFF_CONN + cb * MS::CONN_BYTES);
     const float4 *sFgeo = reinterpret_cast<const float4 *>(smem + MS::OFF_FGEO);
     const uint8_t *sFmask = smem + MS::OFF_TAB;
-    const uint8_t *sPerm = sFmask + NF * NFP;
     // 2a. contravariant fluxes, one task per element node
     for (int task = first; task < ELEMS * NP; task += stride) {
         const int le = task / NP, j = task - le * NP;
@@ -327,23 +323,8 @@ __device__ __forceinline__ void build_rows(const MixedArgs &a, unsigned char *sm
             for (int x = 0; x < DIM; ++x) vn0 = fmaf(a.v0[x], n[x], vn0);
             const int kind = (cn.y >> 5) & 3;
             if (kind == kKindInterior) {
-                float o[4];
-                const long long nl = (long long)cn.x - ebase;
-                if ((unsigned long long)nl < (unsigned long long)ELEMS) {
-                    // neighbour inside the tile: its trace is in the state tile
-                    const int nlf = cn.y & 3, pm = (cn.y >> 2) & 7;
-                    const int nv = sFmask[nlf * NFP + sPerm[pm * NFP + k]];
-#pragma unroll
-                    for (int f = 0; f < NQ; ++f) o[f] = sQ[(f * ELEMS + (int)nl) * QS + nv];
-#pragma unroll
-                    for (int f = NQ; f < 4; ++f) o[f] = 0.0f;
-                } else {
-                    const float4 o4 = sNbr[task];
-                    o[0] = o4.x;
-                    o[1] = o4.y;
-                    o[2] = o4.z;
-                    o[3] = o4.w;
-                }
+                const float4 o4 = sNbr[task];
+                const float o[4] = {o4.x, o4.y, o4.z, o4.w};
                 const float tau = (cn.y & 128) ? -1.0f : 1.0f;
                 const float sp = own[0] + o[0];
                 float svn = 0.0f;
