@@ -40,6 +40,7 @@ struct MixedKernelSet {
     const void *euler = nullptr;  // forward-Euler step kernel
     int elems_per_tile = 0;
     int threads = 0;
+    int pipes = 1;  // independent tile pipelines per CTA
     size_t smem = 0;
     int npad = 0;
     // builds the shared-memory image of the sliced operator and its row
@@ -49,7 +50,8 @@ struct MixedKernelSet {
 
 // masked: the variant for meshes with curved elements (MixedArgs::blist and
 // cmask in use).  kind: 0 = exact fixed-point BF16 slices, 1 = 3xTF32.
-bool get_mixed_kernels(int dim, int order, bool masked, int kind, MixedKernelSet *out);
+// pipes: tile pipelines per CTA, 0 = two where they fit, else one.
+bool get_mixed_kernels(int dim, int order, bool masked, int kind, int pipes, MixedKernelSet *out);
 
 // Arguments of the mixed-precision stage kernels.
 struct MixedArgs {

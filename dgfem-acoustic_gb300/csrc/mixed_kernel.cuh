@@ -48,7 +48,11 @@ namespace dgk {
 // kind::tf32 MMAs, FP32 accumulation).
 constexpr int kTcBf16x4 = 0, kTcTf32x3 = 1;
 
-template <int DIM, int P, int KIND = kTcBf16x4>
+// HALVES = 2: the CTA runs two independent tile pipelines (one per half of
+// its warps), each with half of the tensor memory and its own shared-memory
+// region; the operator image is shared.  While one pipeline waits at a
+// barrier or on its MMAs, the other's warps issue.
+template <int DIM, int P, int KIND = kTcBf16x4, int HALVES = 1>
 struct MixedShape {
     using S = Shape<DIM, P>;
     static constexpr bool TF = KIND == kTcTf32x3;
@@ -61,7 +65,7 @@ struct MixedShape {
     static constexpr int NSLICE = TF ? 2 : 4;       // parts of each operand
     static constexpr int NPAD = (NP + 15) / 16 * 16;
     static constexpr int ELEMS = 128 / NQ;          // elements per tile
-    static constexpr int TMEM_COLS = 512;
+    static constexpr int TMEM_COLS = 512 / HALVES;  // tensor-memory columns of one pipeline
     // Level scheme (where it fits): one accumulator per level L = i+j of the
     // slice pairs (0..3).  The B slices of a K-step lie side by side along N,
     // so A slice i meets B slices 0..3-i in one MMA of N = (4-i) x NPAD,
@@ -96,7 +100,9 @@ struct MixedShape {
     // shared memory layout (bytes)
     static constexpr int r16(int x) { return (x + 15) / 16 * 16; }
     static constexpr int OFF_B = 0;                                   // sliced operator image
-    static constexpr int OFF_Q = OFF_B + BBYTES;                      // state tile [f][le][QS]
+    // pipeline 0's region starts here; pipeline h's at + h * HSTRIDE
+    static constexpr int HBASE = r16(OFF_B + BBYTES);
+    static constexpr int OFF_Q = HBASE;                               // state tile [f][le][QS]
     static constexpr int OFF_NBR = r16(OFF_Q + NQ * ELEMS * QS * 4);  // neighbour traces [task][4]
     static constexpr int OFF_A = r16(OFF_NBR + ELEMS * NSLOT * 16);   // FP32 A rows [128][KSTR]
     static constexpr int OFF_GEO = OFF_A + 128 * KSTR * 4;            // [le][DIM*DIM] floats
@@ -114,15 +120,19 @@ struct MixedShape {
     // into them start after it).
     static constexpr int OUT_FLOATS = 2 * NQ * ELEMS * NP;
     static constexpr int OFF_OUT_OWN = r16(OFF_EB + NPAD * 4);
-    static constexpr bool OUT_OWN = OFF_OUT_OWN + OUT_FLOATS * 4 + 16 <= 227 * 1024;
+    static constexpr bool OUT_OWN =
+        HBASE + HALVES * (r16(OFF_OUT_OWN + OUT_FLOATS * 4 + 16) - HBASE) <= 227 * 1024;
     static constexpr bool OUT_ALIAS = !OUT_OWN && OUT_FLOATS * 4 <= OFF_A - OFF_Q;
     static constexpr bool OVERLAP = OUT_OWN || OUT_ALIAS;
     static constexpr int OFF_OUT = OUT_OWN ? OFF_OUT_OWN : OFF_Q;
     static constexpr int OFF_BAR = OUT_OWN ? r16(OFF_OUT + OUT_FLOATS * 4) : OFF_EB + NPAD * 4;
-    static constexpr int SMEM = OFF_BAR + 16;
+    static constexpr int HSTRIDE = r16(OFF_BAR + 16) - HBASE;         // bytes of one pipeline's region
+    static constexpr int SMEM = HBASE + HALVES * HSTRIDE;
+    // the shape runs when both tensor memory and shared memory suffice
+    static constexpr bool RUNS = FITS && SMEM <= 227 * 1024 && (HALVES == 1 || OVERLAP);
     // the epilogue stages the tile's two output arrays in the A-row region
     static_assert(2 * NQ * ELEMS * NP <= 128 * KSTR, "output staging fits in the A-row region");
-    static_assert(SMEM <= 227 * 1024, "tile does not fit in shared memory");
+    static_assert(HALVES == 2 || SMEM <= 227 * 1024, "tile does not fit in shared memory");
     static_assert(NPASS * KPASS >= KSTEPS && (NPASS == 1 || LEVELS), "the passes cover every K-step");
     static_assert(!LEVELS || (ACC + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256), "level accumulators fit");
     static_assert(!OUT_ALIAS || (OFF_Q + OUT_FLOATS * 4 <= OFF_A && OFF_NBR > OFF_Q && OFF_A > OFF_NBR),
@@ -384,13 +394,30 @@ __device__ __forceinline__ void row_maxima(unsigned char *smem, int first, int s
     }
 }
 
-template <int DIM, int P, int STAGE, int NWG, bool MASKED, int KIND>
-__global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedArgs a) {
-    using MS = MixedShape<DIM, P, KIND>;
+// Barrier of one tile pipeline: the whole CTA when it runs one pipeline, else
+// named barrier `id` over that pipeline's `count` threads.
+template <int HALVES>
+__device__ __forceinline__ void pipe_sync(int id, int count) {
+    if constexpr (HALVES == 1) {
+        __syncthreads();
+    } else {
+        asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+    }
+}
+
+template <int DIM, int P, int STAGE, int NWG, bool MASKED, int KIND, int HALVES>
+__global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(const MixedArgs a) {
+    using MS = MixedShape<DIM, P, KIND, HALVES>;
+    using MS1 = MixedShape<DIM, P, KIND, 1>;  // the helpers' layout: the same region offsets
+    static_assert(MS1::OFF_A == MS::OFF_A && MS1::OFF_MAX == MS::OFF_MAX && MS1::OFF_TAB == MS::OFF_TAB &&
+                      MS1::OFF_EB == MS::OFF_EB && MS1::OFF_CONN == MS::OFF_CONN && MS1::OFF_FGEO == MS::OFF_FGEO,
+                  "per-pipeline regions keep the one-pipeline offsets");
+    static_assert(MS::RUNS, "tile does not fit");
     constexpr int NP = MS::NP, NQ = MS::NQ;
     constexpr int ELEMS = MS::ELEMS, KTOT = MS::KTOT, KSTEPS = MS::KSTEPS, KSTR = MS::KSTR;
     constexpr int NPAD = MS::NPAD, ACOLS = MS::ACOLS;
-    constexpr int NT = 128 * NWG;                       // threads
+    constexpr int NT = 128 * NWG;                       // threads of one pipeline
+    constexpr int NTC = NT * HALVES;                    // threads of the CTA
     constexpr int KSP = (KSTEPS + NWG - 1) / NWG;       // K-steps sliced per warp group
     constexpr int NPP = (NP + NWG - 1) / NWG;           // output nodes per warp group in the epilogue
     constexpr int NCH = (NPP + 7) / 8;                  // 8-column tensor-memory loads per accumulator
@@ -402,18 +429,24 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     static_assert(MS::ACC + (MS::NACC - 1) * NPAD + (NWG - 1) * NPP + 8 * NCH <= MS::TMEM_COLS,
                   "epilogue loads stay inside the allocation");
     static_assert(ELEMS <= 64, "curved-element mask holds 64 elements per tile");
-    extern __shared__ __align__(1024) unsigned char smem[];
+    extern __shared__ __align__(1024) unsigned char smem_cta[];
+    // pipeline of this thread, its index and warp inside the pipeline, and
+    // its pipeline's shared-memory region (the operator image is shared)
+    const int pipe = HALVES == 1 ? 0 : (int)(threadIdx.x / NT);
+    const int tid = (int)threadIdx.x - pipe * NT, warp = tid >> 5, lane = tid & 31;
+    unsigned char *const smem = smem_cta + pipe * MS::HSTRIDE;
+    // named barriers of this pipeline: all its threads, and all but warp 0
+    const int bar_all = 1 + 2 * pipe, bar_rest = 2 + 2 * pipe;
     float *sA = reinterpret_cast<float *>(smem + MS::OFF_A);
     float *sMax = reinterpret_cast<float *>(smem + MS::OFF_MAX);
     uint8_t *sTab = smem + MS::OFF_TAB;
     int *sEb = reinterpret_cast<int *>(smem + MS::OFF_EB);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + MS::OFF_BAR);
-    uint32_t *sTmem = reinterpret_cast<uint32_t *>(smem + MS::OFF_BAR + 8);
+    uint32_t *sTmem = reinterpret_cast<uint32_t *>(smem_cta + MS::OFF_BAR + 8);  // pipeline 0's slot
     int *sFail = reinterpret_cast<int *>(smem + MS::OFF_BAR + 12);
 
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    if (warp == 0) {
-        dgtc::tmem_alloc(sTmem, MS::TMEM_COLS);
+    if (threadIdx.x < 32) {
+        dgtc::tmem_alloc(sTmem, MS::TMEM_COLS * HALVES);
         dgtc::tmem_relinquish();
     }
     if (tid == 0) {
@@ -423,8 +456,8 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     }
     {
         const uint4 *src = reinterpret_cast<const uint4 *>(a.bimg);
-        uint4 *dst = reinterpret_cast<uint4 *>(smem + MS::OFF_B);
-        for (int k = tid; k < MS::BBYTES / 16; k += NT) dst[k] = src[k];
+        uint4 *dst = reinterpret_cast<uint4 *>(smem_cta + MS::OFF_B);
+        for (int k = threadIdx.x; k < MS::BBYTES / 16; k += NTC) dst[k] = src[k];
         for (int k = tid; k < Shape<DIM, P>::NTAB; k += NT) sTab[k] = a.tabs[k];
         for (int k = tid; k < NPAD; k += NT) sEb[k] = a.beb[k];
     }
@@ -432,9 +465,10 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     dgtc::fence_before_sync();
     __syncthreads();
     dgtc::fence_after_sync();
-    const uint32_t tbase = *sTmem;
+    // this pipeline's tensor-memory columns
+    const uint32_t tbase = *sTmem + (uint32_t)(pipe * MS::TMEM_COLS);
     const uint32_t idesc = dgtc::idesc_bf16_f32(128, NPAD);
-    const uint32_t sB = dgtc::smem_u32(smem + MS::OFF_B);
+    const uint32_t sB = dgtc::smem_u32(smem_cta + MS::OFF_B);
     // row of this thread in phases 3 and 5, and which part of the row's work
     // (K-steps when slicing, output nodes in the epilogue) its warp group takes
     const int r = (warp & 3) * 32 + lane;
@@ -468,21 +502,24 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
         eb = (long long)blk * ELEMS;
         mo = (long long)(t32 - et * nbu) * a.bstride;
     };
-    if ((long long)blockIdx.x < ntiles) {
+    // tiles of this pipeline: tfirst, tfirst + tstride, ...
+    const long long tfirst = (long long)blockIdx.x * HALVES + pipe;
+    const long long tstride = (long long)gridDim.x * HALVES;
+    if (tfirst < ntiles) {
         long long eb, mo;
-        tile_base(blockIdx.x, eb, mo);
+        tile_base(tfirst, eb, mo);
         issue_conn_copies<DIM, P, KIND>(a, smem, eb, 0, tid, NT);
         issue_tile_copies<DIM, P, KIND>(a, smem, eb, mo, vec, tid, NT);
         dgtc::cp_async_wait_all();
-        __syncthreads();
+        pipe_sync<HALVES>(bar_all, NT);
         issue_neighbour_copies<DIM, P, KIND>(a, smem, eb, mo, 0, tid, NT);
         dgtc::cp_async_commit();
         if constexpr (OVERLAP) {
             // the first tile's rows now; every later tile's while its
             // predecessor's MMAs run
             dgtc::cp_async_wait_all();
-            __syncthreads();
-            const long long T1 = (long long)blockIdx.x + gridDim.x;
+            pipe_sync<HALVES>(bar_all, NT);
+            const long long T1 = tfirst + tstride;
             if (T1 < ntiles) {
                 long long e1, m1;
                 tile_base(T1, e1, m1);
@@ -490,26 +527,26 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             }
             dgtc::cp_async_commit();
             build_rows<DIM, P, KIND>(a, smem, eb, 0, tid, NT);
-            __syncthreads();
+            pipe_sync<HALVES>(bar_all, NT);
             // the row maxima of every later tile are taken right after its
             // rows, while the previous tile's MMAs run (3xTF32 needs none)
             if constexpr (!MS::TF) row_maxima<DIM, P, NWG, KIND>(smem, tid, NT);
         }
     }
     int cb = 0;  // connectivity buffer of the current tile
-    for (long long tile = blockIdx.x; tile < ntiles && alive; tile += gridDim.x, cb ^= 1) {
+    for (long long tile = tfirst; tile < ntiles && alive; tile += tstride, cb ^= 1) {
         long long ebase, moff;
         tile_base(tile, ebase, moff);
-        const long long next = tile + gridDim.x;
+        const long long next = tile + tstride;
         long long nebase = 0, nmoff = 0;
         if (next < ntiles) tile_base(next, nebase, nmoff);
         if constexpr (!OVERLAP) {
             dgtc::cp_async_wait_all();
-            __syncthreads();
+            pipe_sync<HALVES>(bar_all, NT);
             if (next < ntiles) issue_conn_copies<DIM, P, KIND>(a, smem, nebase, cb ^ 1, tid, NT);
             dgtc::cp_async_commit();
             build_rows<DIM, P, KIND>(a, smem, ebase, cb, tid, NT);
-            __syncthreads();
+            pipe_sync<HALVES>(bar_all, NT);
         }
         // the tile's element data are consumed: start copying the next tile's
         // (with the overlap, warp 0 copies nothing for the next tile: it only
@@ -548,7 +585,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
                 for (int k = ks0 * 16; k < ks1 * 16 && k < KTOT; ++k) m = fmaxf(m, fabsf(arow[k]));
             sMax[part * 128 + r] = m;
         }
-        __syncthreads();
+        pipe_sync<HALVES>(bar_all, NT);
         if (next < ntiles && (!OVERLAP || warp > 0))
             issue_neighbour_copies<DIM, P, KIND>(a, smem, nebase, nmoff, cb ^ 1, OVERLAP ? tid - 32 : tid,
                                            OVERLAP ? NT - 32 : NT);
@@ -618,7 +655,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             }
             dgtc::tmem_st_wait();
             dgtc::fence_before_sync();
-            __syncthreads();
+            pipe_sync<HALVES>(bar_all, NT);
 
             // 4. tensor-core contraction, issued by thread 0 K-step by K-step
             if (tid == 0 && !*sFail) {
@@ -669,8 +706,8 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             // next tile's rows (barrier 1 spans those warps only)
             if (next < ntiles && warp > 0) {
                 dgtc::cp_async_wait_all();
-                asm volatile("bar.sync 1, %0;" ::"r"(NT - 32) : "memory");
-                const long long next2 = next + gridDim.x;
+                asm volatile("bar.sync %0, %1;" ::"r"(bar_rest), "r"(NT - 32) : "memory");
+                const long long next2 = next + tstride;
                 if (next2 < ntiles) {
                     long long e2, m2;
                     tile_base(next2, e2, m2);
@@ -678,7 +715,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
                 }
                 build_rows<DIM, P, KIND>(a, smem, nebase, cb ^ 1, tid - 32, NT - 32);
                 if constexpr (!MS::TF) {
-                    asm volatile("bar.sync 1, %0;" ::"r"(NT - 32) : "memory");
+                    asm volatile("bar.sync %0, %1;" ::"r"(bar_rest), "r"(NT - 32) : "memory");
                     row_maxima<DIM, P, NWG, KIND>(smem, tid - 32, NT - 32);
                 }
             }
@@ -689,7 +726,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
         //    warp group g takes output nodes [g*NPP, (g+1)*NPP)
         if (!dgtc::mbar_wait_bounded(bar, phase, 1u << 30)) *sFail = 1;
         phase ^= 1u;
-        __syncthreads();
+        pipe_sync<HALVES>(bar_all, NT);
         if (*sFail) {
             alive = false;
         } else {
@@ -763,7 +800,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
                     }
                 }
             }
-            __syncthreads();
+            pipe_sync<HALVES>(bar_all, NT);
             const unsigned long long cm = MASKED ? a.cmask[ebase / ELEMS] : 0ull;
             if (vec && ebase + ELEMS <= a.K && cm == 0ull) {
                 constexpr int W = ELEMS * NP / 4;
@@ -784,7 +821,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
             }
         }
         dgtc::fence_before_sync();
-        __syncthreads();
+        pipe_sync<HALVES>(bar_all, NT);
     }
     // no copy may still be writing shared memory when the CTA exits
     dgtc::cp_async_wait_all();
@@ -796,7 +833,7 @@ __global__ void __launch_bounds__(128 * NWG, 1) mixed_stage_kernel(const MixedAr
     }
     dgtc::fence_after_sync();
     __syncthreads();
-    if (warp == 0) dgtc::tmem_dealloc(tbase, MS::TMEM_COLS);
+    if (threadIdx.x < 32) dgtc::tmem_dealloc(*sTmem, MS::TMEM_COLS * HALVES);
 }
 
 }  // namespace dgk

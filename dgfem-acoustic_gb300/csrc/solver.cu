@@ -475,8 +475,12 @@ static int dg_create_batch_impl(const dg_mesh_desc *m, const dg_phys_desc *ph, c
         free_ctx(c);
         return fail(DG_ERR_UNSUPPORTED, "no kernel compiled for this order");
     }
+    if (opts.tc_pipelines < 0 || opts.tc_pipelines > 2) {
+        free_ctx(c);
+        return fail(DG_ERR_ARG, "tc_pipelines must be 0, 1 or 2");
+    }
     if (c->mixed && !dgk::get_mixed_kernels(dim, m->order, lay.curved.C > 0, c->prec == DG_PREC_TF32X3 ? 1 : 0,
-                                            &c->mks)) {
+                                            opts.tc_pipelines, &c->mks)) {
         free_ctx(c);
         return fail(DG_ERR_UNSUPPORTED, "the tensor-core forms support orders 1-4 in 3D and 1-5 in 2D");
     }
@@ -570,13 +574,15 @@ static int dg_create_batch_impl(const dg_mesh_desc *m, const dg_phys_desc *ph, c
                          "cudaFuncSetAttribute(mixed)"))
                     break;
             if (rc != DG_OK) break;
-            // one CTA per SM: each owns the SM's tensor memory
+            // one CTA per SM: each owns the SM's tensor memory and runs
+            // mks.pipes tile pipelines
             long long mtiles = (long long)((K + c->mks.elems_per_tile - 1) / c->mks.elems_per_tile) * nbatch;
             if (mtiles >= (1LL << 31)) {
                 rc = fail(DG_ERR_UNSUPPORTED, "mesh x batch too large for the mixed form's tile index");
                 break;
             }
-            c->grid = (int)std::max(1LL, std::min(mtiles, (long long)nsm));
+            const long long ctas = (mtiles + c->mks.pipes - 1) / c->mks.pipes;
+            c->grid = (int)std::max(1LL, std::min(ctas, (long long)nsm));
         }
         if (lay.curved.C > 0) {
             const dg::CurvedLayout &cv = lay.curved;
@@ -1239,6 +1245,13 @@ int dg_info(dg_ctx *c, long long *dofs, int *fields, long long *state_bytes) {
     if (dofs) *dofs = c->ndof;
     if (fields) *fields = c->nq;
     if (state_bytes) *state_bytes = c->bstride * c->nbatch * (long long)c->rsize * 4;
+    return DG_OK;
+}
+
+int dg_tc_info(dg_ctx *c, int *pipelines, int *tile_elems) {
+    if (!c) return fail(DG_ERR_ARG, "null context");
+    if (pipelines) *pipelines = c->mixed ? c->mks.pipes : 0;
+    if (tile_elems) *tile_elems = c->mixed ? c->mks.elems_per_tile : 0;
     return DG_OK;
 }
 

@@ -90,7 +90,7 @@ class PhysDesc(C.Structure):
 
 class Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("flux_sign", C.c_int), ("device", C.c_int), ("use_graph", C.c_int),
-                ("elems_per_block", C.c_int), ("reserved", C.c_int * 3)]
+                ("elems_per_block", C.c_int), ("tc_pipelines", C.c_int), ("reserved", C.c_int * 2)]
 
 
 class KernelTimes(C.Structure):
@@ -149,6 +149,7 @@ def _declare(L: C.CDLL) -> None:
         "dg_synchronize": (C.c_int, [vp]),
         "dg_info": (C.c_int, [vp, C.POINTER(C.c_longlong), P_i, C.POINTER(C.c_longlong)]),
         "dg_curved_info": (C.c_int, [vp, P_i, P_i, P_i]),
+        "dg_tc_info": (C.c_int, [vp, P_i, P_i]),
         "dgm_set_nodes": (C.c_int, [vp, P_d]),
         "dgm_get_curved": (C.c_int, [vp, P_i, C.POINTER(P_u8)]),
         "dg_host_alloc": (vp, [C.c_ulonglong]),
@@ -508,7 +509,8 @@ class Solver:
     """GPU RK4 right-hand side context (dg_create ... dg_destroy)."""
 
     def __init__(self, pre: Precomp, c0: float, rho0: float, v0=(0.0, 0.0, 0.0), precision: str = "fp64",
-                 flux: str = "reference", use_graph: bool = True, device: int = 0, nbatch: int = 1):
+                 flux: str = "reference", use_graph: bool = True, device: int = 0, nbatch: int = 1,
+                 tc_pipelines: int = 0):
         d = pre.desc()
         ph = PhysDesc(c0, rho0, (C.c_double * 3)(*v0))
         o = Opts()
@@ -517,6 +519,7 @@ class Solver:
         o.flux_sign = {"reference": FLUX_REFERENCE, "upwind": FLUX_UPWIND}[flux]
         o.use_graph = 1 if use_graph else 0
         o.device = device
+        o.tc_pipelines = tc_pipelines
         h = C.c_void_p()
         _check(lib().dg_create_batch(C.byref(d), C.byref(ph), C.byref(o), nbatch, C.byref(h)))
         self._h = h
@@ -667,8 +670,11 @@ class Solver:
         _check(lib().dg_info(self._h, C.byref(d), C.byref(f), C.byref(b)))
         nc, ng, ngf = C.c_int(), C.c_int(), C.c_int()
         _check(lib().dg_curved_info(self._h, C.byref(nc), C.byref(ng), C.byref(ngf)))
+        tp, te = C.c_int(), C.c_int()
+        _check(lib().dg_tc_info(self._h, C.byref(tp), C.byref(te)))
         return {"dofs_per_field": d.value, "fields": f.value, "state_bytes": b.value, "curved": nc.value,
-                "curved_points": ng.value, "curved_face_points": ngf.value}
+                "curved_points": ng.value, "curved_face_points": ngf.value, "tc_pipelines": tp.value,
+                "tc_tile_elems": te.value}
 
 
 def min_inradius(pre: Precomp) -> float:

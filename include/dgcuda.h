@@ -111,7 +111,9 @@ typedef struct dg_opts {
     int device;      /* CUDA device ordinal */
     int use_graph;   /* capture step chunks in CUDA graphs (1) or launch directly (0) */
     int elems_per_block; /* 0 = built-in choice */
-    int reserved[3];
+    int tc_pipelines;    /* tensor-core forms: independent tile pipelines per CTA,
+                          * 0 = two where they fit (else one), 1, or 2 */
+    int reserved[2];
 } dg_opts;
 
 /* Per-kernel timing of dg_profile_steps (CUDA events on the solver stream). */
@@ -217,6 +219,10 @@ int dg_synchronize(dg_ctx *ctx);
 /* Sizes and the device data the context holds (for callers that time or
  * inspect it): number of DOFs per field, fields evolved, bytes of state. */
 int dg_info(dg_ctx *ctx, long long *dofs_per_field, int *fields, long long *state_bytes);
+
+/* Tensor-core forms: tile pipelines per CTA of the context's stage kernels
+ * and elements per tile (both 0 for the FP64 and FP32 forms). */
+int dg_tc_info(dg_ctx *ctx, int *pipelines, int *tile_elems);
 
 /* Curved elements of the context (run by the per-point kernel) and the
  * points of the element and face rules they use. */

@@ -224,3 +224,26 @@ def test_euler_then_rk4_in_one_context(precision, tol):
     assert t == tr
     for q in range(3):
         assert rel_l2(got[q], ref[q]) <= tol
+
+
+@pytest.mark.parametrize("dim,order,nbatch", [(3, 3, 1), (3, 2, 3), (2, 3, 1), (2, 5, 2), (3, 1, 1)])
+def test_mixed_form_one_and_two_tile_pipelines_agree(dim, order, nbatch):
+    """The tensor-core kernels run one tile pipeline per CTA or two (each with
+    half of the warps and of the tensor memory, where that fits).  Both do
+    the same exact sums on every tile, so the states are bit-identical."""
+    mesh = make_mesh(dim, order, "mixed")
+    pre = D.Precomp(mesh)
+    v0 = (30.0, -20.0, 10.0 if dim == 3 else 0.0)
+    dt = D.cfl_dt(pre, C0, v0)
+    u0 = pre.initial_state([(0, *pre.dof_coords().mean(axis=0), 0.02, 1.0)])
+    out = {}
+    for pipes in (1, 2):
+        s = D.Solver(pre, C0, RHO0, v0, precision="mixed", flux="upwind", nbatch=nbatch, tc_pipelines=pipes)
+        assert s.info()["tc_pipelines"] == pipes
+        for m in range(nbatch):
+            s.set_state(u0 * (1.0 + m), member=m)
+        s.rk4_steps(0.0, dt, 9)
+        out[pipes] = [s.get_state(member=m) for m in range(nbatch)]
+        s.close()
+    for m in range(nbatch):
+        assert np.array_equal(out[1][m], out[2][m]), m
