@@ -50,7 +50,7 @@ struct MixedKernelSet {
 
 // masked: the variant for meshes with curved elements (MixedArgs::blist and
 // cmask in use).  kind: 0 = exact fixed-point BF16 slices, 1 = 3xTF32.
-// pipes: tile pipelines per CTA, 0 = two where they fit, else one.
+// pipes: tile pipelines per CTA, 0 or 1 = one, 2 = two where they fit.
 bool get_mixed_kernels(int dim, int order, bool masked, int kind, int pipes, MixedKernelSet *out);
 
 // Arguments of the mixed-precision stage kernels.

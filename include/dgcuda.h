@@ -112,7 +112,8 @@ typedef struct dg_opts {
     int use_graph;   /* capture step chunks in CUDA graphs (1) or launch directly (0) */
     int elems_per_block; /* 0 = built-in choice */
     int tc_pipelines;    /* tensor-core forms: independent tile pipelines per CTA,
-                          * 0 = two where they fit (else one), 1, or 2 */
+                          * 0 or 1 = one, 2 = two where tensor and shared memory
+                          * allow (else one; dg_tc_info tells) */
     int reserved[2];
 } dg_opts;
 
