@@ -784,8 +784,9 @@ def parareal_section(D, args, local):
         if lrn is not None:
             lrn.set_inference(mode)
         w0 = time.perf_counter()
-        u, it, hist = D.parareal(pre, C0, RHO0, u0, nsl, sst, dt, tol=args.parareal_tol, max_iter=nsl, learned=lrn,
-                                 flux=FLUX)
+        max_iter = nsl if args.parareal_max_iter <= 0 else min(nsl, args.parareal_max_iter)
+        u, it, hist = D.parareal(pre, C0, RHO0, u0, nsl, sst, dt, tol=args.parareal_tol, max_iter=max_iter,
+                                 learned=lrn, flux=FLUX)
         wall = time.perf_counter() - w0
         err = max(float(np.linalg.norm(u[q] - ref[q]) / np.linalg.norm(ref[q])) for q in range(4))
         out[name] = {"iterations": it, "wall_ms": wall * 1e3, "rel_l2_vs_serial_fp64": err,
@@ -856,6 +857,8 @@ def main():
     ap.add_argument("--parareal-train-steps", type=int, default=100)
     ap.add_argument("--parareal-epochs", type=int, default=10)
     ap.add_argument("--parareal-tol", type=float, default=1e-5)
+    ap.add_argument("--parareal-max-iter", type=int, default=0,
+                    help="parareal iterations at most (0: as many as slices, which reproduces the serial DG)")
     ap.add_argument("--no-curved", action="store_true", help="skip the curved-element section")
     ap.add_argument("--curved-cells", type=int, default=24)
     ap.add_argument("--curved-steps", type=int, default=50)

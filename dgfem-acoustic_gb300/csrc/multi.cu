@@ -45,6 +45,23 @@ struct MultiMesh {
     int pad;
 };
 
+// Copies mesh m's arguments of one stage into shared memory (the CTA's
+// threads read them from there for every tile of that mesh instead of
+// loading the ~150-byte record from global memory per tile).  Called by the
+// whole CTA when its next item belongs to another mesh: the first barrier
+// keeps the previous tile's readers, the second publishes the copy.
+template <typename Real>
+__device__ __forceinline__ void load_mesh_args(const MultiMesh<Real> *meshes, int m, int stage, StageArgs<Real> *dst,
+                                               int tid) {
+    static_assert(sizeof(StageArgs<Real>) % 8 == 0, "copied as 8-byte words");
+    __syncthreads();
+    constexpr int W = (int)(sizeof(StageArgs<Real>) / 8);
+    if (tid < W)
+        reinterpret_cast<unsigned long long *>(dst)[tid] =
+            __ldg(reinterpret_cast<const unsigned long long *>(&meshes[m].st[stage - 1]) + tid);
+    __syncthreads();
+}
+
 // Shared-memory regions (in Real units) chosen by the host from the orders
 // present: operators, tile state, face values; tables follow in bytes.
 struct MultiSmem {
@@ -60,10 +77,14 @@ __global__ void __launch_bounds__(BT) multi_stage_kernel(const MultiMesh<Real> *
     Real *sQ = sOps + sm.ops;
     Real *sFn = sQ + sm.q;
     uint8_t *sTab = reinterpret_cast<uint8_t *>(sFn + sm.fn);
+    __shared__ StageArgs<Real> sArgs;
     const int tid = threadIdx.x;
-    int cur = 0;
+    int cur = 0, curm = -1;
+    int2 wn = blockIdx.x < nitems ? items[blockIdx.x] : make_int2(0, 0);
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const int2 w = items[it];
+        const int2 w = wn;
+        // the next item's load overlaps this tile
+        if (it + (int)gridDim.x < nitems) wn = items[it + gridDim.x];
         const int order = meshes[w.x].order;
         if (order != cur) {
             // every thread has finished the previous item's tile
@@ -78,7 +99,11 @@ __global__ void __launch_bounds__(BT) multi_stage_kernel(const MultiMesh<Real> *
             __syncthreads();
             cur = order;
         }
-        const StageArgs<Real> a = meshes[w.x].st[STAGE - 1];
+        if (w.x != curm) {
+            load_mesh_args(meshes, w.x, STAGE, &sArgs, tid);
+            curm = w.x;
+        }
+        const StageArgs<Real> &a = sArgs;
         switch (order) {
             case 1: stage_tile<3, 1, Real, STAGE, multi_epb(BT, 1)>(a, 0, w.y, sQ, sFn, sOps, sTab, tid); break;
             case 2: stage_tile<3, 2, Real, STAGE, multi_epb(BT, 2)>(a, 0, w.y, sQ, sFn, sOps, sTab, tid); break;
@@ -110,13 +135,21 @@ __global__ void __launch_bounds__(order_epb(P) * multi_np(P))
     Real *sFn = sQ + EPB * S::NP * 4;
     uint8_t *sTab = reinterpret_cast<uint8_t *>(sFn + EPB * S::NSLOT * 4);
     const int tid = threadIdx.x;
+    __shared__ StageArgs<Real> sArgs;
     for (int k = tid; k < S::NOPS; k += NT) sOps[k] = ops[k];
     for (int k = tid; k < S::NTAB; k += NT) sTab[k] = tabs[k];
     __syncthreads();
+    int curm = -1;
+    int2 wn = blockIdx.x < nitems ? items[blockIdx.x] : make_int2(0, 0);
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const int2 w = items[it];
-        const StageArgs<Real> a = meshes[w.x].st[STAGE - 1];
-        stage_tile<3, P, Real, STAGE, EPB>(a, 0, w.y, sQ, sFn, sOps, sTab, tid);
+        const int2 w = wn;
+        // the next item's load overlaps this tile
+        if (it + (int)gridDim.x < nitems) wn = items[it + gridDim.x];
+        if (w.x != curm) {
+            load_mesh_args(meshes, w.x, STAGE, &sArgs, tid);
+            curm = w.x;
+        }
+        stage_tile<3, P, Real, STAGE, EPB>(sArgs, 0, w.y, sQ, sFn, sOps, sTab, tid);
     }
 }
 
