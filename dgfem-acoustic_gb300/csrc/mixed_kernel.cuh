@@ -625,11 +625,7 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
 #pragma unroll
                 for (int h = 0; h < 8; ++h) {
                     const int k = c * 8 + h;
-                    if (k >= KTOT) {
-                        wh[h] = wl[h] = 0u;
-                        continue;
-                    }
-                    const float x = live ? arow[k] : 0.0f;
+                    const float x = (live && k < KTOT) ? arow[k] : 0.0f;
                     const float xh = dgtc::tf32_round(x);
                     wh[h] = __float_as_uint(xh);
                     wl[h] = __float_as_uint(dgtc::tf32_round(x - xh));
@@ -644,14 +640,7 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
 #pragma unroll
                 for (int h = 0; h < 8; ++h) {
                     const int k = c * 16 + 2 * h;
-                    if (k >= KTOT) {
-                        // padding columns of the last K-step (the same for the
-                        // whole warp): zero slices without slicing
-#pragma unroll
-                        for (int sl = 0; sl < 4; ++sl) w[sl][h] = 0u;
-                        continue;
-                    }
-                    const float x0 = live ? arow[k] : 0.0f;
+                    const float x0 = (live && k < KTOT) ? arow[k] : 0.0f;
                     const float x1 = (live && k + 1 < KTOT) ? arow[k + 1] : 0.0f;
                     float m0[4], m1[4];
                     slice4(x0, sc, m0);
