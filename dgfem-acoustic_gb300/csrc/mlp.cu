@@ -447,6 +447,10 @@ struct dg_mlp {
     int bf_cap = 0;
     std::vector<__nv_bfloat16 *> abf;  // abf[l]: BF16 input of layer l
     int *d_err = nullptr;
+    // GEMMs of training: on the tensor cores (3xTF32 split products,
+    // mlp_train_tc.cu) or on the CUDA cores (gemm_kernel)
+    bool gemm_tc = true;
+    int *d_terr = nullptr;  // set when a tensor-core wait of those GEMMs gives up
 };
 
 namespace {
@@ -552,26 +556,54 @@ int mlp_forward_bf16(dg_mlp *n, const float *X, int rows) {
     return DG_OK;
 }
 
+// training: the GEMMs of a training step (forward, gradients), which run on
+// the tensor cores when n->gemm_tc; FP32 inference stays on the CUDA cores
+// (measured faster for its shapes: 0.39 against 0.52 ms for 11,028 rows).
 template <bool TA, bool TB>
-void gemm(cudaStream_t s, int M, int N, int K, const float *A, int lda, const float *B, int ldb, float *C, int ldc,
-          const float *bias, float *gelu_out, int accumulate) {
+int gemm(dg_mlp *n, bool training, int M, int N, int K, const float *A, int lda, const float *B, int ldb, float *C,
+         int ldc, const float *bias, float *gelu_out, int accumulate) {
+    if (training && n->gemm_tc) {
+        if (!n->d_terr) {
+            CK(cudaMalloc(&n->d_terr, sizeof(int)));
+            CK(cudaMemsetAsync(n->d_terr, 0, sizeof(int), n->stream));
+        }
+        const int r = dgk::tc_gemm_tf32x3(n->stream, TA, TB, M, N, K, A, lda, B, ldb, C, ldc, bias, gelu_out,
+                                          accumulate, n->d_terr);
+        if (r != 0) return fail(DG_ERR_CUDA, "tensor-core GEMM launch failed");
+        return DG_OK;
+    }
     dim3 grid((N + GB - 1) / GB, (M + GB - 1) / GB);
-    gemm_kernel<TA, TB><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, gelu_out, accumulate);
+    gemm_kernel<TA, TB><<<grid, 256, 0, n->stream>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, gelu_out, accumulate);
+    return DG_OK;
 }
 
-// Forward pass of `rows` rows of X (device); output in n->d_Y.
-int mlp_forward(dg_mlp *n, const float *X, int rows) {
+// After the stream has been synchronised: DG_ERR_CUDA if a tensor-core wait
+// of the training GEMMs gave up since the last check (the flag is cleared).
+int check_gemm_err(dg_mlp *n) {
+    if (!n->d_terr) return DG_OK;
+    int err = 0;
+    CK(cudaMemcpy(&err, n->d_terr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!err) return DG_OK;
+    CK(cudaMemset(n->d_terr, 0, sizeof(int)));
+    return fail(DG_ERR_CUDA, "tensor-core wait timed out in an MLP GEMM");
+}
+
+// Forward pass of `rows` rows of X (device); output in n->d_Y.  training:
+// the forward pass of a training step.
+int mlp_forward(dg_mlp *n, const float *X, int rows, bool training = false) {
     int rc = ensure_rows(n, rows);
     if (rc != DG_OK) return rc;
     n->A[0] = const_cast<float *>(X);
     for (int l = 0; l < n->layers; ++l) {
         const float *W = n->d_p + n->woff[l], *b = n->d_p + n->boff[l];
+        int rc;
         if (l + 1 < n->layers)
-            gemm<false, false>(n->stream, rows, n->dout[l], n->din[l], n->A[l], n->din[l], W, n->din[l], n->Z[l],
-                               n->dout[l], b, n->A[l + 1], 0);
+            rc = gemm<false, false>(n, training, rows, n->dout[l], n->din[l], n->A[l], n->din[l], W, n->din[l],
+                                    n->Z[l], n->dout[l], b, n->A[l + 1], 0);
         else
-            gemm<false, false>(n->stream, rows, n->dout[l], n->din[l], n->A[l], n->din[l], W, n->din[l], n->d_Y,
-                               n->dout[l], b, nullptr, 0);
+            rc = gemm<false, false>(n, training, rows, n->dout[l], n->din[l], n->A[l], n->din[l], W, n->din[l],
+                                    n->d_Y, n->dout[l], b, nullptr, 0);
+        if (rc != DG_OK) return rc;
     }
     CK(cudaGetLastError());
     return DG_OK;
@@ -579,7 +611,7 @@ int mlp_forward(dg_mlp *n, const float *X, int rows) {
 
 // Loss and gradients (into d_g) of the mean squared error against T (device).
 int mlp_backward(dg_mlp *n, const float *X, const float *T, int rows, double *loss) {
-    int rc = mlp_forward(n, X, rows);
+    int rc = mlp_forward(n, X, rows, true);
     if (rc != DG_OK) return rc;
     const long long ny = (long long)rows * n->nout;
     CK(cudaMemsetAsync(n->d_loss, 0, 8, n->stream));
@@ -588,14 +620,16 @@ int mlp_backward(dg_mlp *n, const float *X, const float *T, int rows, double *lo
     for (int l = n->layers - 1; l >= 0; --l) {
         const int din = n->din[l], dout = n->dout[l];
         // dW = dZ^T A_l  ([dout x din]), db = column sums of dZ
-        gemm<true, true>(n->stream, dout, din, rows, dZ, dout, n->A[l], din, n->d_g + n->woff[l], din, nullptr,
-                         nullptr, 0);
+        rc = gemm<true, true>(n, true, dout, din, rows, dZ, dout, n->A[l], din, n->d_g + n->woff[l], din, nullptr,
+                              nullptr, 0);
+        if (rc != DG_OK) return rc;
         column_sum_kernel<<<dout, 256, 0, n->stream>>>(dZ, rows, dout, n->d_g + n->boff[l]);
         if (l > 0) {
             // dA_l = dZ W ([rows x din]), then through the GELU of layer l-1
             float *dA = (dZ == n->d_dA) ? n->d_dB : n->d_dA;
-            gemm<false, true>(n->stream, rows, din, dout, dZ, dout, n->d_p + n->woff[l], din, dA, din, nullptr,
-                              nullptr, 0);
+            rc = gemm<false, true>(n, true, rows, din, dout, dZ, dout, n->d_p + n->woff[l], din, dA, din, nullptr,
+                                   nullptr, 0);
+            if (rc != DG_OK) return rc;
             gelu_backward_kernel<<<grid_for((long long)rows * din), 256, 0, n->stream>>>(dA, n->Z[l - 1],
                                                                                          (long long)rows * din);
             dZ = dA;
@@ -683,6 +717,7 @@ void dg_mlp_destroy(dg_mlp *n) {
     for (auto *w : n->wbf)
         if (w) cudaFree(w);
     if (n->d_err) cudaFree(n->d_err);
+    if (n->d_terr) cudaFree(n->d_terr);
     for (float *q : {n->d_p, n->d_g, n->d_m, n->d_v})
         if (q) cudaFree(q);
     if (n->d_loss) cudaFree(n->d_loss);
@@ -704,6 +739,12 @@ int dg_mlp_set_params(dg_mlp *n, const float *p) {
     CK(cudaSetDevice(n->device));
     CK(cudaMemcpy(n->d_p, p, (size_t)n->nparam * 4, cudaMemcpyHostToDevice));
     n->bf_dirty = true;
+    return DG_OK;
+}
+
+int dg_mlp_set_gemm(dg_mlp *n, int mode) {
+    if (!n || (mode != 0 && mode != 1)) return fail(DG_ERR_ARG, "mode must be 0 (CUDA cores) or 1 (tensor cores)");
+    n->gemm_tc = mode == 1;
     return DG_OK;
 }
 
@@ -733,7 +774,7 @@ int dg_mlp_forward(dg_mlp *n, const float *X, int rows, float *Y) {
     if (rc != DG_OK) return rc;
     CK(cudaMemcpyAsync(Y, n->d_Y, (size_t)rows * n->nout * 4, cudaMemcpyDeviceToHost, n->stream));
     CK(cudaStreamSynchronize(n->stream));
-    return DG_OK;
+    return check_gemm_err(n);
 }
 
 int dg_mlp_loss_grad(dg_mlp *n, const float *X, const float *T, int rows, double *loss, float *grad) {
@@ -746,7 +787,8 @@ int dg_mlp_loss_grad(dg_mlp *n, const float *X, const float *T, int rows, double
     rc = mlp_backward(n, n->d_X, n->d_T, rows, loss);
     if (rc != DG_OK) return rc;
     if (grad) CK(cudaMemcpy(grad, n->d_g, (size_t)n->nparam * 4, cudaMemcpyDeviceToHost));
-    return DG_OK;
+    CK(cudaStreamSynchronize(n->stream));
+    return check_gemm_err(n);
 }
 
 int dg_mlp_train_step(dg_mlp *n, const float *X, const float *T, int rows, double lr, double *loss) {
@@ -1101,6 +1143,8 @@ int dg_learned_train(dg_learned *L, int epochs, int batch, double lr, unsigned s
     cudaFree(X);
     cudaFree(T);
     if (rc != DG_OK) return rc;
+    rc = check_gemm_err(n);
+    if (rc != DG_OK) return rc;
     if (loss) *loss = last;
     return DG_OK;
 }
@@ -1119,7 +1163,7 @@ int dg_learned_apply(dg_learned *L, double *const u[4], int napps) {
     CK(cudaStreamSynchronize(L->net->stream));
     for (int f = 0; f < c->nq; ++f)
         CK(cudaMemcpy(u[f], L->d_u0 + f * c->ndof, (size_t)c->ndof * 8, cudaMemcpyDeviceToHost));
-    return DG_OK;
+    return check_gemm_err(L->net);
 }
 
 // Parareal over nslices slices of slice_steps fine RK4 steps from u0 (host).

@@ -19,4 +19,13 @@ __device__ __forceinline__ float gelu_f(float x) {
 int tc_linear(cudaStream_t s, int M, int N, int np, int kp, const void *X, const void *W, const float *bias, bool gelu,
               void *ybf, float *yf32, int ldy, int *err);
 
+// FP32 GEMM of MLP training on the tensor cores (mlp_train_tc.cu), 3xTF32
+// split products with FP32 accumulation: C[m][n] = sum_k op(A)[m][k]
+// op(B)[n][k] (+ bias[n]) (+ C[m][n] when accumulate), gelu_out (if not
+// null) = GELU of the result; op(A)[m][k] = ta ? A[k*lda + m] : A[m*lda + k],
+// op(B) likewise.  Returns 0, -1 on bad sizes, -2 on a launch error; err is
+// set to 1 if a wait on the tensor cores gives up.
+int tc_gemm_tf32x3(cudaStream_t s, bool ta, bool tb, int M, int N, int K, const float *A, int lda, const float *B,
+                   int ldb, float *C, int ldc, const float *bias, float *gelu_out, int accumulate, int *err);
+
 }  // namespace dgk

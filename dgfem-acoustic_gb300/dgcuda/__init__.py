@@ -159,6 +159,7 @@ def _declare(L: C.CDLL) -> None:
         "dg_layout_free": (None, [vp]),
         "dg_tc_selftest": (C.c_int, [C.c_int, P_d]),
         "dg_tc_wait_selftest": (C.c_int, [C.c_int, P_i]),
+        "dg_mlp_set_gemm": (C.c_int, [vp, C.c_int]),
         "dg_tc_selftest_tf32": (C.c_int, [C.c_int, P_d]),
         "dg_euler_steps": (C.c_int, [vp, P_d, C.c_double, C.c_int]),
         "dg_multi_create": (C.c_int, [C.c_int, vp, vp, C.POINTER(Opts), C.POINTER(vp)]),
@@ -839,6 +840,12 @@ class MLP:
         p = np.ascontiguousarray(p, dtype=np.float32)
         _check(lib().dg_mlp_set_params(self._h, _fptr(p)))
 
+    def set_gemm(self, mode: str) -> None:
+        """"tc" (default): the GEMMs of training on the tensor cores with
+        3xTF32 split products; "simt": on the CUDA cores.  FP32 inference
+        runs on the CUDA cores either way."""
+        _check(lib().dg_mlp_set_gemm(self._h, {"simt": 0, "tc": 1}[mode]))
+
     def forward(self, X: np.ndarray, bf16: bool = False) -> np.ndarray:
         """Inference; bf16=True runs it on the tensor cores (BF16 inputs,
         weights and hidden activations, FP32 accumulation)."""
@@ -905,6 +912,13 @@ class Learned:
     def set_inference(self, mode: str) -> None:
         """Coarse steps infer in "fp32" (default) or "bf16" (tensor cores)."""
         _check(lib().dg_learned_set_inference(self._h, {"fp32": 0, "bf16": 1}[mode]))
+
+    def set_gemm(self, mode: str) -> None:
+        """GEMMs of the network's training: "tc" (default, tensor cores,
+        3xTF32) or "simt" (CUDA cores)."""
+        ni, no, net = C.c_int(), C.c_int(), C.c_void_p()
+        _check(lib().dg_learned_info(self._h, C.byref(ni), C.byref(no), C.byref(net)))
+        _check(lib().dg_mlp_set_gemm(net, {"simt": 0, "tc": 1}[mode]))
 
     def step_stats(self) -> dict:
         n, am, amin = C.c_longlong(), C.c_double(), C.c_double()

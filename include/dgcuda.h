@@ -345,6 +345,11 @@ int dg_mlp_forward_bf16(dg_mlp *net, const float *X, int rows, float *Y);
  * like the parameters; grad may be NULL). */
 int dg_mlp_loss_grad(dg_mlp *net, const float *X, const float *T, int rows, double *loss, float *grad);
 int dg_mlp_train_step(dg_mlp *net, const float *X, const float *T, int rows, double lr, double *loss);
+/* Where the GEMMs of training (forward pass, activation and weight
+ * gradients) run: 1 = the tcgen05 tensor cores with 3xTF32 split products
+ * and FP32 accumulation (the default), 0 = the CUDA cores (FP32 FMA).  FP32
+ * inference (dg_mlp_forward, FP32 coarse steps) runs on the CUDA cores. */
+int dg_mlp_set_gemm(dg_mlp *net, int mode);
 
 /* dg_learned: an element-local network (inputs: the element's DOFs, its face
  * neighbours' traces at its face nodes, its boundary-face kinds and inverse

@@ -23,6 +23,7 @@ def rel(a, b):
 def test_mlp_forward_loss_and_gradients_match_oracle(nin, width, nout, hidden, rows):
     rng = np.random.default_rng(nin)
     net = D.MLP(nin, width, nout, hidden, seed=3)
+    net.set_gemm("simt")
     p = net.params()
     assert p.size == sum(o * i + o for (o, i) in M.shapes(nin, width, nout, hidden))
     p = (rng.standard_normal(p.size) * 0.2).astype(np.float32)
@@ -175,3 +176,42 @@ def test_learned_coarse_step_is_bit_reproducible():
     a = L.apply(u0, 5)
     b = L.apply(u0, 5)
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("nin,width,nout,hidden,rows", [(40, 64, 12, 3, 300), (37, 70, 13, 2, 301),
+                                                         (261, 256, 80, 3, 517), (261, 256, 80, 3, 4096)])
+@pytest.mark.parametrize("mode", ["tc", "simt"])
+def test_training_gemms_on_both_paths_match_oracle(nin, width, nout, hidden, rows, mode):
+    """The training GEMMs (forward, activation gradient, weight gradient over
+    the rows, split over CTAs when the rows are many) on the tensor cores
+    (3xTF32 split products, FP32 accumulation: the default) and on the CUDA
+    cores: inference and gradients against the float64 oracle at the same
+    bars (1e-5, 1e-4).  The loss is held to 1e-5 on
+    the CUDA cores and 5e-5 on the tensor cores: their FP32 accumulation
+    across the K-steps of an output (rounded per MMA) measured 1.3e-5 on the
+    width-256 network with outputs of magnitude ~40.  A few Adam steps on
+    either path stay within 1e-4 of the other."""
+    rng = np.random.default_rng(nin + rows)
+    net = D.MLP(nin, width, nout, hidden, seed=7)
+    net.set_gemm(mode)
+    p = (rng.standard_normal(net.params().size) * 0.2).astype(np.float32)
+    net.set_params(p)
+    X = rng.standard_normal((rows, nin)).astype(np.float32)
+    T = rng.standard_normal((rows, nout)).astype(np.float32)
+    Y = net.forward(X)
+    Yo, _, _ = M.forward(p, X, nin, width, nout, hidden)
+    assert rel(Y, Yo) <= 1e-5, rel(Y, Yo)
+    loss, g = net.loss_grad(X, T)
+    lo, go = M.loss_grad(p, X, T, nin, width, nout, hidden)
+    assert abs(loss - lo) <= (5e-5 if mode == "tc" else 1e-5) * lo, (loss, lo)
+    assert rel(g, go) <= 1e-4, rel(g, go)
+    # a few Adam steps move both paths the same way
+    other = D.MLP(nin, width, nout, hidden, seed=7)
+    other.set_gemm("simt" if mode == "tc" else "tc")
+    other.set_params(p)
+    for _ in range(3):
+        net.train_step(X, T, 1e-3)
+        other.train_step(X, T, 1e-3)
+    assert rel(net.params(), other.params().astype(np.float64)) <= 1e-4
+    net.close()
+    other.close()
