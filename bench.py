@@ -446,34 +446,44 @@ def ours_arm(args, world, rank, local, pg):
     roofline = roofline_for(sol, pre, form, t, dt, min(args.steps, 100))
 
     # end to end: every step set_state from pinned host memory, one step,
-    # get_state into pinned host memory, through the C ABI
+    # and the step's result copied out to pinned host memory, through the C
+    # ABI.  The copy-out is dg_get_state_async (the save-step API): it runs
+    # on a side stream while the next step's input goes in and the next step
+    # computes; the run waits for every frame before the clock stops.
     n_e2e = 0 if args.no_e2e else min(args.steps, 200)
-    L = D.lib()
     nbytes = 4 * pre.ndof * 8
-    e2e_value = None
+    e2e_value = e2e_sync_value = None
     if n_e2e:
-        import ctypes as C
-
-        hin, hout = L.dg_host_alloc(nbytes), L.dg_host_alloc(nbytes)
-        if not hin or not hout:
-            raise RuntimeError("pinned host allocation failed")
-        uin = np.ctypeslib.as_array((C.c_double * (4 * pre.ndof)).from_address(hin)).reshape(4, pre.ndof)
-        uout = np.ctypeslib.as_array((C.c_double * (4 * pre.ndof)).from_address(hout)).reshape(4, pre.ndof)
+        uin = D.pinned_array((4, pre.ndof))
+        outs = [D.pinned_array((4, pre.ndof)), D.pinned_array((4, pre.ndof))]
         uin[:] = u0
         barrier(pg)
         sol.synchronize()
         w0 = time.perf_counter()
         te = 0.0
-        for _ in range(n_e2e):
+        tickets = []
+        for k in range(n_e2e):
             sol.set_state(uin)
             te = sol.rk4_steps(te, dt, 1)
-            sol.get_state(uout)
+            tickets.append(sol.get_state_async(outs[k % 2]))
+        for tk in tickets[-2:]:
+            sol.wait_state(tk)  # earlier frames were waited for when their slot was reused
         sol.synchronize()
         w1 = time.perf_counter()
         barrier(pg)
         e2e_value = allreduce_sum(pg, dof_stage_per_step * n_e2e) / allreduce_max(pg, w1 - w0)
-        L.dg_host_free(hin)
-        L.dg_host_free(hout)
+        # the blocking protocol beside it (copy-out after each step, waited for)
+        n_sync = min(n_e2e, 50)
+        sol.synchronize()
+        w0 = time.perf_counter()
+        te = 0.0
+        for _ in range(n_sync):
+            sol.set_state(uin)
+            te = sol.rk4_steps(te, dt, 1)
+            sol.get_state(outs[0])
+        sol.synchronize()
+        w1 = time.perf_counter()
+        e2e_sync_value = allreduce_sum(pg, dof_stage_per_step * n_sync) / allreduce_max(pg, w1 - w0)
     sol.close()
 
     # the other forms on the same workload, and the accuracy of every form
@@ -512,7 +522,11 @@ def ours_arm(args, world, rank, local, pg):
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                "steps": n_e2e, "how": "per step: dg_set_state from pinned host, dg_rk4_steps(1), dg_get_state"},
+                "steps": n_e2e,
+                "how": "per step: dg_set_state from pinned host, dg_rk4_steps(1), dg_get_state_async into pinned "
+                       "host (side-stream copy overlapping the next step; every frame waited for before the clock "
+                       "stops)",
+                "blocking_copy_out_value": e2e_sync_value},
         "clocks": clk.summary(),
         "gpu_launches": 4 * args.steps,
         "monitors": {"energy": e, "nonfinite": bad},
@@ -563,6 +577,13 @@ def batched_section(D, args, local):
     out["tf32x3_over_fp64"] = out["tf32x3"]["value"] / out["fp64"]["value"]
     out["accuracy"] = batched_accuracy(D, pre, dt, srcs, recs, min(4, args.batched_sources),
                                        args.batched_acc_steps, local)
+    # the batch's chosen form: the fastest tensor-core form whose measured
+    # error against the FP64 batch meets 1e-5
+    ok = [f for f in ("mixed", "tf32x3") if out["accuracy"][f]["meets_1e-5"]]
+    if ok:
+        best = max(ok, key=lambda f: out[f]["value"])
+        out["chosen"] = {"form": best, "value": out[best]["value"], "over_fp64": out[best]["value"] / out["fp64"]["value"],
+                         "rel_l2_vs_fp64": out["accuracy"][best]["state_rel_l2_vs_fp64_max"]}
     return out
 
 
