@@ -44,17 +44,18 @@ void b_image(const double *ops, std::vector<uint8_t> &img, std::vector<int> &eb)
         if (amax > 0) std::frexp(amax, &e);
         eb[i] = e;
         for (int k = 0; k < KTOT; ++k) {
+            // radix 2^9 slices, |m| <= 256 (exact in BF16), as the A rows
             double x = std::ldexp(row[k], -e) * 256.0;
-            for (int sl = 0; sl < 4; ++sl) {
+            for (int sl = 0; sl < MS::NSB; ++sl) {
                 double m = std::nearbyint(x);
-                x = (x - m) * 256.0;
-                float val = (float)std::ldexp(m, -8 * sl);
+                x = (x - m) * 512.0;
+                float val = (float)std::ldexp(m, -9 * sl);
                 uint32_t bits;
                 std::memcpy(&bits, &val, 4);
                 uint16_t h = (uint16_t)(bits >> 16);
                 // per K-step the four slices follow one another along N, so
                 // that one MMA can take several slices as one wider operand
-                size_t off = (size_t)((k / 16) * 4 + sl) * MS::BTILE + (i / 8) * 256 + ((k % 16) / 8) * 128 +
+                size_t off = (size_t)((k / 16) * MS::NSB + sl) * MS::BTILE + (i / 8) * 256 + ((k % 16) / 8) * 128 +
                              (i % 8) * 16 + (k % 8) * 2;
                 std::memcpy(&img[off], &h, 2);
             }

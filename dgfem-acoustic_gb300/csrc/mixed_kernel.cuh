@@ -8,16 +8,19 @@
 //   B[i] = ( D_u[i][j]          | LIFT[i][slot] ),
 // so that dt*C is the stage increment (weak volume term minus lift, already
 // multiplied by M^-1).  To keep the contraction at FP64-grade accuracy with
-// FP32 accumulators, both operands are cut into four fixed-point slices with
-// one exponent per row: a = 2^(ea-8) sum_s m_s 2^(-8s), |m_s| <= 256 integer,
-// stored in BF16 exactly; B is sliced on the host the same way per output
-// node.  Slice products are integers (times 2^-8(i+j)); the ten pairs with
-// i+j <= 3 are formed (the pairs with i+j = 4 lie 2^-32 below the row scales,
-// under the FP32 resolution of the result).  Pairs with i+j = 0 and i+j = 1
-// sum exactly in FP32 tensor-memory accumulators (|sum| < 2^24 units), the
-// others in further accumulators.  The epilogue adds them in double-FP32,
-// scales by 2^(ea+eb-16) dt and applies the RK4 stage update with the state u
-// kept as an FP32 pair.
+// FP32 accumulators, both operands are cut into fixed-point slices with one
+// exponent per row and radix 2^9: a = 2^(ea-8) sum_s m_s 2^(-9s), |m_s| <= 256
+// integer (at most 8 significant bits, so exact in BF16); A (FP32) in four
+// slices (36 bits below the row scale; three, 27 bits, where tensor memory
+// holds no more: 3D order 4), B (FP64 operators, sliced on the host per
+// output node) in four (36 bits).  Slice products are integers (times
+// 2^-9(i+j)); the pairs with i+j <= 3 are formed (the pairs with i+j >= 4
+// lie 2^-36 below the row scales).  Level i+j = 0 sums exactly in
+// its FP32 tensor-memory accumulator (|sum| <= K 2^16 < 2^24 for K <= 256),
+// level 1 for K <= 128 (beyond, its rounding lies 2^-33 below the row
+// scales), levels 2 and 3 in two more.  The epilogue adds them in
+// double-FP32, scales by 2^(ea+eb-16) dt and applies the RK4 stage update
+// with the state u kept as an FP32 pair.
 //
 // Roles (128*NWG threads, one CTA per SM, persistent over tiles): cp.async copies
 // bring a tile's state, geometry, connectivity and neighbour traces into
@@ -26,7 +29,8 @@
 // face values).
 // Row r is then sliced by lane r%32 of warps r/32 + 4g of every warp group g
 // (warp w may only touch tensor-memory lanes 32(w%4)..32(w%4)+31), each
-// group taking a share of the K-steps, and stored with tcgen05.st.  One
+// group taking an equal share of the row's tensor-memory columns, and stored
+// with tcgen05.st.  One
 // thread issues the tcgen05.mma and commits them to an mbarrier;
 // the warp groups then read the accumulators of their row with tcgen05.ld,
 // split by output node, for the epilogue.  Every wait is bounded; on timeout the kernel records an error,
@@ -42,10 +46,11 @@
 
 namespace dgk {
 
-// Contraction kinds: the exact fixed-point form (four BF16 slices of each
-// operand, kind::f16 MMAs, exact accumulation) and 3xTF32 (each operand split
-// into a high and a low TF32 part, a_hi b_hi + a_hi b_lo + a_lo b_hi by
-// kind::tf32 MMAs, FP32 accumulation).
+// Contraction kinds: the exact fixed-point form (four or three BF16 slices
+// of each A value, four of each operator value, kind::f16 MMAs, exact
+// accumulation)
+// and 3xTF32 (each operand split into a high and a low TF32 part,
+// a_hi b_hi + a_hi b_lo + a_lo b_hi by kind::tf32 MMAs, FP32 accumulation).
 constexpr int kTcBf16x4 = 0, kTcTf32x3 = 1;
 
 // HALVES = 2: the CTA runs two independent tile pipelines (one per half of
@@ -62,38 +67,28 @@ struct MixedShape {
     static constexpr int KSTEP = TF ? 8 : 16;       // K of one MMA (32 bytes of a K-major row)
     static constexpr int KPAD = (KTOT + KSTEP - 1) / KSTEP * KSTEP;
     static constexpr int KSTEPS = KPAD / KSTEP;
-    static constexpr int NSLICE = TF ? 2 : 4;       // parts of each operand
     static constexpr int NPAD = (NP + 15) / 16 * 16;
     static constexpr int ELEMS = 128 / NQ;          // elements per tile
     static constexpr int TMEM_COLS = 512 / HALVES;  // tensor-memory columns of one pipeline
-    // Level scheme (where it fits): one accumulator per level L = i+j of the
-    // slice pairs (0..3).  The B slices of a K-step lie side by side along N,
-    // so A slice i meets B slices 0..3-i in one MMA of N = (4-i) x NPAD,
-    // accumulating into levels i..3: four MMAs per K-step.  Where the four A
-    // slices of all K-steps and the four levels do not fit in tensor memory
-    // together (3D order 4), the K-steps go in two passes that reuse the A
-    // columns (the second pass is sliced once the first pass's MMAs are done).
+    static constexpr int NSB = TF ? 2 : 4;          // parts of each operator value
+    // parts of each A value: four BF16 slices where their columns (two K
+    // values per column) and the four level accumulators fit, else three
+    static constexpr int NSA = TF ? 2 : (4 * (KPAD / 2) + 4 * NPAD <= TMEM_COLS ? 4 : 3);
+    // Tensor-memory columns of one A part: BF16 packs two K values per
+    // column, TF32 takes one.
+    static constexpr int ACOLS = TF ? KPAD : KPAD / 2;
+    // Level scheme: one accumulator per level L = i+j of the slice pairs
+    // (0..3).  The B slices of a K-step lie side by side along N, so A slice
+    // i meets B slices 0..3-i in one MMA of N = (4-i) x NPAD, accumulating
+    // into levels i..3: one MMA per A slice and K-step.
     // 3xTF32: the two A parts of every K-step (one 32-bit value per column)
-    // and two accumulators (a_hi b_hi + a_lo b_hi, a_hi b_lo), one pass.
-    static constexpr bool LEVELS_ONE = !TF && 4 * (KPAD / 2) + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256;
-    static constexpr int KPASS_TWO = (KSTEPS + 1) / 2;
-    static constexpr bool LEVELS_TWO =
-        !TF && !LEVELS_ONE && 4 * KPASS_TWO * 8 + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256;
-    static constexpr int NPASS = LEVELS_TWO ? 2 : 1;
-    static constexpr int KPASS = NPASS == 2 ? KPASS_TWO : KSTEPS;  // K-steps per pass
-    static constexpr bool LEVELS = LEVELS_ONE || LEVELS_TWO;
-    static constexpr int ACOLS = KPASS * 8;         // tensor-memory columns per A slice (one pass)
-    static constexpr int ACC = TF ? (2 * ACOLS + 31) / 32 * 32 : 4 * ACOLS;  // first accumulator column
-    static constexpr bool FITS = TF ? (ACC + 2 * NPAD <= TMEM_COLS && 2 * NPAD <= 256) : ACC + 3 * NPAD <= TMEM_COLS;
-    // Pair scheme (otherwise): one MMA per slice pair; accumulator 0 for
-    // i+j = 0, 1 for i+j = 1 (both exact), NX more for the seven pairs with
-    // i+j = 2, 3 (spread so that the MMAs of consecutive pairs do not wait on
-    // one another)
-    static constexpr int NACC_FIT = (TMEM_COLS - ACC) / NPAD;
-    static constexpr int NACC = TF ? 2 : LEVELS ? 4 : NACC_FIT < 9 ? NACC_FIT : 9;
-    static constexpr int NX = NACC - 2;
+    // and two accumulators (a_hi b_hi + a_lo b_hi, a_hi b_lo).
+    static constexpr int ACC = TF ? (2 * ACOLS + 31) / 32 * 32 : NSA * ACOLS;  // first accumulator column
+    static constexpr int NACC = TF ? 2 : NSB;
+    static constexpr bool FITS = ACC + NACC * NPAD <= TMEM_COLS && NSB * NPAD <= 256;
+    static constexpr int NX = NACC - 2;             // accumulators past the first two
     static constexpr int BTILE = NPAD * 32;         // bytes of one (K-step, slice) B tile; image [K-step][slice]
-    static constexpr int BBYTES = NSLICE * KSTEPS * BTILE;
+    static constexpr int BBYTES = NSB * KSTEPS * BTILE;
     static constexpr int QS = NP;                   // element stride in the state tile
     static constexpr int KSTR = KPAD + 1;           // padded row stride of the staged A rows (odd)
     static constexpr int MAX_WG = 4;                // warp groups per CTA (4 warps each), at most
@@ -110,7 +105,7 @@ struct MixedShape {
     static constexpr int CONN_BYTES = r16(ELEMS * NF * 8);
     static constexpr int OFF_FGEO = OFF_CONN + 2 * CONN_BYTES;         // [le][NF] float4
     static constexpr int OFF_MAX = OFF_FGEO + ELEMS * NF * 16;
-    static constexpr int OFF_TAB = OFF_MAX + MAX_WG * 128 * 4;
+    static constexpr int OFF_TAB = OFF_MAX + MAX_WG * 128 * 4;       // [MAX_WG][128] row maxima
     static constexpr int OFF_EB = r16(OFF_TAB + S::NTAB);
     // Overlap: the next tile's A rows are built while this tile's MMAs run,
     // so the epilogue stages its outputs outside the A-row region: in a
@@ -133,20 +128,12 @@ struct MixedShape {
     // the epilogue stages the tile's two output arrays in the A-row region
     static_assert(2 * NQ * ELEMS * NP <= 128 * KSTR, "output staging fits in the A-row region");
     static_assert(HALVES == 2 || SMEM <= 227 * 1024, "tile does not fit in shared memory");
-    static_assert(NPASS * KPASS >= KSTEPS && (NPASS == 1 || LEVELS), "the passes cover every K-step");
-    static_assert(!LEVELS || (ACC + 4 * NPAD <= TMEM_COLS && 4 * NPAD <= 256), "level accumulators fit");
     static_assert(!OUT_ALIAS || (OFF_Q + OUT_FLOATS * 4 <= OFF_A && OFF_NBR > OFF_Q && OFF_A > OFF_NBR),
                   "aliased output staging stays inside the state-tile and neighbour-trace regions");
     // at least half of the SM's shared memory, so one CTA (the tensor-memory
     // owner) runs per SM
     static constexpr int SMEM_LAUNCH = SMEM < 118 * 1024 ? 118 * 1024 : SMEM;
 };
-
-// Pair list of the slice products (A slice, B slice) by level i + j; the
-// first ten (i + j <= 3) are formed.
-__device__ __constant__ const int8_t kPairA[13] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 1, 2, 3};
-__device__ __constant__ const int8_t kPairB[13] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0, 3, 2, 1};
-
 
 // (hi, lo) = a + b exactly (Knuth two-sum).
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
@@ -167,27 +154,72 @@ __device__ __forceinline__ int row_exponent(float amax) {
 // 2^k as a float for -126 <= k <= 127.
 __device__ __forceinline__ float exp2i(int k) { return __uint_as_float((unsigned)(k + 127) << 23); }
 
-// Four BF16 fixed-point slices of y = x*scale (|y| < 256): s0 + s1 + s2 + s3
-// with s_k a multiple of 2^-8k and |s_k| <= 256 * 2^-8k (at most 8
-// significant bits, so exact in BF16).  Rounding to a multiple of 2^-8k is
-// done by adding and subtracting 1.5 * 2^(23-8k) (round to nearest even, as
-// rintf of the scaled value; full-rate additions instead of conversions);
-// each remainder y - s_k is exact.
-__device__ __forceinline__ void slice4(float x, float scale, float (&m)[4]) {
-    const float y = x * scale;
-    m[0] = __fsub_rn(__fadd_rn(y, 12582912.0f), 12582912.0f);  // 1.5 * 2^23
-    const float r1 = __fsub_rn(y, m[0]);
-    m[1] = __fsub_rn(__fadd_rn(r1, 49152.0f), 49152.0f);  // 1.5 * 2^15
+// NS (3 or 4) BF16 fixed-point slices of y = x*scale (|y| < 256):
+// s0 + s1 + ... with s_k a multiple of 2^-9k and |s_k| <= 256 * 2^-9k (at
+// most 8 significant bits, so exact in BF16).  Rounding to a multiple of
+// 2^-9k is done by adding and subtracting 1.5 * 2^(23-9k) (round to nearest
+// even, as rintf of the scaled value; full-rate additions instead of
+// conversions); x*scale is exact (scale is a power of two), so the first
+// rounding and the first remainder are single fused multiply-adds, and each
+// remainder is exact.  What is left, |y - sum s_k| <= 2^-(9 NS - 8), is
+// dropped.
+template <int NS>
+__device__ __forceinline__ void slice_fixed(float x, float scale, float (&m)[NS]) {
+    static_assert(NS == 3 || NS == 4, "three or four slices");
+    m[0] = __fsub_rn(__fmaf_rn(x, scale, 12582912.0f), 12582912.0f);  // 1.5 * 2^23
+    const float r1 = __fmaf_rn(x, scale, -m[0]);
+    m[1] = __fsub_rn(__fadd_rn(r1, 24576.0f), 24576.0f);  // 1.5 * 2^14
     const float r2 = __fsub_rn(r1, m[1]);
-    m[2] = __fsub_rn(__fadd_rn(r2, 192.0f), 192.0f);  // 1.5 * 2^7
-    const float r3 = __fsub_rn(r2, m[2]);
-    m[3] = __fsub_rn(__fadd_rn(r3, 0.75f), 0.75f);  // 1.5 * 2^-1
+    m[2] = __fsub_rn(__fadd_rn(r2, 48.0f), 48.0f);  // 1.5 * 2^5
+    if constexpr (NS == 4) {
+        const float r3 = __fsub_rn(r2, m[2]);
+        m[3] = __fsub_rn(__fadd_rn(r3, 0.09375f), 0.09375f);  // 1.5 * 2^-4
+    }
 }
 
 // Two values exactly representable in BF16, packed low = first, high =
 // second: their upper halves (a byte permute, no rounding needed).
 __device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
     return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
+}
+
+// Slices CW tensor-memory columns of row arow, from column col on, into
+// the A parts and stores them at taddr (part p at taddr + p * ACOLS): BF16,
+// two K values per column, NS fixed-point slices with scale sc; 3xTF32,
+// one value per column, its TF32 high part and remainder.  Columns past KTOT
+// get zeros.
+template <int KIND, int NS, int KTOT, int ACOLS, int CW>
+__device__ __forceinline__ void slice_columns(const float *arow, bool live, float sc, int col, uint32_t taddr) {
+    if constexpr (KIND == kTcTf32x3) {
+        uint32_t wh[CW], wl[CW];
+#pragma unroll
+        for (int h = 0; h < CW; ++h) {
+            const int k = col + h;
+            const float x = (live && k < KTOT) ? arow[k] : 0.0f;
+            const float xh = dgtc::tf32_round(x);
+            wh[h] = __float_as_uint(xh);
+            wl[h] = __float_as_uint(dgtc::tf32_round(x - xh));
+        }
+        __syncwarp();
+        dgtc::tmem_st_n<CW>(taddr, wh);
+        dgtc::tmem_st_n<CW>(taddr + ACOLS, wl);
+    } else {
+        uint32_t w[NS][CW];
+#pragma unroll
+        for (int h = 0; h < CW; ++h) {
+            const int k = 2 * (col + h);
+            const float x0 = (live && k < KTOT) ? arow[k] : 0.0f;
+            const float x1 = (live && k + 1 < KTOT) ? arow[k + 1] : 0.0f;
+            float m0[NS], m1[NS];
+            slice_fixed<NS>(x0, sc, m0);
+            slice_fixed<NS>(x1, sc, m1);
+#pragma unroll
+            for (int sl = 0; sl < NS; ++sl) w[sl][h] = bf16x2_bits(m0[sl], m1[sl]);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int sl = 0; sl < NS; ++sl) dgtc::tmem_st_n<CW>(taddr + sl * ACOLS, w[sl]);
+    }
 }
 
 // Issues the cp.async copies of a tile's connectivity words into buffer cb;
@@ -268,7 +300,11 @@ __device__ __forceinline__ void issue_neighbour_copies(const MixedArgs &a, unsig
 // Phase 2: the tile's A rows in shared memory (FP32): contravariant volume
 // fluxes (one task per element node) and the face values negated and scaled
 // by detJf/detJe (one task per face slot), from the tile's state, geometry,
-// connectivity words (buffer cb) and neighbour traces.
+// connectivity words (buffer cb) and neighbour traces.  The calling threads
+// take the volume tasks first, first + stride, ... (stride a multiple of 32,
+// first - lane the same for the lanes of a warp) and the face tasks with the
+// warps in reverse order, so that the warps with one volume task more than
+// others get one face task less.
 template <int DIM, int P, int KIND>
 __device__ __forceinline__ void build_rows(const MixedArgs &a, unsigned char *smem, long long ebase, int cb, int first,
                                            int stride) {
@@ -282,6 +318,7 @@ __device__ __forceinline__ void build_rows(const MixedArgs &a, unsigned char *sm
     const int2 *sConn = reinterpret_cast<const int2 *>(smem + MS::OFF_CONN + cb * MS::CONN_BYTES);
     const float4 *sFgeo = reinterpret_cast<const float4 *>(smem + MS::OFF_FGEO);
     const uint8_t *sFmask = smem + MS::OFF_TAB;
+    const int lane = (int)(threadIdx.x & 31);
     // 2a. contravariant fluxes, one task per element node
     for (int task = first; task < ELEMS * NP; task += stride) {
         const int le = task / NP, j = task - le * NP;
@@ -309,7 +346,7 @@ __device__ __forceinline__ void build_rows(const MixedArgs &a, unsigned char *sm
         }
     }
     // 2b. face values, negated and scaled: -(detJf/detJe) Fn
-    for (int task = first; task < ELEMS * NSLOT; task += stride) {
+    for (int task = stride - 32 - (first - lane) + lane; task < ELEMS * NSLOT; task += stride) {
         const int le = task / NSLOT, s = task - le * NSLOT;
         const int lf = s / NFP, k = s - lf * NFP;
         float Fn[NQ];
@@ -374,19 +411,19 @@ __device__ __forceinline__ void build_rows(const MixedArgs &a, unsigned char *sm
     }
 }
 
-// Largest magnitude of each A row over the K-steps of each warp group's
-// slicing range: sMax[g*128 + r] for part g of row r (items (g, r) spread over
-// the threads first, first + stride, ...).
+// Largest magnitude of each A row over NWG equal parts of its K range:
+// sMax[g*128 + r] for part g of row r (items (g, r) spread over the threads
+// first, first + stride, ...).
 template <int DIM, int P, int NWG, int KIND>
 __device__ __forceinline__ void row_maxima(unsigned char *smem, int first, int stride) {
     using MS = MixedShape<DIM, P, KIND>;
-    constexpr int KSTEPS = MS::KSTEPS, KTOT = MS::KTOT, KSTR = MS::KSTR;
-    constexpr int KSP = (KSTEPS + NWG - 1) / NWG;
+    constexpr int KTOT = MS::KTOT, KSTR = MS::KSTR;
+    constexpr int KP = (KTOT + NWG - 1) / NWG;
     const float *sA = reinterpret_cast<const float *>(smem + MS::OFF_A);
     float *sMax = reinterpret_cast<float *>(smem + MS::OFF_MAX);
     for (int w = first; w < NWG * 128; w += stride) {
         const int g = w >> 7, r = w & 127;
-        const int k0 = g * KSP * 16, k1 = min((g + 1) * KSP * 16, KTOT);
+        const int k0 = g * KP, k1 = min(k0 + KP, KTOT);
         const float *arow = &sA[r * KSTR];
         float m = 0.0f;
         for (int k = k0; k < k1; ++k) m = fmaxf(m, fabsf(arow[k]));
@@ -418,14 +455,17 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
     constexpr int NPAD = MS::NPAD, ACOLS = MS::ACOLS;
     constexpr int NT = 128 * NWG;                       // threads of one pipeline
     constexpr int NTC = NT * HALVES;                    // threads of the CTA
-    constexpr int KSP = (KSTEPS + NWG - 1) / NWG;       // K-steps sliced per warp group
+    // tensor-memory columns of one A part that hold K values, and the
+    // columns each warp group slices
+    constexpr int NCOL = MS::TF ? KTOT : (KTOT + 1) / 2;
+    constexpr int CPG = (NCOL + NWG - 1) / NWG;
+    static_assert(NWG * CPG <= ACOLS, "the warp groups' columns stay inside each A part");
     constexpr int NPP = (NP + NWG - 1) / NWG;           // output nodes per warp group in the epilogue
     constexpr int NCH = (NPP + 7) / 8;                  // 8-column tensor-memory loads per accumulator
     static_assert(MS::FITS, "tile does not fit in tensor memory");
     static_assert(NWG >= 1 && NWG <= MS::MAX_WG, "warp groups");
     constexpr int NX = MS::NX;
     constexpr bool OVERLAP = MS::OVERLAP;
-    static_assert(MS::TF || NX >= 1, "at least three accumulators");
     static_assert(MS::ACC + (MS::NACC - 1) * NPAD + (NWG - 1) * NPP + 8 * NCH <= MS::TMEM_COLS,
                   "epilogue loads stay inside the allocation");
     static_assert(ELEMS <= 64, "curved-element mask holds 64 elements per tile");
@@ -467,7 +507,19 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
     dgtc::fence_after_sync();
     // this pipeline's tensor-memory columns
     const uint32_t tbase = *sTmem + (uint32_t)(pipe * MS::TMEM_COLS);
-    const uint32_t idesc = dgtc::idesc_bf16_f32(128, NPAD);
+    // A-part columns past the warp groups' shares hold no K values: they meet
+    // zero operator rows, but must hold finite values, so they are zeroed once
+    constexpr int PADC = ACOLS - NWG * CPG;
+    static_assert(PADC < 16, "pad columns");
+    if constexpr (PADC > 0) {
+        if (warp < 4) {
+            const uint32_t zero[16] = {};
+#pragma unroll
+            for (int pt = 0; pt < MS::NSA; ++pt)
+                dgtc::tmem_st_n<PADC>(dgtc::tmem_lane_addr(tbase, warp, pt * ACOLS + NWG * CPG), zero);
+            dgtc::tmem_st_wait();
+        }
+    }
     const uint32_t sB = dgtc::smem_u32(smem_cta + MS::OFF_B);
     // row of this thread in phases 3 and 5, and which part of the row's work
     // (K-steps when slicing, output nodes in the epilogue) its warp group takes
@@ -559,11 +611,8 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
         // the row maxima makes every thread's copies visible
         dgtc::cp_async_wait_group<1>();
 
-        // 3. slices of the A rows into tensor memory; warp group g takes
-        //    K-steps [g*KSP, (g+1)*KSP) of rows 0..127
+        // 3. slices of the A rows into tensor memory (rows 0..127)
         const bool row_ok = (rf < NQ) && (ebase + rle < a.K);
-        const int ks0 = part * KSP < KSTEPS ? part * KSP : KSTEPS;
-        const int ks1 = ks0 + KSP < KSTEPS ? ks0 + KSP : KSTEPS;
         // operands of this thread's RK update, loaded now so that their latency
         // overlaps the slicing and the contraction
         const int i0 = part * NPP;
@@ -580,9 +629,10 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
         }
         const float *arow = &sA[r * KSTR];
         if constexpr (!OVERLAP && !MS::TF) {
+            constexpr int KP = (KTOT + NWG - 1) / NWG;
             float m = 0.0f;
             if (row_ok)
-                for (int k = ks0 * 16; k < ks1 * 16 && k < KTOT; ++k) m = fmaxf(m, fabsf(arow[k]));
+                for (int k = part * KP; k < part * KP + KP && k < KTOT; ++k) m = fmaxf(m, fabsf(arow[k]));
             sMax[part * 128 + r] = m;
         }
         pipe_sync<HALVES>(bar_all, NT);
@@ -603,102 +653,50 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
             live = row_ok && ea > -110;
             sc = live ? exp2i(8 - ea) : 0.0f;
         }
-        // K-steps of each pass (one pass unless tensor memory is short); the
-        // pass's K-steps are spread over the warp groups for the slicing
-        constexpr int NPASS = MS::NPASS, KPASS = MS::KPASS;
-        constexpr int KSPP = (KPASS + NWG - 1) / NWG;
+        // 3 (cont.). warp group g slices columns [g*CPG, (g+1)*CPG) of the
+        // row's tensor-memory columns in chunks of eight
+        {
+            const int col0 = part * CPG;
+            const uint32_t ta = dgtc::tmem_lane_addr(tbase, warp, col0);
 #pragma unroll 1
-        for (int pass = 0; pass < NPASS; ++pass) {
-            const int kb = pass * KPASS, ke = kb + KPASS < KSTEPS ? kb + KPASS : KSTEPS;
-            const int c0 = NPASS == 1 ? ks0 : (kb + part * KSPP < ke ? kb + part * KSPP : ke);
-            const int c1 = NPASS == 1 ? ks1 : (c0 + KSPP < ke ? c0 + KSPP : ke);
-            if (pass > 0) {
-                // the previous pass's MMAs read the A columns about to be rewritten
-                if (!dgtc::mbar_wait_bounded(bar, phase, 1u << 30)) *sFail = 1;
-                phase ^= 1u;
-                dgtc::fence_after_sync();
-            }
-#pragma unroll 1
-            for (int c = c0; c < c1 && MS::TF; ++c) {
-                // 3xTF32: high part and remainder of every value, one per column
-                uint32_t wh[8], wl[8];
-#pragma unroll
-                for (int h = 0; h < 8; ++h) {
-                    const int k = c * 8 + h;
-                    const float x = (live && k < KTOT) ? arow[k] : 0.0f;
-                    const float xh = dgtc::tf32_round(x);
-                    wh[h] = __float_as_uint(xh);
-                    wl[h] = __float_as_uint(dgtc::tf32_round(x - xh));
-                }
-                __syncwarp();
-                dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, c * 8), wh);
-                dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, ACOLS + c * 8), wl);
-            }
-#pragma unroll 1
-            for (int c = c0; c < c1 && !MS::TF; ++c) {
-                uint32_t w[4][8];
-#pragma unroll
-                for (int h = 0; h < 8; ++h) {
-                    const int k = c * 16 + 2 * h;
-                    const float x0 = (live && k < KTOT) ? arow[k] : 0.0f;
-                    const float x1 = (live && k + 1 < KTOT) ? arow[k + 1] : 0.0f;
-                    float m0[4], m1[4];
-                    slice4(x0, sc, m0);
-                    slice4(x1, sc, m1);
-#pragma unroll
-                    for (int sl = 0; sl < 4; ++sl) w[sl][h] = bf16x2_bits(m0[sl], m1[sl]);
-                }
-                __syncwarp();
-#pragma unroll
-                for (int sl = 0; sl < 4; ++sl)
-                    dgtc::tmem_st8(dgtc::tmem_lane_addr(tbase, warp, sl * ACOLS + (c - kb) * 8), w[sl]);
-            }
-            dgtc::tmem_st_wait();
-            dgtc::fence_before_sync();
-            pipe_sync<HALVES>(bar_all, NT);
+            for (int c = 0; c < CPG / 8; ++c)
+                slice_columns<KIND, MS::NSA, KTOT, ACOLS, 8>(arow, live, sc, col0 + 8 * c, ta + 8 * c);
+            if constexpr (CPG % 8 > 0)
+                slice_columns<KIND, MS::NSA, KTOT, ACOLS, CPG % 8>(arow, live, sc, col0 + CPG / 8 * 8,
+                                                                    ta + CPG / 8 * 8);
+        }
+        dgtc::tmem_st_wait();
+        dgtc::fence_before_sync();
+        pipe_sync<HALVES>(bar_all, NT);
 
-            // 4. tensor-core contraction, issued by thread 0 K-step by K-step
-            if (tid == 0 && !*sFail) {
-                dgtc::fence_after_sync();
-                if constexpr (MS::TF) {
-                    // per K-step: a_hi against [b_hi | b_lo] into both
-                    // accumulators, then a_lo against b_hi into the first
+        // 4. tensor-core contraction, issued by thread 0 K-step by K-step
+        if (tid == 0 && !*sFail) {
+            dgtc::fence_after_sync();
+            if constexpr (MS::TF) {
+                // per K-step: a_hi against [b_hi | b_lo] into both
+                // accumulators, then a_lo against b_hi into the first
 #pragma unroll 1
-                    for (int t = 0; t < KSTEPS; ++t) {
-                        const uint64_t bd = dgtc::desc_kmajor(sB + t * 2 * MS::BTILE, 128, 256);
-                        dgtc::mma_tf32_ts(tbase + MS::ACC, tbase + t * 8, bd, dgtc::idesc_tf32_f32(128, 2 * NPAD),
-                                          t > 0 ? 1u : 0u);
-                        dgtc::mma_tf32_ts(tbase + MS::ACC, tbase + ACOLS + t * 8, bd, dgtc::idesc_tf32_f32(128, NPAD),
-                                          1u);
-                    }
-                } else if constexpr (MS::LEVELS) {
-                    // A slice 0 at K-step 0 starts all four levels
-#pragma unroll 1
-                    for (int t = kb; t < ke; ++t) {
-                        const uint64_t bd = dgtc::desc_kmajor(sB + t * 4 * MS::BTILE, 128, 256);
-#pragma unroll
-                        for (int ia = 0; ia < 4; ++ia)
-                            dgtc::mma_bf16_ts(tbase + MS::ACC + ia * NPAD, tbase + ia * ACOLS + (t - kb) * 8, bd,
-                                              dgtc::idesc_bf16_f32(128, (4 - ia) * NPAD),
-                                              (t > 0 || ia > 0) ? 1u : 0u);
-                    }
-                } else {
-                    unsigned started = 0;  // bit per accumulator
-#pragma unroll 1
-                    for (int t = 0; t < KSTEPS; ++t) {
-#pragma unroll
-                        for (int pi = 0; pi < 10; ++pi) {
-                            const int ia = kPairA[pi], jb = kPairB[pi];
-                            const int slot = pi == 0 ? 0 : pi < 3 ? 1 : 2 + (pi - 3) % NX;
-                            const uint64_t bd = dgtc::desc_kmajor(sB + (t * 4 + jb) * MS::BTILE, 128, 256);
-                            dgtc::mma_bf16_ts(tbase + MS::ACC + slot * NPAD, tbase + ia * ACOLS + t * 8, bd, idesc,
-                                              (started >> slot) & 1u);
-                            started |= 1u << slot;
-                        }
-                    }
+                for (int t = 0; t < KSTEPS; ++t) {
+                    const uint64_t bd = dgtc::desc_kmajor(sB + t * MS::NSB * MS::BTILE, 128, 256);
+                    dgtc::mma_tf32_ts(tbase + MS::ACC, tbase + t * 8, bd, dgtc::idesc_tf32_f32(128, 2 * NPAD),
+                                      t > 0 ? 1u : 0u);
+                    dgtc::mma_tf32_ts(tbase + MS::ACC, tbase + ACOLS + t * 8, bd, dgtc::idesc_tf32_f32(128, NPAD),
+                                      1u);
                 }
-                dgtc::mma_commit(bar);
+            } else {
+                // A slice i against B slices 0..3-i into levels i..3; A slice
+                // 0 at K-step 0 starts all four levels
+#pragma unroll 1
+                for (int t = 0; t < KSTEPS; ++t) {
+                    const uint64_t bd = dgtc::desc_kmajor(sB + t * MS::NSB * MS::BTILE, 128, 256);
+#pragma unroll
+                    for (int ia = 0; ia < MS::NSA; ++ia)
+                        dgtc::mma_bf16_ts(tbase + MS::ACC + ia * NPAD, tbase + ia * ACOLS + t * 8, bd,
+                                          dgtc::idesc_bf16_f32(128, (MS::NSB - ia) * NPAD),
+                                          (t > 0 || ia > 0) ? 1u : 0u);
+                }
             }
+            dgtc::mma_commit(bar);
         }
         __syncwarp();
         if constexpr (OVERLAP) {

@@ -172,10 +172,39 @@ __device__ __forceinline__ uint32_t tmem_lane_addr(uint32_t base, int warp, uint
     return base + ((uint32_t)(32 * (warp & 3)) << 16) + col;
 }
 
-__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&v)[8]) {
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t *v) {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
                  "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
                  : "memory");
+}
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, const uint32_t *v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(taddr), "r"(v[0]), "r"(v[1]),
+                 "r"(v[2]), "r"(v[3])
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_st2(uint32_t taddr, const uint32_t *v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1, %2};" ::"r"(taddr), "r"(v[0]), "r"(v[1])
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_st1(uint32_t taddr, uint32_t v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x1.b32 [%0], {%1};" ::"r"(taddr), "r"(v) : "memory");
+}
+// N consecutive columns (N <= 15, a compile-time count) as stores of 8, 4,
+// 2 and 1 columns.
+template <int N>
+__device__ __forceinline__ void tmem_st_n(uint32_t taddr, const uint32_t *v) {
+    if constexpr (N >= 8) {
+        tmem_st8(taddr, v);
+        tmem_st_n<N - 8>(taddr + 8, v + 8);
+    } else if constexpr (N >= 4) {
+        tmem_st4(taddr, v);
+        tmem_st_n<N - 4>(taddr + 4, v + 4);
+    } else if constexpr (N >= 2) {
+        tmem_st2(taddr, v);
+        tmem_st_n<N - 2>(taddr + 2, v + 2);
+    } else if constexpr (N == 1) {
+        tmem_st1(taddr, v[0]);
+    }
 }
 __device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
