@@ -90,7 +90,10 @@ struct MixedShape {
     static constexpr int BTILE = NPAD * 32;         // bytes of one (K-step, slice) B tile; image [K-step][slice]
     static constexpr int BBYTES = NSB * KSTEPS * BTILE;
     static constexpr int QS = NP;                   // element stride in the state tile
-    static constexpr int KSTR = KPAD + 1;           // padded row stride of the staged A rows (odd)
+    // row stride of the staged A rows: even, so that column pairs are 8-byte
+    // loads, with KSTR/2 odd, so that the 8-byte loads of 16 consecutive
+    // rows fall in distinct banks
+    static constexpr int KSTR = KPAD + 2;
     static constexpr int MAX_WG = 4;                // warp groups per CTA (4 warps each), at most
     // shared memory layout (bytes)
     static constexpr int r16(int x) { return (x + 15) / 16 * 16; }
@@ -121,10 +124,11 @@ struct MixedShape {
     static constexpr bool OVERLAP = OUT_OWN || OUT_ALIAS;
     static constexpr int OFF_OUT = OUT_OWN ? OFF_OUT_OWN : OFF_Q;
     static constexpr int OFF_BAR = OUT_OWN ? r16(OFF_OUT + OUT_FLOATS * 4) : OFF_EB + NPAD * 4;
+    // [OFF_BAR, +16): the mbarrier, the tensor-memory base, the error flag
     static constexpr int HSTRIDE = r16(OFF_BAR + 16) - HBASE;         // bytes of one pipeline's region
     static constexpr int SMEM = HBASE + HALVES * HSTRIDE;
     // the shape runs when both tensor memory and shared memory suffice
-    static constexpr bool RUNS = FITS && SMEM <= 227 * 1024 && (HALVES == 1 || OVERLAP);
+    static constexpr bool RUNS = FITS && SMEM <= 227 * 1024 && OVERLAP;
     // the epilogue stages the tile's two output arrays in the A-row region
     static_assert(2 * NQ * ELEMS * NP <= 128 * KSTR, "output staging fits in the A-row region");
     static_assert(HALVES == 2 || SMEM <= 227 * 1024, "tile does not fit in shared memory");
@@ -133,6 +137,7 @@ struct MixedShape {
     // at least half of the SM's shared memory, so one CTA (the tensor-memory
     // owner) runs per SM
     static constexpr int SMEM_LAUNCH = SMEM < 118 * 1024 ? 118 * 1024 : SMEM;
+    static_assert(BBYTES <= 256 * 1024 - 16, "operator image descriptors stay inside the 14-bit address field");
 };
 
 // (hi, lo) = a + b exactly (Knuth two-sum).
@@ -177,6 +182,30 @@ __device__ __forceinline__ void slice_fixed(float x, float scale, float (&m)[NS]
     }
 }
 
+// slice_fixed for two values at once (paired FP32 instructions); slice s of
+// both values goes to w[s] as two BF16 halves (low = first value).
+template <int NS>
+__device__ __forceinline__ void slice_fixed_pair(dgtc::f32x2 x, dgtc::f32x2 scale, uint32_t (&w)[NS]) {
+    static_assert(NS == 3 || NS == 4, "three or four slices");
+    using namespace dgtc;
+    const f32x2 M0 = f2_splat(12582912.0f), M1 = f2_splat(24576.0f), M2 = f2_splat(48.0f);
+    f32x2 z = f2_fma(x, scale, M0);
+    f32x2 r = f2_fma(x, scale, f2_sub(M0, z));  // y - s0, exact
+    f32x2 m = f2_sub(z, M0);
+    w[0] = __byte_perm(f2_lo_bits(m), f2_hi_bits(m), 0x7632);
+    m = f2_sub(f2_add(r, M1), M1);
+    w[1] = __byte_perm(f2_lo_bits(m), f2_hi_bits(m), 0x7632);
+    r = f2_sub(r, m);
+    m = f2_sub(f2_add(r, M2), M2);
+    w[2] = __byte_perm(f2_lo_bits(m), f2_hi_bits(m), 0x7632);
+    if constexpr (NS == 4) {
+        const f32x2 M3 = f2_splat(0.09375f);
+        r = f2_sub(r, m);
+        m = f2_sub(f2_add(r, M3), M3);
+        w[3] = __byte_perm(f2_lo_bits(m), f2_hi_bits(m), 0x7632);
+    }
+}
+
 // Two values exactly representable in BF16, packed low = first, high =
 // second: their upper halves (a byte permute, no rounding needed).
 __device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
@@ -186,16 +215,18 @@ __device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
 // Slices CW tensor-memory columns of row arow, from column col on, into
 // the A parts and stores them at taddr (part p at taddr + p * ACOLS): BF16,
 // two K values per column, NS fixed-point slices with scale sc; 3xTF32,
-// one value per column, its TF32 high part and remainder.  Columns past KTOT
-// get zeros.
-template <int KIND, int NS, int KTOT, int ACOLS, int CW>
+// one value per column, its TF32 high part and remainder.  PADDED: the staged
+// rows hold zeros past KTOT and dead rows hold zeros (no guards; the BF16
+// path reads column pairs as 8-byte loads and slices them with paired
+// instructions); else columns past KTOT and rows that are not live get zeros.
+template <int KIND, int NS, int KTOT, int ACOLS, int CW, bool PADDED>
 __device__ __forceinline__ void slice_columns(const float *arow, bool live, float sc, int col, uint32_t taddr) {
     if constexpr (KIND == kTcTf32x3) {
         uint32_t wh[CW], wl[CW];
 #pragma unroll
         for (int h = 0; h < CW; ++h) {
             const int k = col + h;
-            const float x = (live && k < KTOT) ? arow[k] : 0.0f;
+            const float x = PADDED ? arow[k] : (live && k < KTOT) ? arow[k] : 0.0f;
             const float xh = dgtc::tf32_round(x);
             wh[h] = __float_as_uint(xh);
             wl[h] = __float_as_uint(dgtc::tf32_round(x - xh));
@@ -203,6 +234,20 @@ __device__ __forceinline__ void slice_columns(const float *arow, bool live, floa
         __syncwarp();
         dgtc::tmem_st_n<CW>(taddr, wh);
         dgtc::tmem_st_n<CW>(taddr + ACOLS, wl);
+    } else if constexpr (PADDED) {
+        uint32_t w[NS][CW];
+        const dgtc::f32x2 sc2 = dgtc::f2_splat(sc);
+#pragma unroll
+        for (int h = 0; h < CW; ++h) {
+            const float2 v = *reinterpret_cast<const float2 *>(&arow[2 * (col + h)]);
+            uint32_t ws[NS];
+            slice_fixed_pair<NS>(dgtc::f2_make(v.x, v.y), sc2, ws);
+#pragma unroll
+            for (int sl = 0; sl < NS; ++sl) w[sl][h] = ws[sl];
+        }
+        __syncwarp();
+#pragma unroll
+        for (int sl = 0; sl < NS; ++sl) dgtc::tmem_st_n<CW>(taddr + sl * ACOLS, w[sl]);
     } else {
         uint32_t w[NS][CW];
 #pragma unroll
@@ -230,9 +275,15 @@ __device__ __forceinline__ void issue_conn_copies(const MixedArgs &a, unsigned c
     using MS = MixedShape<DIM, P, KIND>;
     constexpr int NF = MS::NF, ELEMS = MS::ELEMS;
     int2 *sConn = reinterpret_cast<int2 *>(smem + MS::OFF_CONN + cb * MS::CONN_BYTES);
-    for (int idx = first; idx < ELEMS * NF; idx += stride) {
-        const bool ok = ebase + idx / NF < a.K;
-        dgtc::cp_async8(&sConn[idx], ok ? &a.conn[ebase * NF + idx] : a.conn, ok ? 8u : 0u);
+    static_assert(ELEMS * NF % 2 == 0, "a tile's connectivity words are whole 16-byte chunks");
+    if (ebase + ELEMS <= a.K && ((uintptr_t)a.conn & 15u) == 0) {
+        for (int idx = first; idx < ELEMS * NF / 2; idx += stride)
+            dgtc::cp_async16(&sConn[2 * idx], &a.conn[ebase * NF + 2 * idx], 16u);
+    } else {
+        for (int idx = first; idx < ELEMS * NF; idx += stride) {
+            const bool ok = ebase + idx / NF < a.K;
+            dgtc::cp_async8(&sConn[idx], ok ? &a.conn[ebase * NF + idx] : a.conn, ok ? 8u : 0u);
+        }
     }
 }
 
@@ -262,9 +313,15 @@ __device__ __forceinline__ void issue_tile_copies(const MixedArgs &a, unsigned c
             dgtc::cp_async4(&sQ[f * ELEMS * NP + rem], src, ok ? 4u : 0u);
         }
     }
-    for (int idx = first; idx < ELEMS * DIM * DIM; idx += stride) {
-        const bool ok = ebase + idx / (DIM * DIM) < a.K;
-        dgtc::cp_async4(&sGeo[idx], ok ? &a.geo[ebase * DIM * DIM + idx] : a.geo, ok ? 4u : 0u);
+    static_assert(ELEMS * DIM * DIM % 4 == 0, "a tile's geometry factors are whole 16-byte chunks");
+    if (ebase + ELEMS <= a.K && ((uintptr_t)a.geo & 15u) == 0) {
+        for (int idx = first; idx < ELEMS * DIM * DIM / 4; idx += stride)
+            dgtc::cp_async16(&sGeo[4 * idx], &a.geo[ebase * DIM * DIM + 4 * idx], 16u);
+    } else {
+        for (int idx = first; idx < ELEMS * DIM * DIM; idx += stride) {
+            const bool ok = ebase + idx / (DIM * DIM) < a.K;
+            dgtc::cp_async4(&sGeo[idx], ok ? &a.geo[ebase * DIM * DIM + idx] : a.geo, ok ? 4u : 0u);
+        }
     }
     for (int idx = first; idx < ELEMS * NF; idx += stride) {
         const bool ok = ebase + idx / NF < a.K;
@@ -411,24 +468,41 @@ __device__ __forceinline__ void build_rows(const MixedArgs &a, unsigned char *sm
     }
 }
 
-// Largest magnitude of each A row over NWG equal parts of its K range:
-// sMax[g*128 + r] for part g of row r (items (g, r) spread over the threads
-// first, first + stride, ...).
-template <int DIM, int P, int NWG, int KIND>
-__device__ __forceinline__ void row_maxima(unsigned char *smem, int first, int stride) {
+// The MMAs of K-steps [T0, T1) into the accumulator set at dacc, every
+// instruction unrolled with its operands known at compile time up to the
+// tensor-memory base and the operator image's descriptor (a loop over the
+// K-steps issues each tcgen05.mma at about half the rate).  3xTF32: per
+// K-step a_hi against [b_hi | b_lo] into both accumulators, then a_lo
+// against b_hi into the first.  Fixed-point slices: A slice i against B
+// slices 0..3-i into levels i..3; A slice 0 at K-step T0 starts all four
+// levels.
+template <int DIM, int P, int KIND, int T0, int T1>
+__device__ __forceinline__ void issue_mmas(uint32_t dacc, uint32_t tbase, uint64_t bd0) {
     using MS = MixedShape<DIM, P, KIND>;
-    constexpr int KTOT = MS::KTOT, KSTR = MS::KSTR;
-    constexpr int KP = (KTOT + NWG - 1) / NWG;
-    const float *sA = reinterpret_cast<const float *>(smem + MS::OFF_A);
-    float *sMax = reinterpret_cast<float *>(smem + MS::OFF_MAX);
-    for (int w = first; w < NWG * 128; w += stride) {
-        const int g = w >> 7, r = w & 127;
-        const int k0 = g * KP, k1 = min(k0 + KP, KTOT);
-        const float *arow = &sA[r * KSTR];
-        float m = 0.0f;
-        for (int k = k0; k < k1; ++k) m = fmaxf(m, fabsf(arow[k]));
-        sMax[w] = m;
+    constexpr int NPAD = MS::NPAD, ACOLS = MS::ACOLS;
+#pragma unroll
+    for (int t = T0; t < T1; ++t) {
+        // start address field (bits 0-13) in 16-byte units: the image stays
+        // below 256 KB, so adding the offset does not carry out of the field
+        const uint64_t bd = bd0 + (uint64_t)((t * MS::NSB * MS::BTILE) >> 4);
+        if constexpr (MS::TF) {
+            dgtc::mma_tf32_ts(dacc, tbase + t * 8, bd, dgtc::idesc_tf32_f32(128, 2 * NPAD), t > T0 ? 1u : 0u);
+            dgtc::mma_tf32_ts(dacc, tbase + ACOLS + t * 8, bd, dgtc::idesc_tf32_f32(128, NPAD), 1u);
+        } else {
+#pragma unroll
+            for (int ia = 0; ia < MS::NSA; ++ia)
+                dgtc::mma_bf16_ts(dacc + ia * NPAD, tbase + ia * ACOLS + t * 8, bd,
+                                  dgtc::idesc_bf16_f32(128, (MS::NSB - ia) * NPAD), (t > T0 || ia > 0) ? 1u : 0u);
+        }
     }
+}
+
+// N (4 or 8) consecutive tensor-memory columns of the warp's lanes.
+template <int N>
+__device__ __forceinline__ void ld_cols(uint32_t taddr, uint32_t (&v)[N]) {
+    static_assert(N == 4 || N == 8, "4 or 8 columns");
+    if constexpr (N == 8) dgtc::tmem_ld8(taddr, v);
+    else dgtc::tmem_ld4(taddr, v);
 }
 
 // Barrier of one tile pipeline: the whole CTA when it runs one pipeline, else
@@ -461,12 +535,15 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
     constexpr int CPG = (NCOL + NWG - 1) / NWG;
     static_assert(NWG * CPG <= ACOLS, "the warp groups' columns stay inside each A part");
     constexpr int NPP = (NP + NWG - 1) / NWG;           // output nodes per warp group in the epilogue
-    constexpr int NCH = (NPP + 7) / 8;                  // 8-column tensor-memory loads per accumulator
+    constexpr int EC = 8;                               // output nodes per tensor-memory load in the epilogue
+    constexpr int NCH = (NPP + EC - 1) / EC;            // loads per accumulator
     static_assert(MS::FITS, "tile does not fit in tensor memory");
     static_assert(NWG >= 1 && NWG <= MS::MAX_WG, "warp groups");
     constexpr int NX = MS::NX;
     constexpr bool OVERLAP = MS::OVERLAP;
-    static_assert(MS::ACC + (MS::NACC - 1) * NPAD + (NWG - 1) * NPP + 8 * NCH <= MS::TMEM_COLS,
+    constexpr int NBW = 4 * NWG - 1;                     // warps that build rows while the MMAs run
+    static_assert(OVERLAP, "the next tile's rows are built while the MMAs run");
+    static_assert(MS::ACC + (MS::NACC - 1) * NPAD + (NWG - 1) * NPP + EC * NCH <= MS::TMEM_COLS,
                   "epilogue loads stay inside the allocation");
     static_assert(ELEMS <= 64, "curved-element mask holds 64 elements per tile");
     extern __shared__ __align__(1024) unsigned char smem_cta[];
@@ -475,8 +552,12 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
     const int pipe = HALVES == 1 ? 0 : (int)(threadIdx.x / NT);
     const int tid = (int)threadIdx.x - pipe * NT, warp = tid >> 5, lane = tid & 31;
     unsigned char *const smem = smem_cta + pipe * MS::HSTRIDE;
-    // named barriers of this pipeline: all its threads, and all but warp 0
+    // named barriers of this pipeline: all its threads, and the row builders
     const int bar_all = 1 + 2 * pipe, bar_rest = 2 + 2 * pipe;
+    // the row builders (every warp but warp 0, which issues the MMAs) and
+    // their index
+    const bool builder = warp != 0;
+    const int bidx = tid - 32;
     float *sA = reinterpret_cast<float *>(smem + MS::OFF_A);
     float *sMax = reinterpret_cast<float *>(smem + MS::OFF_MAX);
     uint8_t *sTab = smem + MS::OFF_TAB;
@@ -500,6 +581,14 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
         for (int k = threadIdx.x; k < MS::BBYTES / 16; k += NTC) dst[k] = src[k];
         for (int k = tid; k < Shape<DIM, P>::NTAB; k += NT) sTab[k] = a.tabs[k];
         for (int k = tid; k < NPAD; k += NT) sEb[k] = a.beb[k];
+        // the A-row staging holds zeros past KTOT and in the rows past the
+        // tile's (field, element) rows; no phase writes there afterwards (the
+        // epilogue stages its outputs in a region of their own or in the
+        // state-tile and neighbour-trace regions)
+        for (int k = tid; k < 128 * MS::KSTR; k += NT) {
+            const int rr = k / MS::KSTR, kk = k - rr * MS::KSTR;
+            if (kk >= KTOT || rr >= NQ * ELEMS) sA[k] = 0.0f;
+        }
     }
     dgtc::fence_proxy_async_smem();
     dgtc::fence_before_sync();
@@ -566,24 +655,19 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
         pipe_sync<HALVES>(bar_all, NT);
         issue_neighbour_copies<DIM, P, KIND>(a, smem, eb, mo, 0, tid, NT);
         dgtc::cp_async_commit();
-        if constexpr (OVERLAP) {
-            // the first tile's rows now; every later tile's while its
-            // predecessor's MMAs run
-            dgtc::cp_async_wait_all();
-            pipe_sync<HALVES>(bar_all, NT);
-            const long long T1 = tfirst + tstride;
-            if (T1 < ntiles) {
-                long long e1, m1;
-                tile_base(T1, e1, m1);
-                issue_conn_copies<DIM, P, KIND>(a, smem, e1, 1, tid, NT);
-            }
-            dgtc::cp_async_commit();
-            build_rows<DIM, P, KIND>(a, smem, eb, 0, tid, NT);
-            pipe_sync<HALVES>(bar_all, NT);
-            // the row maxima of every later tile are taken right after its
-            // rows, while the previous tile's MMAs run (3xTF32 needs none)
-            if constexpr (!MS::TF) row_maxima<DIM, P, NWG, KIND>(smem, tid, NT);
+        // the first tile's rows now; every later tile's while its
+        // predecessor's MMAs run
+        dgtc::cp_async_wait_all();
+        pipe_sync<HALVES>(bar_all, NT);
+        const long long T1 = tfirst + tstride;
+        if (T1 < ntiles) {
+            long long e1, m1;
+            tile_base(T1, e1, m1);
+            issue_conn_copies<DIM, P, KIND>(a, smem, e1, 1, tid, NT);
         }
+        dgtc::cp_async_commit();
+        build_rows<DIM, P, KIND>(a, smem, eb, 0, tid, NT);
+        pipe_sync<HALVES>(bar_all, NT);
     }
     int cb = 0;  // connectivity buffer of the current tile
     for (long long tile = tfirst; tile < ntiles && alive; tile += tstride, cb ^= 1) {
@@ -592,19 +676,10 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
         const long long next = tile + tstride;
         long long nebase = 0, nmoff = 0;
         if (next < ntiles) tile_base(next, nebase, nmoff);
-        if constexpr (!OVERLAP) {
-            dgtc::cp_async_wait_all();
-            pipe_sync<HALVES>(bar_all, NT);
-            if (next < ntiles) issue_conn_copies<DIM, P, KIND>(a, smem, nebase, cb ^ 1, tid, NT);
-            dgtc::cp_async_commit();
-            build_rows<DIM, P, KIND>(a, smem, ebase, cb, tid, NT);
-            pipe_sync<HALVES>(bar_all, NT);
-        }
         // the tile's element data are consumed: start copying the next tile's
-        // (with the overlap, warp 0 copies nothing for the next tile: it only
-        // issues the MMAs while the other warps consume these copies)
-        if (next < ntiles && (!OVERLAP || warp > 0))
-            issue_tile_copies<DIM, P, KIND>(a, smem, nebase, nmoff, vec, OVERLAP ? tid - 32 : tid, OVERLAP ? NT - 32 : NT);
+        // (the row builders, which wait for these copies; the MMA issuers
+        // copy nothing for the next tile)
+        if (next < ntiles && builder) issue_tile_copies<DIM, P, KIND>(a, smem, nebase, nmoff, vec, bidx, NBW * 32);
         dgtc::cp_async_commit();
         // this thread's connectivity copies of the next tile are complete (only
         // the group just committed may still be pending); the barrier after
@@ -628,17 +703,21 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
             }
         }
         const float *arow = &sA[r * KSTR];
-        if constexpr (!OVERLAP && !MS::TF) {
-            constexpr int KP = (KTOT + NWG - 1) / NWG;
+        if constexpr (!MS::TF) {
+            // largest magnitude of this thread's slicing columns of row r (the
+            // staged rows hold zeros past KTOT); the barrier below publishes it
+            const float2 *ap = reinterpret_cast<const float2 *>(arow);
             float m = 0.0f;
-            if (row_ok)
-                for (int k = part * KP; k < part * KP + KP && k < KTOT; ++k) m = fmaxf(m, fabsf(arow[k]));
+#pragma unroll 4
+            for (int c = part * CPG; c < part * CPG + CPG; ++c) {
+                const float2 v = ap[c];
+                m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+            }
             sMax[part * 128 + r] = m;
         }
         pipe_sync<HALVES>(bar_all, NT);
-        if (next < ntiles && (!OVERLAP || warp > 0))
-            issue_neighbour_copies<DIM, P, KIND>(a, smem, nebase, nmoff, cb ^ 1, OVERLAP ? tid - 32 : tid,
-                                           OVERLAP ? NT - 32 : NT);
+        if (next < ntiles && builder)
+            issue_neighbour_copies<DIM, P, KIND>(a, smem, nebase, nmoff, cb ^ 1, bidx, NBW * 32);
         dgtc::cp_async_commit();
         int ea = 0;
         bool live = row_ok;
@@ -654,71 +733,43 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
             sc = live ? exp2i(8 - ea) : 0.0f;
         }
         // 3 (cont.). warp group g slices columns [g*CPG, (g+1)*CPG) of the
-        // row's tensor-memory columns in chunks of eight
+        // row's tensor-memory columns in chunks of CH
         {
+            constexpr int CH = 8;
             const int col0 = part * CPG;
             const uint32_t ta = dgtc::tmem_lane_addr(tbase, warp, col0);
 #pragma unroll 1
-            for (int c = 0; c < CPG / 8; ++c)
-                slice_columns<KIND, MS::NSA, KTOT, ACOLS, 8>(arow, live, sc, col0 + 8 * c, ta + 8 * c);
-            if constexpr (CPG % 8 > 0)
-                slice_columns<KIND, MS::NSA, KTOT, ACOLS, CPG % 8>(arow, live, sc, col0 + CPG / 8 * 8,
-                                                                    ta + CPG / 8 * 8);
+            for (int c = 0; c < CPG / CH; ++c)
+                slice_columns<KIND, MS::NSA, KTOT, ACOLS, CH, true>(arow, live, sc, col0 + CH * c, ta + CH * c);
+            if constexpr (CPG % CH > 0)
+                slice_columns<KIND, MS::NSA, KTOT, ACOLS, CPG % CH, true>(arow, live, sc, col0 + CPG / CH * CH,
+                                                                           ta + CPG / CH * CH);
         }
         dgtc::tmem_st_wait();
         dgtc::fence_before_sync();
         pipe_sync<HALVES>(bar_all, NT);
 
-        // 4. tensor-core contraction, issued by thread 0 K-step by K-step
+        // 4. tensor-core contraction, issued by thread 0 (unrolled)
         if (tid == 0 && !*sFail) {
             dgtc::fence_after_sync();
-            if constexpr (MS::TF) {
-                // per K-step: a_hi against [b_hi | b_lo] into both
-                // accumulators, then a_lo against b_hi into the first
-#pragma unroll 1
-                for (int t = 0; t < KSTEPS; ++t) {
-                    const uint64_t bd = dgtc::desc_kmajor(sB + t * MS::NSB * MS::BTILE, 128, 256);
-                    dgtc::mma_tf32_ts(tbase + MS::ACC, tbase + t * 8, bd, dgtc::idesc_tf32_f32(128, 2 * NPAD),
-                                      t > 0 ? 1u : 0u);
-                    dgtc::mma_tf32_ts(tbase + MS::ACC, tbase + ACOLS + t * 8, bd, dgtc::idesc_tf32_f32(128, NPAD),
-                                      1u);
-                }
-            } else {
-                // A slice i against B slices 0..3-i into levels i..3; A slice
-                // 0 at K-step 0 starts all four levels
-#pragma unroll 1
-                for (int t = 0; t < KSTEPS; ++t) {
-                    const uint64_t bd = dgtc::desc_kmajor(sB + t * MS::NSB * MS::BTILE, 128, 256);
-#pragma unroll
-                    for (int ia = 0; ia < MS::NSA; ++ia)
-                        dgtc::mma_bf16_ts(tbase + MS::ACC + ia * NPAD, tbase + ia * ACOLS + t * 8, bd,
-                                          dgtc::idesc_bf16_f32(128, (MS::NSB - ia) * NPAD),
-                                          (t > 0 || ia > 0) ? 1u : 0u);
-                }
-            }
+            issue_mmas<DIM, P, KIND, 0, KSTEPS>(tbase + MS::ACC, tbase, dgtc::desc_kmajor(sB, 128, 256));
             dgtc::mma_commit(bar);
         }
         __syncwarp();
-        if constexpr (OVERLAP) {
-            // while warp 0 issues the MMAs and they run, warps 1.. build the
-            // next tile's rows (barrier 1 spans those warps only)
-            if (next < ntiles && warp > 0) {
-                dgtc::cp_async_wait_all();
-                asm volatile("bar.sync %0, %1;" ::"r"(bar_rest), "r"(NT - 32) : "memory");
-                const long long next2 = next + tstride;
-                if (next2 < ntiles) {
-                    long long e2, m2;
-                    tile_base(next2, e2, m2);
-                    issue_conn_copies<DIM, P, KIND>(a, smem, e2, cb, tid - 32, NT - 32);
-                }
-                build_rows<DIM, P, KIND>(a, smem, nebase, cb ^ 1, tid - 32, NT - 32);
-                if constexpr (!MS::TF) {
-                    asm volatile("bar.sync %0, %1;" ::"r"(bar_rest), "r"(NT - 32) : "memory");
-                    row_maxima<DIM, P, NWG, KIND>(smem, tid - 32, NT - 32);
-                }
+        // while warp 0 issues the MMAs and they run, the other warps build the
+        // next tile's rows (barrier bar_rest spans those warps only)
+        if (next < ntiles && builder) {
+            dgtc::cp_async_wait_all();
+            asm volatile("bar.sync %0, %1;" ::"r"(bar_rest), "r"(NBW * 32) : "memory");
+            const long long next2 = next + tstride;
+            if (next2 < ntiles) {
+                long long e2, m2;
+                tile_base(next2, e2, m2);
+                issue_conn_copies<DIM, P, KIND>(a, smem, e2, cb, bidx, NBW * 32);
             }
-            dgtc::cp_async_commit();
+            build_rows<DIM, P, KIND>(a, smem, nebase, cb ^ 1, bidx, NBW * 32);
         }
+        dgtc::cp_async_commit();
 
         // 5. epilogue: accumulators -> stage increment, RK4 stage update;
         //    warp group g takes output nodes [g*NPP, (g+1)*NPP)
@@ -729,51 +780,39 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
             alive = false;
         } else {
             dgtc::fence_after_sync();
-            uint32_t v0[8 * NCH], v1[8 * NCH];
-            float v2[8 * NCH];  // sum of the accumulators of the pairs with i+j >= 2
+            // outputs go through shared memory so that the global stores are
+            // whole-tile vectors; the accumulators are read eight output
+            // nodes at a time
+            float *sO0 = reinterpret_cast<float *>(smem + MS::OFF_OUT);  // acc, or the new low part
+            float *sO1 = sO0 + NQ * ELEMS * NP;   // next stage input / new state
+            const float sdt = live ? a.dt * exp2i(ea - 16) : 0.0f;
+            static_assert(NX <= 2, "at most two accumulators past the first two");
 #pragma unroll
             for (int c = 0; c < NCH; ++c) {
-                dgtc::tmem_ld8(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 0 * NPAD + i0 + 8 * c), v0 + 8 * c);
-                dgtc::tmem_ld8(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 1 * NPAD + i0 + 8 * c), v1 + 8 * c);
-            }
+                uint32_t v0[EC], v1[EC], vx[NX > 0 ? NX : 1][EC];
+                const int cc = i0 + EC * c;
+                ld_cols<EC>(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 0 * NPAD + cc), v0);
+                ld_cols<EC>(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + 1 * NPAD + cc), v1);
 #pragma unroll
-            for (int k = 0; k < 8 * NCH; ++k) v2[k] = 0.0f;
-            if constexpr (NX == 0) dgtc::tmem_ld_wait();
-            // the extra accumulators, four at a time
-#pragma unroll
-            for (int x0 = 0; x0 < NX; x0 += 4) {
-                uint32_t vx[4][8 * NCH];
-#pragma unroll
-                for (int x = 0; x < 4; ++x)
-                    if (x0 + x < NX)
-#pragma unroll
-                        for (int c = 0; c < NCH; ++c)
-                            dgtc::tmem_ld8(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + (2 + x0 + x) * NPAD + i0 + 8 * c),
-                                           vx[x] + 8 * c);
+                for (int x = 0; x < NX; ++x) ld_cols<EC>(dgtc::tmem_lane_addr(tbase, warp, MS::ACC + (2 + x) * NPAD + cc), vx[x]);
                 dgtc::tmem_ld_wait();
+                if (!row_ok) continue;
 #pragma unroll
-                for (int x = 0; x < 4; ++x)
-                    if (x0 + x < NX)
-#pragma unroll
-                        for (int k = 0; k < 8 * NCH; ++k) v2[k] += __uint_as_float(vx[x][k]);
-            }
-            // outputs go through shared memory (the A-row region, free since
-            // the slicing) so that the global stores are whole-tile vectors
-            float *sO0 = OVERLAP ? reinterpret_cast<float *>(smem + MS::OFF_OUT) : sA;  // acc, or the new low part
-            float *sO1 = sO0 + NQ * ELEMS * NP;   // next stage input / new state
-            if (row_ok) {
-                const float sdt = live ? a.dt * exp2i(ea - 16) : 0.0f;
-#pragma unroll
-                for (int t = 0; t < NPP; ++t) {
+                for (int h = 0; h < EC; ++h) {
+                    const int t = EC * c + h;
                     const int i = i0 + t;
-                    if (i >= NP) break;
+                    if (t >= NPP || i >= NP) break;
                     float rr;
                     if constexpr (MS::TF) {
-                        rr = a.dt * (__uint_as_float(v0[t]) + __uint_as_float(v1[t]));
+                        rr = a.dt * (__uint_as_float(v0[h]) + __uint_as_float(v1[h]));
                     } else {
+                        // levels 2 and 3 (the pairs with i+j >= 2)
+                        float v2 = 0.0f;
+#pragma unroll
+                        for (int x = 0; x < NX; ++x) v2 += __uint_as_float(vx[x][h]);
                         float hi, lo;
-                        two_sum(__uint_as_float(v0[t]), __uint_as_float(v1[t]), hi, lo);
-                        lo += v2[t];
+                        two_sum(__uint_as_float(v0[h]), __uint_as_float(v1[h]), hi, lo);
+                        lo += v2;
                         const float scl = sdt * exp2i(sEb[i]);
                         rr = fmaf(scl, hi, scl * lo);
                     }

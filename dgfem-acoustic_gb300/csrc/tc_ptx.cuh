@@ -263,6 +263,32 @@ __device__ __forceinline__ float ld_early(const float *p) {
     return v;
 }
 
+// Two FP32 values in one 64-bit register (low half = first): Blackwell's
+// paired FP32 instructions (add/sub/mul/fma .rn.f32x2) act on both halves
+// with the rounding of the scalar instructions, at one instruction per pair.
+using f32x2 = unsigned long long;
+__device__ __forceinline__ f32x2 f2_make(float lo, float hi) {
+    return ((f32x2)__float_as_uint(hi) << 32) | (f32x2)__float_as_uint(lo);
+}
+__device__ __forceinline__ f32x2 f2_splat(float v) { return f2_make(v, v); }
+__device__ __forceinline__ uint32_t f2_lo_bits(f32x2 v) { return (uint32_t)v; }
+__device__ __forceinline__ uint32_t f2_hi_bits(f32x2 v) { return (uint32_t)(v >> 32); }
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
 // Two BF16 values (exactly representable) packed low = first, high = second.
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     uint32_t a = __float_as_uint(lo) >> 16, b = __float_as_uint(hi) >> 16;
