@@ -858,7 +858,11 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
             }
         }
         dgtc::fence_before_sync();
-        pipe_sync<HALVES>(bar_all, NT);
+        // with the outputs staged in a region of their own, the next tile
+        // reaches that region only after several barriers; staged in the
+        // state-tile region (3D P4), they must be read before the next tile's
+        // copies refill it
+        if constexpr (!MS::OUT_OWN) pipe_sync<HALVES>(bar_all, NT);
     }
     // no copy may still be writing shared memory when the CTA exits
     dgtc::cp_async_wait_all();
