@@ -773,18 +773,21 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
 
         // 5. epilogue: accumulators -> stage increment, RK4 stage update;
         //    warp group g takes output nodes [g*NPP, (g+1)*NPP)
-        if (!dgtc::mbar_wait_bounded(bar, phase, 1u << 30)) *sFail = 1;
+        // every thread waits for the MMAs itself; a failure is published by
+        // the staging barrier below, after which every thread reads the flag
+        const bool mma_done = dgtc::mbar_wait_bounded(bar, phase, 1u << 30);
+        if (!mma_done) *sFail = 1;
         phase ^= 1u;
-        pipe_sync<HALVES>(bar_all, NT);
-        if (*sFail) {
-            alive = false;
-        } else {
-            dgtc::fence_after_sync();
-            // outputs go through shared memory so that the global stores are
-            // whole-tile vectors; the accumulators are read eight output
-            // nodes at a time
-            float *sO0 = reinterpret_cast<float *>(smem + MS::OFF_OUT);  // acc, or the new low part
-            float *sO1 = sO0 + NQ * ELEMS * NP;   // next stage input / new state
+        // outputs staged in the state-tile region (3D P4): every row builder
+        // must have finished reading it first
+        if constexpr (!MS::OUT_OWN) pipe_sync<HALVES>(bar_all, NT);
+        dgtc::fence_after_sync();
+        // outputs go through shared memory so that the global stores are
+        // whole-tile vectors; the accumulators are read eight output nodes at
+        // a time
+        float *sO0 = reinterpret_cast<float *>(smem + MS::OFF_OUT);  // acc, or the new low part
+        float *sO1 = sO0 + NQ * ELEMS * NP;   // next stage input / new state
+        if (mma_done) {
             const float sdt = live ? a.dt * exp2i(ea - 16) : 0.0f;
             static_assert(NX <= 2, "at most two accumulators past the first two");
 #pragma unroll
@@ -837,7 +840,11 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
                     }
                 }
             }
-            pipe_sync<HALVES>(bar_all, NT);
+        }
+        pipe_sync<HALVES>(bar_all, NT);
+        if (*sFail) {
+            alive = false;
+        } else {
             const unsigned long long cm = MASKED ? a.cmask[ebase / ELEMS] : 0ull;
             if (vec && ebase + ELEMS <= a.K && cm == 0ull) {
                 constexpr int W = ELEMS * NP / 4;
