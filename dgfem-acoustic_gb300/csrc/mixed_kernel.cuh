@@ -552,8 +552,8 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
     const int pipe = HALVES == 1 ? 0 : (int)(threadIdx.x / NT);
     const int tid = (int)threadIdx.x - pipe * NT, warp = tid >> 5, lane = tid & 31;
     unsigned char *const smem = smem_cta + pipe * MS::HSTRIDE;
-    // named barriers of this pipeline: all its threads, and the row builders
-    const int bar_all = 1 + 2 * pipe, bar_rest = 2 + 2 * pipe;
+    // named barrier of this pipeline (all its threads)
+    const int bar_all = 1 + pipe;
     // the row builders (every warp but warp 0, which issues the MMAs) and
     // their index
     const bool builder = warp != 0;
@@ -746,6 +746,9 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
                                                                            ta + CPG / CH * CH);
         }
         dgtc::tmem_st_wait();
+        // the next tile's element data and neighbour traces (this thread's
+        // copies): complete now, published by the barrier to the row builders
+        dgtc::cp_async_wait_all();
         dgtc::fence_before_sync();
         pipe_sync<HALVES>(bar_all, NT);
 
@@ -757,10 +760,8 @@ __global__ void __launch_bounds__(128 * NWG * HALVES, 1) mixed_stage_kernel(cons
         }
         __syncwarp();
         // while warp 0 issues the MMAs and they run, the other warps build the
-        // next tile's rows (barrier bar_rest spans those warps only)
+        // next tile's rows
         if (next < ntiles && builder) {
-            dgtc::cp_async_wait_all();
-            asm volatile("bar.sync %0, %1;" ::"r"(bar_rest), "r"(NBW * 32) : "memory");
             const long long next2 = next + tstride;
             if (next2 < ntiles) {
                 long long e2, m2;
