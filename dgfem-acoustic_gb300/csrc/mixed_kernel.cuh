@@ -22,18 +22,20 @@
 // double-FP32, scales by 2^(ea+eb-16) dt and applies the RK4 stage update
 // with the state u kept as an FP32 pair.
 //
-// Roles (128*NWG threads, one CTA per SM, persistent over tiles): cp.async copies
-// bring a tile's state, geometry, connectivity and neighbour traces into
-// shared memory one tile ahead; all threads build the A rows in shared memory
-// (one task per element node for the volume fluxes, one per face slot for the
-// face values).
-// Row r is then sliced by lane r%32 of warps r/32 + 4g of every warp group g
+// Roles (128*NWG threads, one CTA per SM, persistent over tiles): cp.async
+// copies bring a tile's state, geometry, connectivity and neighbour traces
+// into shared memory one tile ahead; warps 1.. build the next tile's A rows
+// in shared memory (one task per element node for the volume fluxes, one per
+// face slot for the face values) while warp 0 issues this tile's MMAs.
+// Row r is sliced by lane r%32 of warps r/32 + 4g of every warp group g
 // (warp w may only touch tensor-memory lanes 32(w%4)..32(w%4)+31), each
-// group taking an equal share of the row's tensor-memory columns, and stored
-// with tcgen05.st.  One
-// thread issues the tcgen05.mma and commits them to an mbarrier;
-// the warp groups then read the accumulators of their row with tcgen05.ld,
-// split by output node, for the epilogue.  Every wait is bounded; on timeout the kernel records an error,
+// group taking an equal share of the row's tensor-memory columns (and the
+// largest magnitude of its share, for the row's exponent), two values at a
+// time with paired FP32 instructions, and stored with tcgen05.st.  One
+// thread issues the tcgen05.mma as one unrolled sequence and commits them to
+// an mbarrier; every thread waits on it, and the warp groups read the
+// accumulators of their row with tcgen05.ld, split by output node, for the
+// epilogue.  Every wait is bounded; on timeout the kernel records an error,
 // waits once more for the MMAs in flight, frees tensor memory and stops.
 #pragma once
 #include <cuda_runtime.h>
