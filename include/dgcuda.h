@@ -106,7 +106,7 @@ typedef struct dg_phys_desc {
 } dg_phys_desc;
 
 typedef struct dg_opts {
-    int precision;   /* DG_PREC_FP64 | DG_PREC_FP32 */
+    int precision;   /* DG_PREC_FP64 | DG_PREC_FP32 | DG_PREC_MIXED | DG_PREC_TF32X3 */
     int flux_sign;   /* DG_FLUX_REFERENCE | DG_FLUX_UPWIND */
     int device;      /* CUDA device ordinal */
     int use_graph;   /* capture step chunks in CUDA graphs (1) or launch directly (0) */
