@@ -83,4 +83,15 @@ struct dg_ctx {
     cudaEvent_t snap_ready[2] = {nullptr, nullptr}, snap_done[2] = {nullptr, nullptr};
     long long save_ticket[2] = {-1, -1};
     long long save_next = 0;
+    // staged state uploads (dg_stage_state / dg_commit_state): host-to-device
+    // copies into a two-slot ring of FP64 device buffers on a side stream;
+    // the commit converts a slot into the state on the solver stream.
+    // load_ticket[s] = last ticket staged on slot s (-1: none); load_used[s]
+    // is recorded by the commit that reads slot s (load_used_set[s])
+    cudaStream_t load_stream = nullptr;
+    double *d_load[2] = {nullptr, nullptr};
+    cudaEvent_t load_done[2] = {nullptr, nullptr}, load_used[2] = {nullptr, nullptr};
+    bool load_used_set[2] = {false, false};
+    long long load_ticket[2] = {-1, -1};
+    long long load_next = 0;
 };

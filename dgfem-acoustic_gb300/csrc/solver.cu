@@ -203,10 +203,18 @@ void free_ctx(dg_ctx *c) {
         cudaStreamSynchronize(c->save_stream);
         cudaStreamDestroy(c->save_stream);
     }
+    if (c->load_stream) {
+        // staged copies from the caller's buffers may still be in flight
+        cudaStreamSynchronize(c->load_stream);
+        cudaStreamDestroy(c->load_stream);
+    }
     for (int k = 0; k < 2; ++k) {
         if (c->snap_ready[k]) cudaEventDestroy(c->snap_ready[k]);
         if (c->snap_done[k]) cudaEventDestroy(c->snap_done[k]);
         if (c->d_snap[k]) cudaFree(c->d_snap[k]);
+        if (c->load_done[k]) cudaEventDestroy(c->load_done[k]);
+        if (c->load_used[k]) cudaEventDestroy(c->load_used[k]);
+        if (c->d_load[k]) cudaFree(c->d_load[k]);
     }
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     for (auto ev : c->events) cudaEventDestroy(ev);
@@ -821,6 +829,63 @@ int get_state_async(dg_ctx *c, double *host, long long *ticket) {
     return DG_OK;
 }
 
+// Starts the host-to-device copy of a whole state (member 0, fields one after
+// the other, FP64) into a staging slot on the load stream; dg_commit_state
+// makes it the state.
+int stage_state(dg_ctx *c, const double *host, long long *ticket) {
+    if (!c || !host || !ticket) return fail(DG_ERR_ARG, "null argument");
+    CK(cudaSetDevice(c->device));
+    if (!c->load_stream) {
+        CK(cudaStreamCreateWithFlags(&c->load_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            CK(cudaEventCreateWithFlags(&c->load_done[k], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&c->load_used[k], cudaEventDisableTiming));
+        }
+    }
+    const int slot = (int)(c->load_next % 2);
+    const size_t bytes = (size_t)c->nq * c->ndof * 8;
+    if (!c->d_load[slot]) {
+        cudaError_t e = cudaMalloc(&c->d_load[slot], bytes);
+        if (e != cudaSuccess) {
+            c->d_load[slot] = nullptr;
+            return fail(DG_ERR_NOMEM, std::string("cudaMalloc(staging): ") + cudaGetErrorString(e));
+        }
+    }
+    // the commit that last read this slot must have run first
+    if (c->load_used_set[slot]) CK(cudaStreamWaitEvent(c->load_stream, c->load_used[slot], 0));
+    CK(cudaMemcpyAsync(c->d_load[slot], host, bytes, cudaMemcpyHostToDevice, c->load_stream));
+    CK(cudaEventRecord(c->load_done[slot], c->load_stream));
+    c->load_ticket[slot] = c->load_next;
+    *ticket = c->load_next++;
+    return DG_OK;
+}
+
+// Makes a staged state the state of member 0: on the solver stream, after
+// the staged copy and after the work already enqueued there.
+int commit_state(dg_ctx *c, long long ticket) {
+    if (!c) return fail(DG_ERR_ARG, "null context");
+    if (ticket < 0 || ticket >= c->load_next) return fail(DG_ERR_ARG, "unknown ticket");
+    const int slot = (int)(ticket % 2);
+    if (c->load_ticket[slot] != ticket) return fail(DG_ERR_ARG, "ticket overwritten by a later staged state");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamWaitEvent(c->stream, c->load_done[slot], 0));
+    const double *src = c->d_load[slot];
+    for (int f = 0; f < c->nq; ++f) {
+        const long long off = f * c->ndof;
+        char *dst = (char *)c->d_u + off * c->rsize;
+        if (c->prec == DG_PREC_FP64)
+            CK(cudaMemcpyAsync(dst, src + off, (size_t)c->ndof * 8, cudaMemcpyDeviceToDevice, c->stream));
+        else if (c->mixed)
+            split_kernel<<<1024, 256, 0, c->stream>>>(src + off, (float *)dst, c->d_ulo + off, c->ndof);
+        else
+            cast_kernel<float><<<1024, 256, 0, c->stream>>>(src + off, (float *)dst, c->ndof);
+        CK(cudaGetLastError());
+    }
+    CK(cudaEventRecord(c->load_used[slot], c->stream));
+    c->load_used_set[slot] = true;
+    return DG_OK;
+}
+
 int wait_state(dg_ctx *c, long long ticket) {
     if (!c) return fail(DG_ERR_ARG, "null context");
     if (ticket < 0 || ticket >= c->save_next) return fail(DG_ERR_ARG, "unknown ticket");
@@ -894,6 +959,8 @@ int dg_get_state(dg_ctx *c, double *const u[4]) { return get_member(c, 0, u); }
 int dg_get_state_async(dg_ctx *c, double *host, long long *ticket) { return get_state_async(c, host, ticket); }
 
 int dg_wait_state(dg_ctx *c, long long ticket) { return wait_state(c, ticket); }
+int dg_stage_state(dg_ctx *c, const double *host, long long *ticket) { return stage_state(c, host, ticket); }
+int dg_commit_state(dg_ctx *c, long long ticket) { return commit_state(c, ticket); }
 
 int dg_set_state_member(dg_ctx *c, int member, const double *const u[4]) { return set_member(c, member, u); }
 

@@ -146,6 +146,8 @@ def _declare(L: C.CDLL) -> None:
         "dg_error_vs": (C.c_int, [vp, C.c_int, vp, C.c_int, P_d, C.POINTER(C.c_longlong)]),
         "dg_get_state_async": (C.c_int, [vp, P_d, C.POINTER(C.c_longlong)]),
         "dg_wait_state": (C.c_int, [vp, C.c_longlong]),
+        "dg_stage_state": (C.c_int, [vp, P_d, C.POINTER(C.c_longlong)]),
+        "dg_commit_state": (C.c_int, [vp, C.c_longlong]),
         "dg_synchronize": (C.c_int, [vp]),
         "dg_info": (C.c_int, [vp, C.POINTER(C.c_longlong), P_i, C.POINTER(C.c_longlong)]),
         "dg_curved_info": (C.c_int, [vp, P_i, P_i, P_i]),
@@ -651,6 +653,23 @@ class Solver:
 
     def wait_state(self, ticket: int) -> None:
         _check(lib().dg_wait_state(self._h, ticket))
+
+    def stage_state(self, u: np.ndarray) -> int:
+        """Starts the upload of u ([4][ndof] float64, contiguous, ideally in
+        pinned memory: see pinned_array) into a staging buffer and returns a
+        ticket for commit_state; u must stay unchanged until the commit has
+        run (a later step or synchronize returns after it)."""
+        if not (isinstance(u, np.ndarray) and u.dtype == np.float64 and u.shape == (4, self.ndof)
+                and u.flags["C_CONTIGUOUS"]):
+            raise ValueError(f"state must be a contiguous float64 array of shape (4, {self.ndof})")
+        t = C.c_longlong()
+        _check(lib().dg_stage_state(self._h, _dptr(u), C.byref(t)))
+        return t.value
+
+    def commit_state(self, ticket: int) -> None:
+        """Makes a staged state the state of member 0, after the work already
+        enqueued and before any later work."""
+        _check(lib().dg_commit_state(self._h, ticket))
 
     def error_vs(self, ref: "Solver", member: int = 0, ref_member: int = 0) -> tuple[list[float], int]:
         """FP64 relative L2 error per field of this context's state (batch

@@ -151,6 +151,22 @@ int dg_get_state(dg_ctx *ctx, double *const u[4]);
 int dg_get_state_async(dg_ctx *ctx, double *host, long long *ticket);
 int dg_wait_state(dg_ctx *ctx, long long ticket);
 
+/* Staged state upload (the counterpart of dg_get_state_async for a caller
+ * that feeds a new state every step): dg_stage_state starts the copy of
+ * host[4*num_el*el_num_nodes] (fields p, vx, vy, vz one after the other; vz
+ * is ignored in 2D and not checked) into a device staging buffer on a side
+ * stream and returns at once with a ticket; dg_commit_state(ticket) makes
+ * that copy the state of member 0, in stream order: after the work already
+ * enqueued (the steps before it see the old state) and before any work
+ * enqueued later.  A stage called before the previous step lets the copy
+ * cross the host link while that step runs.  host must stay unchanged until
+ * the commit has run (a later dg_rk4_steps, dg_get_state or dg_synchronize
+ * returns after it), and should be pinned (dg_host_alloc) for the copy to
+ * overlap.  Two staged states can wait; a third stage reuses the oldest
+ * slot (committing an overwritten ticket is DG_ERR_ARG). */
+int dg_stage_state(dg_ctx *ctx, const double *host, long long *ticket);
+int dg_commit_state(dg_ctx *ctx, long long ticket);
+
 /* Hard sources: for source s, nodes dof_idx[offsets[s] .. offsets[s+1]) get
  * p = amp*sin(2*pi*freq*t + phase) while t < duration, at the start of each
  * step.  params[s*4 + 0..3] = amp, freq, phase, duration.  Later sources

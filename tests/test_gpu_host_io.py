@@ -97,3 +97,44 @@ def test_async_copy_out_frames_equal_blocking_copies(prec):
         assert np.array_equal(outs[k], want[k]), k
     with pytest.raises(D.DGError):
         a.wait_state(99)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "mixed"])
+def test_staged_state_uploads_equal_blocking_uploads(prec):
+    """dg_stage_state copies a state to the device on a side stream and
+    dg_commit_state makes it the state in stream order: each step sequence
+    fed through stage/commit (the next input staged before the current step
+    runs, one input pageable, a third stage reusing the first slot) equals,
+    bit for bit, the same sequence fed through the blocking dg_set_state;
+    committing an overwritten or unknown ticket is an error."""
+    mesh = D.Mesh.box_tet(3, 2, 2, order=3, side_names=("Absorbing", "Reflecting") * 3)
+    pre = D.Precomp(mesh)
+    v0 = (50.0, 0.0, 0.0)
+    dt = D.cfl_dt(pre, 340.0, v0)
+    rng = np.random.default_rng(11)
+    ins = [D.pinned_array((4, pre.ndof)), D.pinned_array((4, pre.ndof)), np.empty((4, pre.ndof))]
+    for k, u in enumerate(ins):
+        u[:] = pre.initial_state([(0, 0.3 + 0.2 * k, 0.5, 0.5, 0.02, 1.0)]) + 1e-3 * rng.standard_normal((4, pre.ndof))
+    a = D.Solver(pre, 340.0, 1.225, v0, precision=prec, flux="upwind")
+    b = D.Solver(pre, 340.0, 1.225, v0, precision=prec, flux="upwind")
+    got, want = [], []
+    tk = a.stage_state(ins[0])
+    t = tb = 0.0
+    for k in range(3):
+        a.commit_state(tk)
+        if k + 1 < 3:
+            tk = a.stage_state(ins[k + 1])  # crosses the host link while step k runs
+        t = a.rk4_steps(t, dt, 4)
+        got.append(a.get_state().copy())
+        b.set_state(ins[k])
+        tb = b.rk4_steps(tb, dt, 4)
+        want.append(b.get_state().copy())
+    for k in range(3):
+        assert np.array_equal(got[k], want[k]), k
+    old = a.stage_state(ins[0])
+    a.stage_state(ins[1])
+    a.stage_state(ins[2])  # the third stage reuses the slot of the first
+    with pytest.raises(D.DGError):
+        a.commit_state(old)
+    with pytest.raises(D.DGError):
+        a.commit_state(99)
