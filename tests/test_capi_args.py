@@ -184,3 +184,19 @@ def test_noalloc_rejects_states_beyond_capacity():
     code = D.lib().dg_rk4_steps_noalloc(C.byref(dl), C.c_void_p(4096), C.byref(tt), 1e-6, 1, None)
     assert code == -3
     assert b"capacity" in D.lib().dg_last_error()
+
+
+def test_state_transfer_entry_points_refuse_null_arguments():
+    """The overlapped state transfers check their arguments before any device
+    call: a null context, host array or ticket pointer is DG_ERR_ARG with a
+    message (no GPU needed)."""
+    lib = D.lib()
+    host = np.zeros(16)
+    t = C.c_longlong()
+    for code in (lib.dg_stage_state(None, host.ctypes.data_as(D.P_d), C.byref(t)),
+                 lib.dg_stage_state(None, None, C.byref(t)),
+                 lib.dg_commit_state(None, 0),
+                 lib.dg_get_state_async(None, host.ctypes.data_as(D.P_d), C.byref(t)),
+                 lib.dg_wait_state(None, 0)):
+        assert code == DG_ERR_ARG
+        assert lib.dg_last_error()
